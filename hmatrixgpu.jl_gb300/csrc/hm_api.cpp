@@ -1,0 +1,448 @@
+// C ABI of libhmgpu: H-matrix objects, import of the reference's flattened
+// layout, the product entry points and the info/export queries.
+#include <chrono>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "hm_api.h"
+
+namespace hm {
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(HMGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+HMatrix::~HMatrix() { release(); }
+
+void HMatrix::release() {
+  for (void *p : dev_allocs) cudaFree(p);
+  dev_allocs.clear();
+}
+
+int HMatrix::dalloc(void **p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HMGPU_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                     cudaGetErrorString(e));
+  }
+  dev_allocs.push_back(*p);
+  device_bytes += static_cast<int64_t>(bytes);
+  return HMGPU_OK;
+}
+
+void HMatrix::dfree(void *p) {
+  if (!p) return;
+  for (size_t i = 0; i < dev_allocs.size(); i++)
+    if (dev_allocs[i] == p) {
+      dev_allocs.erase(dev_allocs.begin() + i);
+      break;
+    }
+  cudaFree(p);
+}
+
+template <typename V>
+static int upload(HMatrix &H, V **dst, const std::vector<V> &src) {
+  int rc = H.dalloc(reinterpret_cast<void **>(dst), src.size() * sizeof(V));
+  if (rc) return rc;
+  if (src.empty()) return HMGPU_OK;
+  cudaError_t e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(V), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? HMGPU_OK : cuda_fail(e, "cudaMemcpy");
+}
+
+// Builds the product layout from the block set and the FP64 row-major factors
+// held on the device (d64: dense, u64/v64: low-rank; per-block offsets).
+int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
+                    const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
+                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen) {
+  const bool f64 = H.opt.precision == HMGPU_F64;
+  const bool comp = !f64 && H.opt.compensated;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, H.device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
+  H.num_sms = prop.multiProcessorCount;
+  H.grid_v = H.num_sms * occupancy_v(f64);
+  H.grid_du = H.num_sms * occupancy_du(f64, comp);
+  const int vec = f64 ? 2 : 4;
+  make_plan(H.bs, vec, H.grid_v * (kThreads / 32), dense_src_off, u_src_off, H.plan);
+  const Plan &p = H.plan;
+  const size_t es = f64 ? 8 : 4;
+  int rc;
+  if ((rc = H.dalloc(&H.panels, p.panel_len * es))) return rc;
+  if ((rc = H.dalloc(&H.vdata, p.v_len * es))) return rc;
+  if ((rc = H.dalloc(&H.xt, p.xt_len * es))) return rc;
+  cudaMemset(H.xt, 0, p.xt_len * es);
+  cudaMemset(H.vdata, 0, p.v_len * es);
+  if ((rc = upload(H, &H.dp.tiles, p.tiles))) return rc;
+  if ((rc = upload(H, &H.dp.order, p.order))) return rc;
+  if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
+  if ((rc = upload(H, &H.dp.vunits, p.vunits))) return rc;
+  if ((rc = upload(H, &H.dp.warp_begin, p.warp_begin))) return rc;
+  std::vector<int32_t> t0(H.bs.m), s0(H.bs.n);
+  for (int64_t i = 0; i < H.bs.m; i++) t0[i] = static_cast<int32_t>(H.bs.tmap[i] - 1);
+  for (int64_t j = 0; j < H.bs.n; j++) s0[j] = static_cast<int32_t>(H.bs.smap[j] - 1);
+  if ((rc = upload(H, &H.dp.tmap0, t0))) return rc;
+  if ((rc = upload(H, &H.dp.smap0, s0))) return rc;
+  if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.counter), 64))) return rc;
+  cudaMemset(H.dp.counter, 0, 64);
+  H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
+  H.dp.nwarps = p.nwarps;
+  H.dp.m = H.bs.m;
+  H.dp.n = H.bs.n;
+  H.dp.x_len = p.x_len;
+  H.dp.xt_len = p.xt_len;
+
+  // pack panels
+  PackJob *djobs = nullptr;
+  if ((rc = upload(H, &djobs, p.pjobs))) return rc;
+  e = launch_pack_panels(f64, djobs, static_cast<int64_t>(p.pjobs.size()), d64, u64, H.panels, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "pack panels");
+  if (gen) {
+    rc = gen->generate(H, djobs, static_cast<int64_t>(p.pjobs.size()));
+    if (rc) return rc;
+  }
+  // pack V rows
+  std::vector<VPackJob> vj;
+  for (size_t a = 0; a < H.bs.a_r.size(); a++) {
+    if (H.bs.a_r[a] == 0) continue;
+    VPackJob j;
+    j.src_off = v_src_off[a];
+    j.dst_off = p.v_off[a];
+    j.n = H.bs.a_ce[a] - H.bs.a_cs[a];
+    j.r = H.bs.a_r[a];
+    j.stride = p.v_stride[a];
+    j.phase = p.v_phase[a];
+    vj.push_back(j);
+  }
+  VPackJob *dvj = nullptr;
+  if ((rc = upload(H, &dvj, vj))) return rc;
+  e = launch_pack_v(f64, dvj, static_cast<int64_t>(vj.size()), v64, H.vdata, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "pack V");
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "layout packing");
+  H.dfree(djobs);
+  H.dfree(dvj);
+  H.device_bytes -= static_cast<int64_t>(p.pjobs.size() * sizeof(PackJob) + vj.size() * sizeof(VPackJob));
+  return HMGPU_OK;
+}
+
+int HMatrix::ensure_io(size_t xbytes, size_t ybytes) {
+  int rc;
+  if (xbytes > io_x_bytes) {
+    dfree(io_x);
+    io_x = nullptr;
+    io_x_bytes = 0;
+    if ((rc = dalloc(&io_x, xbytes))) return rc;
+    io_x_bytes = xbytes;
+  }
+  if (ybytes > io_y_bytes) {
+    dfree(io_y);
+    io_y = nullptr;
+    io_y_bytes = 0;
+    if ((rc = dalloc(&io_y, ybytes))) return rc;
+    io_y_bytes = ybytes;
+  }
+  return HMGPU_OK;
+}
+
+}  // namespace hm
+
+using hm::HMatrix;
+
+// ---------------------------------------------------------------------------
+// import of the reference's flattened HMatrix{Float64}
+// ---------------------------------------------------------------------------
+static int check_perm(const int64_t *map, int64_t len, const char *name) {
+  if (len > 0 && !map) return hm::fail(HMGPU_ERR_INVALID, std::string(name) + " is NULL");
+  std::vector<char> seen(len, 0);
+  for (int64_t i = 0; i < len; i++) {
+    int64_t v = map[i];
+    if (v < 1 || v > len || seen[v - 1])
+      return hm::fail(HMGPU_ERR_INVALID, std::string(name) + " is not a permutation of 1:" +
+                                             std::to_string(len) + " (entry " +
+                                             std::to_string(i + 1) + " = " + std::to_string(v) + ")");
+    seen[v - 1] = 1;
+  }
+  return HMGPU_OK;
+}
+
+static int copy_table(const int64_t *src, int64_t count, std::vector<int64_t> &dst) {
+  dst.resize(count);
+  if (count == 0) return HMGPU_OK;
+  cudaError_t e = cudaMemcpy(dst.data(), src, count * sizeof(int64_t), cudaMemcpyDefault);
+  return e == cudaSuccess ? HMGPU_OK : hm::cuda_fail(e, "reading an index table");
+}
+
+extern "C" int hmgpu_hmatrix_import_flat(const hmgpu_options *opt, int64_t m, int64_t n,
+                                         const int64_t *target_map, const int64_t *source_map,
+                                         const int64_t *dense_idx, int64_t nD,
+                                         const double *dense_data, int64_t dense_len,
+                                         const int64_t *U_idx, int64_t nA, const double *U_data,
+                                         int64_t U_len, const int64_t *V_idx, int64_t R,
+                                         const double *V_data, int64_t V_len,
+                                         hmgpu_hmatrix **out) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (!out) return hm::fail(HMGPU_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (m <= 0 || n <= 0 || m >= (int64_t(1) << 31) || n >= (int64_t(1) << 31))
+    return hm::fail(HMGPU_ERR_INVALID, "matrix size out of range");
+  if (nD < 0 || nA < 0 || R < 0 || dense_len < 0 || U_len < 0 || V_len < 0)
+    return hm::fail(HMGPU_ERR_INVALID, "negative count");
+  hmgpu_options o{HMGPU_F32, 0, 0, 0};
+  if (opt) o = *opt;
+  if (o.precision != HMGPU_F64 && o.precision != HMGPU_F32 && o.precision != HMGPU_MIXED)
+    return hm::fail(HMGPU_ERR_INVALID, "unknown precision mode");
+
+  std::vector<int64_t> tm, sm, di, ui, vi;
+  int rc;
+  if ((rc = copy_table(target_map, m, tm)) || (rc = copy_table(source_map, n, sm)) ||
+      (rc = copy_table(dense_idx, 5 * nD, di)) || (rc = copy_table(U_idx, 5 * nA, ui)) ||
+      (rc = copy_table(V_idx, 3 * R, vi)))
+    return rc;
+  if ((rc = check_perm(tm.data(), m, "target_index_map"))) return rc;
+  if ((rc = check_perm(sm.data(), n, "source_index_map"))) return rc;
+
+  auto H = std::make_unique<HMatrix>();
+  H->opt = o;
+  cudaGetDevice(&H->device);
+  hm::BlockSet &bs = H->bs;
+  bs.m = m;
+  bs.n = n;
+  bs.tmap = tm;
+  bs.smap = sm;
+  std::vector<int64_t> dsrc(nD), usrc(nA), vsrc(nA);
+  for (int64_t b = 0; b < nD; b++) {
+    const int64_t *d = &di[5 * b];
+    if (d[0] < 1 || d[1] < d[0] || d[1] > m || d[2] < 1 || d[3] < d[2] || d[3] > n)
+      return hm::fail(HMGPU_ERR_INVALID, "dense block " + std::to_string(b + 1) + " has an invalid range");
+    int64_t len = (d[1] - d[0] + 1) * (d[3] - d[2] + 1);
+    if (d[4] < 0 || d[4] + len > dense_len)
+      return hm::fail(HMGPU_ERR_INVALID, "dense block " + std::to_string(b + 1) + " offset out of range");
+    bs.d_rs.push_back(static_cast<int32_t>(d[0] - 1));
+    bs.d_re.push_back(static_cast<int32_t>(d[1]));
+    bs.d_cs.push_back(static_cast<int32_t>(d[2] - 1));
+    bs.d_ce.push_back(static_cast<int32_t>(d[3]));
+    dsrc[b] = d[4];
+  }
+  int64_t next_row = 1;
+  for (int64_t b = 0; b < nA; b++) {
+    const int64_t *u = &ui[5 * b];
+    if (u[0] < 1 || u[1] < u[0] || u[1] > m)
+      return hm::fail(HMGPU_ERR_INVALID, "low-rank block " + std::to_string(b + 1) + " has an invalid row range");
+    int64_t r = u[3] - u[2] + 1;
+    if (u[2] != next_row || r < 0 || u[3] > R)
+      return hm::fail(HMGPU_ERR_INVALID, "low-rank block " + std::to_string(b + 1) +
+                                              " has an invalid Vx range (rows 3-4 of U_block_indices)");
+    next_row += r;
+    int64_t mb = u[1] - u[0] + 1;
+    if (u[4] < 0 || u[4] + mb * r > U_len)
+      return hm::fail(HMGPU_ERR_INVALID, "low-rank block " + std::to_string(b + 1) + " U offset out of range");
+    int64_t cs = -1, ce = -1, voff = 0;
+    if (r > 0) {
+      const int64_t *v = &vi[3 * (u[2] - 1)];
+      cs = v[0];
+      ce = v[1];
+      voff = v[2];
+      if (cs < 1 || ce < cs || ce > n)
+        return hm::fail(HMGPU_ERR_INVALID, "V_block_indices has an invalid column range");
+      int64_t nb = ce - cs + 1;
+      for (int64_t k = 0; k < r; k++) {
+        const int64_t *vk = &vi[3 * (u[2] - 1 + k)];
+        if (vk[0] != cs || vk[1] != ce || vk[2] != voff + k * nb)
+          return hm::fail(HMGPU_ERR_INVALID, "V_block_indices rows of low-rank block " +
+                                                  std::to_string(b + 1) + " are inconsistent");
+      }
+      if (voff < 0 || voff + r * nb > V_len)
+        return hm::fail(HMGPU_ERR_INVALID, "low-rank block " + std::to_string(b + 1) + " V offset out of range");
+    } else {
+      cs = 1;  // a rank-0 block contributes nothing; its columns are irrelevant
+      ce = 1;
+    }
+    bs.a_rs.push_back(static_cast<int32_t>(u[0] - 1));
+    bs.a_re.push_back(static_cast<int32_t>(u[1]));
+    bs.a_cs.push_back(static_cast<int32_t>(cs - 1));
+    bs.a_ce.push_back(static_cast<int32_t>(ce));
+    bs.a_r.push_back(static_cast<int32_t>(r));
+    usrc[b] = u[4];
+    vsrc[b] = voff;
+  }
+  if (next_row - 1 != R)
+    return hm::fail(HMGPU_ERR_INVALID, "sum of ranks differs from the V table length");
+
+  // upload the FP64 factors, then re-lay them out
+  double *d64 = nullptr, *u64 = nullptr, *v64 = nullptr;
+  if ((rc = H->dalloc(reinterpret_cast<void **>(&d64), dense_len * 8)) ||
+      (rc = H->dalloc(reinterpret_cast<void **>(&u64), U_len * 8)) ||
+      (rc = H->dalloc(reinterpret_cast<void **>(&v64), V_len * 8)))
+    return rc;
+  cudaError_t e = cudaSuccess;
+  if (dense_len) e = cudaMemcpy(d64, dense_data, dense_len * 8, cudaMemcpyDefault);
+  if (e == cudaSuccess && U_len) e = cudaMemcpy(u64, U_data, U_len * 8, cudaMemcpyDefault);
+  if (e == cudaSuccess && V_len) e = cudaMemcpy(v64, V_data, V_len * 8, cudaMemcpyDefault);
+  if (e != cudaSuccess) return hm::cuda_fail(e, "copying factor data");
+  if ((rc = hm::finalize_layout(*H, d64, dsrc, u64, usrc, v64, vsrc, nullptr))) return rc;
+  H->dfree(d64);
+  H->device_bytes -= dense_len * 8;
+  if (o.keep_factors) {
+    H->u64 = u64;
+    H->v64 = v64;
+    H->u_src_off = usrc;
+    H->v_src_off = vsrc;
+  } else {
+    H->dfree(u64);
+    H->dfree(v64);
+    H->device_bytes -= (U_len + V_len) * 8;
+  }
+  H->build_seconds =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  *out = reinterpret_cast<hmgpu_hmatrix *>(H.release());
+  return HMGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// product
+// ---------------------------------------------------------------------------
+extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nrhs, int64_t ldx,
+                            int64_t ldy, void *stream) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  if (nrhs < 0) return hm::fail(HMGPU_ERR_INVALID, "nrhs < 0");
+  if (nrhs == 0) return HMGPU_OK;
+  if (!x || !y) return hm::fail(HMGPU_ERR_INVALID, "x or y is NULL");
+  if (ldx < H.bs.n || ldy < H.bs.m) return hm::fail(HMGPU_ERR_INVALID, "leading dimension too small");
+  const bool f64 = H.opt.precision == HMGPU_F64;
+  const bool comp = !f64 && (H.opt.compensated || H.opt.precision == HMGPU_MIXED);
+  const size_t es = f64 ? 8 : 4;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (int64_t k = 0; k < nrhs; k++) {
+    cudaError_t e = hm::launch_matvec(f64, comp, H.dp, H.panels, H.vdata, H.xt,
+                                      static_cast<const char *>(x) + k * ldx * es,
+                                      static_cast<char *>(y) + k * ldy * es, H.grid_v, H.grid_du, s);
+    if (e != cudaSuccess) return hm::cuda_fail(e, "matvec launch");
+  }
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_matvec_host(hmgpu_hmatrix *h, const void *x, void *y, int64_t nrhs,
+                                 int64_t ldx, int64_t ldy) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  if (nrhs < 0 || ldx < H.bs.n || ldy < H.bs.m) return hm::fail(HMGPU_ERR_INVALID, "bad sizes");
+  if (nrhs == 0) return HMGPU_OK;
+  const size_t es = H.opt.precision == HMGPU_F64 ? 8 : 4;
+  int rc = H.ensure_io(nrhs * H.bs.n * es, nrhs * H.bs.m * es);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy2D(H.io_x, H.bs.n * es, x, ldx * es, H.bs.n * es, nrhs, cudaMemcpyDefault);
+  if (e != cudaSuccess) return hm::cuda_fail(e, "copying x to the device");
+  rc = hmgpu_matvec(h, H.io_x, H.io_y, nrhs, H.bs.n, H.bs.m, nullptr);
+  if (rc) return rc;
+  e = cudaMemcpy2D(y, ldy * es, H.io_y, H.bs.m * es, H.bs.m * es, nrhs, cudaMemcpyDefault);
+  if (e != cudaSuccess) return hm::cuda_fail(e, "copying y to the host");
+  return HMGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// queries
+// ---------------------------------------------------------------------------
+extern "C" int hmgpu_hmatrix_info(const hmgpu_hmatrix *h, hmgpu_info *info) {
+  if (!h || !info) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
+  const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);
+  const hm::BlockSet &b = H.bs;
+  std::memset(info, 0, sizeof *info);
+  info->m = b.m;
+  info->n = b.n;
+  info->n_dense = static_cast<int64_t>(b.d_rs.size());
+  info->n_approx = static_cast<int64_t>(b.a_rs.size());
+  int64_t rmin = 0, rmax = 0, dmin = 0, dmax = 0, rt = 0;
+  for (size_t a = 0; a < b.a_r.size(); a++) {
+    if (a == 0 || b.a_r[a] < rmin) rmin = b.a_r[a];
+    if (a == 0 || b.a_r[a] > rmax) rmax = b.a_r[a];
+    rt += b.a_r[a];
+  }
+  for (size_t d = 0; d < b.d_rs.size(); d++) {
+    int64_t s = static_cast<int64_t>(b.d_re[d] - b.d_rs[d]) * (b.d_ce[d] - b.d_cs[d]);
+    if (d == 0 || s < dmin) dmin = s;
+    if (d == 0 || s > dmax) dmax = s;
+  }
+  info->min_rank = rmin;
+  info->max_rank = rmax;
+  info->min_dense_size = dmin;
+  info->max_dense_size = dmax;
+  info->total_rank = rt;
+  info->dense_entries = H.plan.dense_entries;
+  info->far_entries = H.plan.far_entries;
+  double comp = static_cast<double>(H.plan.dense_entries + H.plan.far_entries);
+  info->compression_ratio = comp > 0 ? static_cast<double>(b.m) * b.n / comp : 0.0;
+  const int64_t es = H.opt.precision == HMGPU_F64 ? 8 : 4;
+  info->matrix_bytes = (H.plan.panel_len + H.plan.v_len) * es;
+  info->device_bytes = H.device_bytes;
+  info->n_tiles = static_cast<int64_t>(H.plan.tiles.size());
+  info->precision = H.opt.precision;
+  info->build_seconds = H.build_seconds;
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_blocks(const hmgpu_hmatrix *h, int64_t *dense_idx,
+                                    int64_t *approx_idx) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  const hm::BlockSet &b = reinterpret_cast<const HMatrix *>(h)->bs;
+  if (dense_idx)
+    for (size_t d = 0; d < b.d_rs.size(); d++) {
+      dense_idx[4 * d] = b.d_rs[d] + 1;
+      dense_idx[4 * d + 1] = b.d_re[d];
+      dense_idx[4 * d + 2] = b.d_cs[d] + 1;
+      dense_idx[4 * d + 3] = b.d_ce[d];
+    }
+  if (approx_idx)
+    for (size_t a = 0; a < b.a_rs.size(); a++) {
+      approx_idx[5 * a] = b.a_rs[a] + 1;
+      approx_idx[5 * a + 1] = b.a_re[a];
+      approx_idx[5 * a + 2] = b.a_cs[a] + 1;
+      approx_idx[5 * a + 3] = b.a_ce[a];
+      approx_idx[5 * a + 4] = b.a_r[a];
+    }
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_index_maps(const hmgpu_hmatrix *h, int64_t *tmap, int64_t *smap) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  const hm::BlockSet &b = reinterpret_cast<const HMatrix *>(h)->bs;
+  if (tmap) std::memcpy(tmap, b.tmap.data(), b.tmap.size() * sizeof(int64_t));
+  if (smap) std::memcpy(smap, b.smap.data(), b.smap.size() * sizeof(int64_t));
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_block_factors(const hmgpu_hmatrix *h, int64_t blk, double *U,
+                                           double *V) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);
+  if (!H.u64) return hm::fail(HMGPU_ERR_UNSUPPORTED, "factors were not kept (keep_factors = 0)");
+  const hm::BlockSet &b = H.bs;
+  if (blk < 0 || blk >= static_cast<int64_t>(b.a_r.size()))
+    return hm::fail(HMGPU_ERR_INVALID, "block index out of range");
+  int64_t mb = b.a_re[blk] - b.a_rs[blk], nb = b.a_ce[blk] - b.a_cs[blk], r = b.a_r[blk];
+  cudaError_t e = cudaSuccess;
+  if (U && mb * r) e = cudaMemcpy(U, H.u64 + H.u_src_off[blk], mb * r * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && V && nb * r)
+    e = cudaMemcpy(V, H.v64 + H.v_src_off[blk], nb * r * 8, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? HMGPU_OK : hm::cuda_fail(e, "copying factors");
+}
+
+extern "C" int hmgpu_hmatrix_aca_ranks(const hmgpu_hmatrix *h, int64_t *aca_rank,
+                                       int64_t *final_rank) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  const hm::BlockSet &b = reinterpret_cast<const HMatrix *>(h)->bs;
+  if (aca_rank && !b.aca_rank.empty())
+    std::memcpy(aca_rank, b.aca_rank.data(), b.aca_rank.size() * sizeof(int64_t));
+  if (final_rank && !b.final_rank.empty())
+    std::memcpy(final_rank, b.final_rank.data(), b.final_rank.size() * sizeof(int64_t));
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_free(hmgpu_hmatrix *h) {
+  delete reinterpret_cast<HMatrix *>(h);
+  return HMGPU_OK;
+}

@@ -1,0 +1,51 @@
+// The H-matrix object behind the opaque hmgpu_hmatrix handle.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "hm_device.h"
+
+namespace hm {
+
+struct HMatrix;
+
+// Fills panel columns of kind-2 pack jobs (dense blocks generated on the device).
+struct DenseGenerator {
+  virtual ~DenseGenerator() = default;
+  virtual int generate(HMatrix &H, const PackJob *djobs, int64_t njobs) = 0;
+};
+
+struct HMatrix {
+  int device = 0;
+  hmgpu_options opt{HMGPU_F32, 0, 0, 0};
+  BlockSet bs;
+  Plan plan;
+  DevPlan dp;
+  void *panels = nullptr;  // tile panels, element type of the mode
+  void *vdata = nullptr;   // V rows
+  void *xt = nullptr;      // XT = [x permuted | t]
+  int num_sms = 0, grid_v = 0, grid_du = 0;
+  // kept FP64 factors (keep_factors)
+  double *u64 = nullptr, *v64 = nullptr;
+  std::vector<int64_t> u_src_off, v_src_off;
+  // staging of hmgpu_matvec_host
+  void *io_x = nullptr, *io_y = nullptr;
+  size_t io_x_bytes = 0, io_y_bytes = 0;
+  double build_seconds = 0.0;
+  int64_t device_bytes = 0;
+  std::vector<void *> dev_allocs;
+
+  ~HMatrix();
+  void release();
+  int dalloc(void **p, size_t bytes);
+  void dfree(void *p);
+  int ensure_io(size_t xbytes, size_t ybytes);
+};
+
+int cuda_fail(cudaError_t e, const char *what);
+int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
+                    const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
+                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen);
+
+}  // namespace hm

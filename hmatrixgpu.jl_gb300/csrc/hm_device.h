@@ -1,0 +1,46 @@
+// Device-side launchers of libhmgpu (implemented in the .cu files).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "hm_internal.h"
+
+namespace hm {
+
+// Device copies of a Plan plus the per-product scratch.
+struct DevPlan {
+  TileDesc *tiles = nullptr;
+  int32_t *order = nullptr;
+  Seg *segs = nullptr;
+  int32_t ntiles = 0;
+  VUnit *vunits = nullptr;
+  int32_t *warp_begin = nullptr;
+  int32_t nwarps = 0;
+  int32_t *tmap0 = nullptr;  // 0-based target map, length m
+  int32_t *smap0 = nullptr;  // 0-based source map, length n
+  int32_t *counter = nullptr;  // tile ticket of the near/U pass
+  int64_t m = 0, n = 0, x_len = 0, xt_len = 0;
+};
+
+constexpr int kThreads = 256;  // threads per CTA of the product kernels
+
+// Resident CTAs per SM of the V pass and of the near/U pass for an element type.
+int occupancy_v(bool f64);
+int occupancy_du(bool f64, bool comp);
+
+// One product y = H x (single right-hand side) on `stream`:
+//   x permutation into XT, V pass (t = V x), near/U pass (y = D x + U t).
+cudaError_t launch_matvec(bool f64, bool comp, const DevPlan &p, const void *panels,
+                          const void *vdata, void *xt, const void *x, void *y, int grid_v,
+                          int grid_du, cudaStream_t stream);
+
+// Packing of FP64 row-major block factors into the product layout.
+cudaError_t launch_pack_panels(bool f64, const PackJob *jobs, int64_t njobs, const double *dsrc,
+                               const double *usrc, void *panels, cudaStream_t stream);
+struct VPackJob {
+  int64_t src_off, dst_off;
+  int32_t n, r, stride, phase;
+};
+cudaError_t launch_pack_v(bool f64, const VPackJob *jobs, int64_t njobs, const double *vsrc,
+                          void *vdata, cudaStream_t stream);
+
+}  // namespace hm

@@ -1,0 +1,132 @@
+// Internal declarations shared by the host (.cpp) and device (.cu) parts of libhmgpu.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/hmgpu.h"
+
+namespace hm {
+
+// ---- errors -----------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+
+// ---- cluster tree (src/tree.jl) --------------------------------------------------
+struct Node {
+  int64_t start, end;  // 1-based start, exclusive end, scaled by dims
+  int64_t left, right; // children, -1 for none
+  double center[3];
+  double radius;
+  bool leaf;
+};
+
+struct Tree {
+  int64_t npts = 0, dims = 1;
+  std::vector<int64_t> index_map;  // 1-based, length dims*npts
+  std::vector<Node> nodes;         // pre-order
+};
+
+int build_tree(const double *coords, int64_t npts, int64_t leaf, int64_t dims, Tree &t);
+
+// ---- block tree (src/block.jl) ---------------------------------------------------
+struct BNode {
+  int32_t x, y;         // target node, source node
+  int32_t left, right;  // children, -1 for none
+  bool adm, dense;
+};
+
+struct Blocks {
+  std::vector<BNode> nodes;
+  std::vector<int32_t> dense;   // pairs (x, y)
+  std::vector<int32_t> approx;  // pairs (x, y)
+};
+
+void build_blocks(const Tree &X, const Tree &Y, double eta, bool merge, Blocks &b);
+
+// ---- the assembled block structure ------------------------------------------------
+// Block ranges are 0-based and half-open in permuted index space.
+struct BlockSet {
+  int64_t m = 0, n = 0;
+  std::vector<int64_t> tmap, smap;  // 1-based, as the reference
+  // dense blocks, reference order
+  std::vector<int32_t> d_rs, d_re, d_cs, d_ce;
+  // low-rank blocks, reference order
+  std::vector<int32_t> a_rs, a_re, a_cs, a_ce, a_r;
+  // per admissible leaf of the block tree (builds only)
+  std::vector<int64_t> aca_rank, final_rank;
+};
+
+// ---- matvec layout ------------------------------------------------------------------
+// A row tile is a run of permuted rows that every block either covers or misses.
+// Its panel stores, column-major, all columns that touch those rows: the
+// columns of the covering dense blocks (vector entries from the permuted x)
+// and the rank columns of the covering low-rank blocks (entries from t = V x).
+struct TileDesc {
+  int64_t data_off;  // element offset of the panel (multiple of the 16-byte vector)
+  int32_t row0;      // first permuted row
+  int32_t m;         // rows
+  int32_t ncols;     // columns
+  int32_t seg0;      // first segment
+  int32_t nseg;      // segment count
+  int32_t pad;
+};
+static_assert(sizeof(TileDesc) == 32, "TileDesc layout");
+
+// A run of panel columns whose vector entries are contiguous in XT = [x_perm | t].
+struct Seg {
+  int32_t col0, ncols, vec_off, pad;
+};
+
+// A unit of the V pass: rows [0, nrows) of one low-rank block, each row a
+// phase-aligned run of `stride` elements dotted with XT[x_off : x_off+stride).
+struct VUnit {
+  int64_t v_off;   // element offset of the first row
+  int32_t stride;  // row stride in elements (multiple of the vector width)
+  int32_t nrows;
+  int32_t x_off;   // XT offset (aligned) matching stored position 0
+  int32_t t_off;   // XT offset of the first output
+  int32_t lanes;   // lanes per row (power of two <= 32)
+  int32_t pad;
+};
+static_assert(sizeof(VUnit) == 32, "VUnit layout");
+
+// Copy job of the packing pass: a row-major source slice -> column-major panel.
+struct PackJob {
+  int64_t src_off;   // element offset in the source array
+  int64_t dst_off;   // element offset in the panel array
+  int32_t src_ld;    // source row stride
+  int32_t ncols;
+  int32_t m;         // rows
+  int32_t kind;      // 0 dense source, 1 U source, 2 dense generated from the kernel
+  int32_t row0;      // generated: first permuted row
+  int32_t col0;      // generated: first permuted column
+};
+
+struct Plan {
+  int vec = 4;            // elements per 16-byte vector
+  int64_t x_len = 0;      // XT x-region length (>= n + 4, multiple of vec)
+  int64_t R = 0;          // total rank
+  int64_t xt_len = 0;     // x_len + R rounded up
+  std::vector<TileDesc> tiles;
+  std::vector<int32_t> order;  // tiles by decreasing work
+  std::vector<Seg> segs;
+  int64_t panel_len = 0;
+  std::vector<PackJob> pjobs;
+  // V pass
+  std::vector<int64_t> v_off, t_off;  // per low-rank block
+  std::vector<int32_t> v_stride, v_phase;
+  std::vector<VUnit> vunits;
+  std::vector<int32_t> warp_begin;  // nwarps + 1
+  int nwarps = 0;
+  int64_t v_len = 0;
+  // bytes
+  int64_t dense_entries = 0, far_entries = 0;
+};
+
+// Builds the layout for a block set; `src_*_off` are per-block offsets of the
+// row-major FP64 source factors (dense blocks: -1 when generated from a kernel).
+void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_t> &dense_src_off,
+               const std::vector<int64_t> &u_src_off, Plan &p);
+
+}  // namespace hm

@@ -1,0 +1,212 @@
+// Host-side planning of the device layout used by the H-matrix product.
+//
+// The reference's device product (src/mult.jl:41-146) scans every block
+// descriptor for every row.  Here the structure is resolved once, at build
+// time, into:
+//   * row tiles: maximal runs of permuted rows that every block either fully
+//     covers or misses (at most kMaxTileRows rows each).  Each tile owns its
+//     rows of y, which makes the product deterministic without atomics;
+//   * one column-major panel per tile holding every column that touches those
+//     rows (dense-block columns, then low-rank U columns), with a list of
+//     segments telling where each column's vector entry lives in XT = [x | t];
+//   * the V factors row by row, each row phase-aligned with the permuted x so
+//     that a 16-byte load of V pairs with a 16-byte load of x;
+//   * a static, byte-balanced split of the V rows over the resident warps.
+#include <algorithm>
+#include <numeric>
+
+#include "hm_internal.h"
+
+namespace hm {
+
+static constexpr int kMaxTileRows = 128;
+static constexpr int64_t kVUnitBytes = 64 * 1024;
+
+static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_t> &dense_src_off,
+               const std::vector<int64_t> &u_src_off, Plan &p) {
+  const int esize = 16 / vec;
+  p = Plan();
+  p.vec = vec;
+  const int64_t m = bs.m, n = bs.n;
+  const size_t nd = bs.d_rs.size(), na = bs.a_rs.size();
+  p.x_len = round_up(n + 4, vec);
+
+  // ---- t offsets (ranks, reference order) -----------------------------------
+  p.t_off.assign(na, 0);
+  int64_t R = 0;
+  for (size_t b = 0; b < na; b++) {
+    p.t_off[b] = p.x_len + R;
+    R += bs.a_r[b];
+  }
+  p.R = R;
+  p.xt_len = round_up(p.x_len + R, vec);
+
+  // ---- row tiles --------------------------------------------------------------
+  std::vector<int32_t> cuts;
+  cuts.reserve(2 * (nd + na) + 2);
+  cuts.push_back(0);
+  cuts.push_back(static_cast<int32_t>(m));
+  for (size_t b = 0; b < nd; b++) {
+    cuts.push_back(bs.d_rs[b]);
+    cuts.push_back(bs.d_re[b]);
+  }
+  for (size_t b = 0; b < na; b++) {
+    cuts.push_back(bs.a_rs[b]);
+    cuts.push_back(bs.a_re[b]);
+  }
+  std::sort(cuts.begin(), cuts.end());
+  cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+  std::vector<int32_t> trow0, trows;
+  for (size_t i = 0; i + 1 < cuts.size(); i++) {
+    int32_t a = cuts[i], len = cuts[i + 1] - cuts[i];
+    int32_t parts = (len + kMaxTileRows - 1) / kMaxTileRows;
+    for (int32_t q = 0; q < parts; q++) {
+      int32_t s = a + static_cast<int32_t>((int64_t)len * q / parts);
+      int32_t e = a + static_cast<int32_t>((int64_t)len * (q + 1) / parts);
+      trow0.push_back(s);
+      trows.push_back(e - s);
+    }
+  }
+  const size_t nt = trow0.size();
+  auto tile_of = [&](int32_t row) {  // tile whose row0 == row (row is a cut)
+    return static_cast<size_t>(std::lower_bound(trow0.begin(), trow0.end(), row) - trow0.begin());
+  };
+
+  // ---- contributions per tile (CSR): dense blocks first, then low-rank -------
+  std::vector<int64_t> cnt(nt + 1, 0);
+  for (size_t b = 0; b < nd; b++)
+    for (size_t t = tile_of(bs.d_rs[b]); t < nt && trow0[t] < bs.d_re[b]; t++) cnt[t + 1]++;
+  for (size_t b = 0; b < na; b++)
+    if (bs.a_r[b] > 0)
+      for (size_t t = tile_of(bs.a_rs[b]); t < nt && trow0[t] < bs.a_re[b]; t++) cnt[t + 1]++;
+  for (size_t t = 0; t < nt; t++) cnt[t + 1] += cnt[t];
+  std::vector<int64_t> contrib(cnt[nt]);  // block id; low-rank ids offset by nd
+  {
+    std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+    for (size_t b = 0; b < nd; b++)
+      for (size_t t = tile_of(bs.d_rs[b]); t < nt && trow0[t] < bs.d_re[b]; t++)
+        contrib[fill[t]++] = static_cast<int64_t>(b);
+    for (size_t b = 0; b < na; b++)
+      if (bs.a_r[b] > 0)
+        for (size_t t = tile_of(bs.a_rs[b]); t < nt && trow0[t] < bs.a_re[b]; t++)
+          contrib[fill[t]++] = static_cast<int64_t>(nd + b);
+  }
+
+  // ---- panels, segments, pack jobs ---------------------------------------------
+  p.tiles.resize(nt);
+  p.pjobs.reserve(contrib.size());
+  int64_t off = 0;
+  for (size_t t = 0; t < nt; t++) {
+    TileDesc &d = p.tiles[t];
+    d.row0 = trow0[t];
+    d.m = trows[t];
+    d.data_off = off;
+    d.seg0 = static_cast<int32_t>(p.segs.size());
+    int32_t col = 0;
+    for (int64_t q = cnt[t]; q < cnt[t + 1]; q++) {
+      int64_t b = contrib[q];
+      int32_t ncols, vec_off;
+      PackJob j{};
+      j.m = d.m;
+      j.dst_off = off + static_cast<int64_t>(col) * d.m;
+      if (b < static_cast<int64_t>(nd)) {
+        ncols = bs.d_ce[b] - bs.d_cs[b];
+        vec_off = bs.d_cs[b];
+        if (dense_src_off[b] >= 0) {
+          j.kind = 0;
+          j.src_off = dense_src_off[b] + static_cast<int64_t>(d.row0 - bs.d_rs[b]) * ncols;
+          j.src_ld = ncols;
+        } else {
+          j.kind = 2;
+          j.row0 = d.row0;
+          j.col0 = bs.d_cs[b];
+        }
+      } else {
+        int64_t a = b - nd;
+        ncols = bs.a_r[a];
+        vec_off = static_cast<int32_t>(p.t_off[a]);
+        j.kind = 1;
+        j.src_off = u_src_off[a] + static_cast<int64_t>(d.row0 - bs.a_rs[a]) * ncols;
+        j.src_ld = ncols;
+      }
+      j.ncols = ncols;
+      p.pjobs.push_back(j);
+      if (!p.segs.empty() && static_cast<int32_t>(p.segs.size()) > d.seg0 &&
+          p.segs.back().vec_off + p.segs.back().ncols == vec_off) {
+        p.segs.back().ncols += ncols;  // contiguous in XT: extend the segment
+      } else {
+        p.segs.push_back(Seg{col, ncols, vec_off, 0});
+      }
+      col += ncols;
+    }
+    d.ncols = col;
+    d.nseg = static_cast<int32_t>(p.segs.size()) - d.seg0;
+    off += round_up(static_cast<int64_t>(d.m) * col, vec);
+  }
+  p.panel_len = off;
+  p.order.resize(nt);
+  std::iota(p.order.begin(), p.order.end(), 0);
+  std::stable_sort(p.order.begin(), p.order.end(), [&](int32_t a, int32_t b) {
+    return static_cast<int64_t>(p.tiles[a].m) * p.tiles[a].ncols >
+           static_cast<int64_t>(p.tiles[b].m) * p.tiles[b].ncols;
+  });
+
+  // ---- V pass -----------------------------------------------------------------------
+  p.v_off.assign(na, 0);
+  p.v_stride.assign(na, 0);
+  p.v_phase.assign(na, 0);
+  int64_t voff = 0;
+  std::vector<int64_t> uweight;
+  for (size_t a = 0; a < na; a++) {
+    int32_t nb = bs.a_ce[a] - bs.a_cs[a], r = bs.a_r[a];
+    int32_t ph = bs.a_cs[a] % vec;
+    int32_t stride = static_cast<int32_t>(round_up(ph + nb, vec));
+    p.v_off[a] = voff;
+    p.v_stride[a] = stride;
+    p.v_phase[a] = ph;
+    if (r == 0) continue;
+    int32_t nv = stride / vec, lanes = 1;
+    while (lanes < nv && lanes < 32) lanes *= 2;
+    int64_t row_bytes = static_cast<int64_t>(stride) * esize;
+    int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, kVUnitBytes / row_bytes));
+    for (int32_t k0 = 0; k0 < r; k0 += rows_per) {
+      VUnit u{};
+      u.v_off = voff + static_cast<int64_t>(k0) * stride;
+      u.stride = stride;
+      u.nrows = std::min(rows_per, r - k0);
+      u.x_off = bs.a_cs[a] - ph;
+      u.t_off = static_cast<int32_t>(p.t_off[a] + k0);
+      u.lanes = lanes;
+      p.vunits.push_back(u);
+      uweight.push_back(row_bytes * u.nrows + 256);
+    }
+    voff += static_cast<int64_t>(stride) * r;
+  }
+  p.v_len = round_up(std::max<int64_t>(voff, vec), vec);
+  p.nwarps = std::max(1, nwarps);
+  p.warp_begin.assign(p.nwarps + 1, 0);
+  {
+    int64_t total = std::accumulate(uweight.begin(), uweight.end(), int64_t(0));
+    int64_t acc = 0;
+    size_t u = 0;
+    for (int w = 0; w < p.nwarps; w++) {
+      p.warp_begin[w] = static_cast<int32_t>(u);
+      int64_t goal = total * (w + 1) / p.nwarps;
+      while (u < uweight.size() && acc + uweight[u] / 2 <= goal) acc += uweight[u++];
+    }
+    p.warp_begin[p.nwarps] = static_cast<int32_t>(uweight.size());
+  }
+
+  // ---- entry counts ------------------------------------------------------------------
+  p.dense_entries = 0;
+  for (size_t b = 0; b < nd; b++)
+    p.dense_entries += static_cast<int64_t>(bs.d_re[b] - bs.d_rs[b]) * (bs.d_ce[b] - bs.d_cs[b]);
+  p.far_entries = 0;
+  for (size_t a = 0; a < na; a++)
+    p.far_entries += static_cast<int64_t>(bs.a_r[a]) *
+                     ((bs.a_re[a] - bs.a_rs[a]) + (bs.a_ce[a] - bs.a_cs[a]));
+}
+
+}  // namespace hm

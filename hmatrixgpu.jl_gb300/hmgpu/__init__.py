@@ -1,0 +1,419 @@
+"""hmgpu -- Python face of libhmgpu, mirroring HMatrixGPU.jl's API.
+
+    ClusterTree(coordinates; max_points_per_leaf=32, dims=1)   src/tree.jl:45
+    info(tree)                                                  src/tree.jl:153
+    BlockTree(X, Y; eta=1.5)                                    src/block.jl:31
+    traverse(block_tree)                                        src/block.jl:127
+    ACA_plus(n_rows, n_cols, calc_rows, calc_cols, eps)         src/aca.jl:36
+    SVD_recompress(U, V, eps)                                   src/aca.jl:123
+    HMatrix(K, X, Y; eta=1.5, eps=1e-5, ...)                    src/hmatrix.jl:72
+    info(hmatrix)                                               src/hmatrix.jl:289
+    mul_(y, H, x)   == mul!(y, H, x)                            src/mult.jl:159
+    H * x, H @ x                                                src/mult.jl:203
+
+Coordinates are 3 x N arrays (one column per point) as in the reference.  All
+compute runs in libhmgpu (CUDA, sm_103a); the tree and partition are the
+library's host code.  Nothing here falls back to another implementation: if
+the library cannot be loaded or a GPU is missing, the call raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (F64, F32, MIXED, PRECISIONS, KERNEL_IDS, HMGPUError, Info, KernelDesc,
+                   Options, I64P, I8P, F64P, check, lib, ptr)
+from . import _build
+
+__all__ = ["ClusterTree", "BlockTree", "ACA_plus", "SVD_recompress", "HMatrix", "Kernel", "info",
+           "traverse", "mul_", "HMGPUError", "build"]
+
+
+def build(verbose=False):
+    """Compiles libhmgpu.so (sm_103a) in-tree."""
+    return _build.build(verbose=verbose)
+
+
+def _coords(coordinates):
+    a = np.asarray(coordinates, dtype=np.float64)
+    if a.ndim != 2 or a.shape[0] != 3:
+        raise ValueError("coordinates must be a 3 x N array (one column per point)")
+    return np.asfortranarray(a)
+
+
+class ClusterNode:
+    """View of one node of a ClusterTree (src/tree.jl:6-14)."""
+
+    __slots__ = ("tree", "id")
+
+    def __init__(self, tree, i):
+        self.tree, self.id = tree, int(i)
+
+    is_leaf = property(lambda s: bool(s.tree._leaf[s.id]))
+    start_idx = property(lambda s: int(s.tree._start[s.id]))
+    end_idx = property(lambda s: int(s.tree._end[s.id]))
+    center = property(lambda s: s.tree._center[s.id].copy())
+    radius = property(lambda s: float(s.tree._radius[s.id]))
+    left = property(lambda s: ClusterNode(s.tree, s.tree._left[s.id]) if s.tree._left[s.id] >= 0 else None)
+    right = property(lambda s: ClusterNode(s.tree, s.tree._right[s.id]) if s.tree._right[s.id] >= 0 else None)
+
+
+class ClusterTree:
+    """ClusterTree(coordinates; max_points_per_leaf=32, dims=1) (src/tree.jl:45-67)."""
+
+    def __init__(self, coordinates, max_points_per_leaf=32, dims=1):
+        if dims <= 0:
+            raise ValueError("Parameter `dims` must be a positive integer.")
+        self.coordinates = _coords(coordinates)
+        L = lib()
+        h = C.c_void_p()
+        check(L.hmgpu_tree_build(ptr(self.coordinates), self.coordinates.shape[1],
+                                 int(max_points_per_leaf), int(dims), C.byref(h)))
+        self._h = h
+        self.dims = dims
+        self.max_points_per_leaf = max_points_per_leaf
+        v = [C.c_int64() for _ in range(5)]
+        check(L.hmgpu_tree_info(h, *[C.byref(x) for x in v]))
+        nn, il, self._depth, self._maxp, self._minp = [x.value for x in v]
+        self.index_map = np.empty(il, np.int64)
+        self._start = np.empty(nn, np.int64)
+        self._end = np.empty(nn, np.int64)
+        self._leaf = np.empty(nn, np.int8)
+        self._left = np.empty(nn, np.int64)
+        self._right = np.empty(nn, np.int64)
+        self._center = np.empty((nn, 3))
+        self._radius = np.empty(nn)
+        check(L.hmgpu_tree_export(h, ptr(self.index_map, I64P), ptr(self._start, I64P),
+                                  ptr(self._end, I64P), ptr(self._leaf, I8P), ptr(self._left, I64P),
+                                  ptr(self._right, I64P), ptr(self._center), ptr(self._radius)))
+
+    @property
+    def root(self):
+        return ClusterNode(self, 0)
+
+    @property
+    def num_nodes(self):
+        return len(self._start)
+
+    def info(self):
+        """info(::ClusterTree) (src/tree.jl:153-187)."""
+        return {"depth": self._depth, "max_points": self._maxp, "min_points": self._minp}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().hmgpu_tree_free(h)
+            self._h = None
+
+
+class BlockTreeNode:
+    """View of one node of a BlockTree (src/block.jl:2-9)."""
+
+    __slots__ = ("bt", "id")
+
+    def __init__(self, bt, i):
+        self.bt, self.id = bt, int(i)
+
+    target_tree = property(lambda s: ClusterNode(s.bt.X, s.bt._target[s.id]))
+    source_tree = property(lambda s: ClusterNode(s.bt.Y, s.bt._source[s.id]))
+    is_admissible = property(lambda s: bool(s.bt._adm[s.id]))
+    is_dense = property(lambda s: bool(s.bt._dense[s.id]))
+    left = property(lambda s: BlockTreeNode(s.bt, s.bt._left[s.id]) if s.bt._left[s.id] >= 0 else None)
+    right = property(lambda s: BlockTreeNode(s.bt, s.bt._right[s.id]) if s.bt._right[s.id] >= 0 else None)
+
+
+class BlockTree:
+    """BlockTree(X, Y; eta=1.5) (src/block.jl:31-44). `merge=True` also applies
+    merge_dense_matrices! (src/block.jl:98-112) as HMatrix does."""
+
+    def __init__(self, X, Y, eta=1.5, merge=False):
+        self.X, self.Y, self.eta = X, Y, eta
+        L = lib()
+        h = C.c_void_p()
+        check(L.hmgpu_blocks_build(X._h, Y._h, float(eta), int(bool(merge)), C.byref(h)))
+        try:
+            v = [C.c_int64() for _ in range(3)]
+            check(L.hmgpu_blocks_counts(h, *[C.byref(x) for x in v]))
+            nd, na, nn = [x.value for x in v]
+            self._dense_pairs = np.empty((nd, 2), np.int64)
+            self._approx_pairs = np.empty((na, 2), np.int64)
+            check(L.hmgpu_blocks_export(h, ptr(self._dense_pairs, I64P), ptr(self._approx_pairs, I64P)))
+            self._target = np.empty(nn, np.int64)
+            self._source = np.empty(nn, np.int64)
+            self._adm = np.empty(nn, np.int8)
+            self._dense = np.empty(nn, np.int8)
+            self._left = np.empty(nn, np.int64)
+            self._right = np.empty(nn, np.int64)
+            check(L.hmgpu_blocks_export_nodes(h, ptr(self._target, I64P), ptr(self._source, I64P),
+                                              ptr(self._adm, I8P), ptr(self._dense, I8P),
+                                              ptr(self._left, I64P), ptr(self._right, I64P)))
+        finally:
+            L.hmgpu_blocks_free(h)
+        self.target_index_map = X.index_map
+        self.source_index_map = Y.index_map
+
+    @property
+    def root(self):
+        return BlockTreeNode(self, 0)
+
+    def traverse(self):
+        """traverse(block_tree) (src/block.jl:127-155): (direct_list, approx_list)
+        of (target ClusterNode, source ClusterNode) pairs."""
+        d = [(ClusterNode(self.X, a), ClusterNode(self.Y, b)) for a, b in self._dense_pairs]
+        a = [(ClusterNode(self.X, x), ClusterNode(self.Y, y)) for x, y in self._approx_pairs]
+        return d, a
+
+
+def traverse(block_tree):
+    return block_tree.traverse()
+
+
+def ACA_plus(n_rows, n_cols, calc_rows, calc_cols, eps, max_iter=None):
+    """ACA_plus(n_rows, n_cols, calc_rows, calc_cols, eps; max_iter=n_rows)
+    (src/aca.jl:36-106). The row callbacks are evaluated once per row to place
+    the block on the device; the partially pivoted ACA+ then runs in the
+    library's batched device kernel. Returns (U n_rows x k, V k x n_cols)."""
+    A = np.empty((n_rows, n_cols), order="F")
+    for i in range(n_rows):
+        A[i, :] = np.asarray(calc_rows(i + 1), dtype=np.float64).reshape(-1)
+    mi = int(max_iter) if max_iter is not None else 0
+    cap = max(1, min(n_rows, n_cols, mi if mi > 0 else n_rows))
+    U = np.zeros((n_rows, cap), order="F")
+    V = np.zeros((cap, n_cols), order="F")
+    k = C.c_int64()
+    check(lib().hmgpu_aca_plus(ptr(A), n_rows, n_rows, n_cols, float(eps), mi, cap, ptr(U), ptr(V),
+                               C.byref(k)))
+    k = k.value
+    return np.array(U[:, :k]), np.array(V[:k, :])
+
+
+def SVD_recompress(U, V, eps):
+    """SVD_recompress(U, V, eps) (src/aca.jl:123-143), FP64 on the device."""
+    U = np.asfortranarray(U, dtype=np.float64)
+    V = np.asfortranarray(V, dtype=np.float64)
+    m, k = U.shape
+    n = V.shape[1]
+    Uo = np.zeros((m, max(k, 1)), order="F")
+    Vo = np.zeros(max(k, 1) * n)
+    r = C.c_int64()
+    check(lib().hmgpu_svd_recompress(m, n, k, ptr(U), ptr(V), float(eps), ptr(Uo), ptr(Vo), C.byref(r)))
+    r = r.value
+    return np.array(Uo[:, :r]), np.array(Vo[: r * n].reshape((r, n), order="F"))
+
+
+class Kernel:
+    """A matrix K generated on the device: kind in {'laplace', 'yukawa', 'log2d',
+    'vector_r', 'dipolar'} over target points X and source points Y (3 x N), or
+    'explicit' with a dense matrix A."""
+
+    def __init__(self, kind, X=None, Y=None, A=None):
+        if kind not in KERNEL_IDS:
+            raise ValueError(f"unknown kernel {kind!r}")
+        self.kind = kind
+        if kind == "explicit":
+            self.A = np.asfortranarray(A, dtype=np.float64)
+            self.X = self.Y = None
+            self.shape = self.A.shape
+        else:
+            self.X = _coords(X)
+            self.Y = _coords(X if Y is None else Y)
+            nx, ny = self.X.shape[1], self.Y.shape[1]
+            self.shape = {"vector_r": (nx, 3 * ny), "dipolar": (3 * nx, 3 * ny)}.get(kind, (nx, ny))
+            self.A = None
+
+    def desc(self):
+        d = KernelDesc()
+        d.kind = KERNEL_IDS[self.kind]
+        if self.A is not None:
+            d.A = ptr(self.A)
+            d.lda = self.shape[0]
+        else:
+            d.X = ptr(self.X)
+            d.nX = self.X.shape[1]
+            d.Y = ptr(self.Y)
+            d.nY = self.Y.shape[1]
+        return d
+
+    def size(self):
+        return self.shape
+
+
+def _opts(precision, compensated, keep_factors):
+    o = Options()
+    o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    o.compensated = int(bool(compensated))
+    o.keep_factors = int(bool(keep_factors))
+    return o
+
+
+class HMatrix:
+    """HMatrix(K, X, Y; eta=1.5, eps=1e-5, svd_recompress=True) (src/hmatrix.jl:72-148),
+    assembled on the device, stored in `precision` ('f64', 'f32' or 'mixed')."""
+
+    def __init__(self, K, X, Y, eta=1.5, eps=1e-5, svd_recompress=True, precision="f64",
+                 compensated=False, keep_factors=False, _handle=None):
+        self._h = None
+        if _handle is not None:
+            self._h = _handle
+        else:
+            if not isinstance(K, Kernel):
+                K = Kernel("explicit", A=K)
+            self.K = K
+            o = _opts(precision, compensated, keep_factors)
+            h = C.c_void_p()
+            d = K.desc()
+            check(lib().hmgpu_hmatrix_build(C.byref(o), C.byref(d), X._h, Y._h, float(eta),
+                                             float(eps), int(bool(svd_recompress)), C.byref(h)))
+            self._h = h
+        self._load_meta()
+
+    @classmethod
+    def from_flat(cls, m, n, target_index_map, source_index_map, dense_block_indices, dense_blocks,
+                  U_block_indices, U_matrices, V_block_indices, V_matrices, precision="f64",
+                  compensated=False, keep_factors=False):
+        """Imports the reference's flattened HMatrix{Float64} fields
+        (src/hmatrix.jl:46-57): index tables as (nblocks, 5) / (R, 3) arrays of
+        the 1-based Julia columns."""
+        a64 = lambda a: np.ascontiguousarray(a, dtype=np.int64)
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        tm, sm = a64(target_index_map), a64(source_index_map)
+        di, ui, vi = a64(dense_block_indices), a64(U_block_indices), a64(V_block_indices)
+        dd, ud, vd = f64(dense_blocks), f64(U_matrices), f64(V_matrices)
+        o = _opts(precision, compensated, keep_factors)
+        h = C.c_void_p()
+        check(lib().hmgpu_hmatrix_import_flat(
+            C.byref(o), m, n, ptr(tm, I64P), ptr(sm, I64P), ptr(di, I64P), di.shape[0] if di.size else 0,
+            ptr(dd), dd.size, ptr(ui, I64P), ui.shape[0] if ui.size else 0, ptr(ud), ud.size,
+            ptr(vi, I64P), vi.shape[0] if vi.size else 0, ptr(vd), vd.size, C.byref(h)))
+        return cls(None, None, None, _handle=h)
+
+    def _load_meta(self):
+        inf = Info()
+        check(lib().hmgpu_hmatrix_info(self._h, C.byref(inf)))
+        self._info = inf
+        self.shape = (inf.m, inf.n)
+        self.dtype = np.float64 if inf.precision == F64 else np.float32
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().hmgpu_hmatrix_free(h)
+            self._h = None
+
+    # ---- queries ---------------------------------------------------------------------
+    def info(self):
+        """info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures."""
+        i = self._info
+        return {"data_type": self.dtype, "size": (i.m, i.n), "leaves": i.n_dense + i.n_approx,
+                "admissible_leaves": i.n_approx, "full_leaves": i.n_dense,
+                "min_rank": i.min_rank, "max_rank": i.max_rank,
+                "min_dense_size": i.min_dense_size, "max_dense_size": i.max_dense_size,
+                "compression_ratio": i.compression_ratio, "total_rank": i.total_rank,
+                "dense_entries": i.dense_entries, "far_entries": i.far_entries,
+                "matrix_bytes": i.matrix_bytes, "device_bytes": i.device_bytes,
+                "n_tiles": i.n_tiles, "hi_only_blocks": i.hi_only_blocks,
+                "build_seconds": i.build_seconds}
+
+    def blocks(self):
+        """(dense (nD, 4), approx (nA, 5)) block tables: 1-based inclusive ranges, rank last."""
+        i = self._info
+        d = np.empty((i.n_dense, 4), np.int64)
+        a = np.empty((i.n_approx, 5), np.int64)
+        check(lib().hmgpu_hmatrix_blocks(self._h, ptr(d, I64P), ptr(a, I64P)))
+        return d, a
+
+    def index_maps(self):
+        t = np.empty(self.shape[0], np.int64)
+        s = np.empty(self.shape[1], np.int64)
+        check(lib().hmgpu_hmatrix_index_maps(self._h, ptr(t, I64P), ptr(s, I64P)))
+        return t, s
+
+    def block_factors(self, b):
+        """FP64 (U, V) of low-rank block b (0-based); needs keep_factors=True."""
+        _, a = self.blocks()
+        rs, re, cs, ce, r = a[b]
+        U = np.empty((re - rs + 1, r))
+        V = np.empty((r, ce - cs + 1))
+        check(lib().hmgpu_hmatrix_block_factors(self._h, int(b), ptr(U), ptr(V)))
+        return U, V
+
+    def aca_ranks(self):
+        n = getattr(self, "_ncand", None)
+        raise NotImplementedError if n is None else None
+
+    # ---- products ------------------------------------------------------------------
+    def mul(self, y, x, stream=None):
+        """mul!(y, H, x): y and x are torch CUDA tensors (stream-ordered on the
+        current torch stream unless `stream` is given) or numpy arrays (host,
+        synchronous). Vectors or (n, nrhs) column-major/Fortran matrices."""
+        return mul_(y, self, x, stream=stream)
+
+    def __mul__(self, x):
+        """H * x (src/mult.jl:203-209)."""
+        return self.matvec(x)
+
+    __matmul__ = __mul__
+
+    def matvec(self, x):
+        m = self.shape[0]
+        if _is_torch(x):
+            import torch
+            shape = (m,) if x.dim() == 1 else (x.shape[1], m)
+            y = torch.empty(shape, dtype=x.dtype, device=x.device)
+            if x.dim() == 2:
+                y = y.t()
+            mul_(y, self, x)
+            return y
+        x = np.asarray(x)
+        y = np.empty((m,) + x.shape[1:], dtype=self.dtype, order="F")
+        mul_(y, self, x)
+        return y
+
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def mul_(y, H, x, stream=None):
+    """mul!(y, H, x) (src/mult.jl:159-189): overwrites y with H x, original ordering."""
+    m, n = H.shape
+    L = lib()
+    if _is_torch(x):
+        import torch
+        if not (x.is_cuda and y.is_cuda):
+            raise ValueError("torch tensors must be CUDA tensors")
+        want = torch.float64 if H.dtype == np.float64 else torch.float32
+        if x.dtype != want or y.dtype != want:
+            raise TypeError(f"x and y must be {want} for this H-matrix")
+        nrhs = 1 if x.dim() == 1 else x.shape[1]
+        if x.shape[0] != n or y.shape[0] != m or (x.dim() == 2 and y.shape[1] != nrhs):
+            raise ValueError("dimension mismatch")
+        if x.dim() == 2 and (x.stride(0) != 1 or y.stride(0) != 1):
+            raise ValueError("x and y must be column-major (use .t().contiguous().t())")
+        ldx = x.stride(1) if x.dim() == 2 else n
+        ldy = y.stride(1) if y.dim() == 2 else m
+        if stream is None:
+            stream = torch.cuda.current_stream(x.device).cuda_stream
+        with torch.cuda.device(x.device):
+            check(L.hmgpu_matvec(H._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), nrhs,
+                                 ldx, ldy, C.c_void_p(stream)))
+        return y
+    xa = np.asarray(x)
+    if xa.dtype != H.dtype:
+        raise TypeError(f"x must be {np.dtype(H.dtype)} for this H-matrix")
+    if not isinstance(y, np.ndarray) or y.dtype != H.dtype:
+        raise TypeError(f"y must be a numpy {np.dtype(H.dtype)} array")
+    xa = np.asfortranarray(xa)
+    nrhs = 1 if xa.ndim == 1 else xa.shape[1]
+    if xa.shape[0] != n or y.shape[0] != m:
+        raise ValueError("dimension mismatch")
+    yb = y if y.flags.f_contiguous else np.empty(y.shape, y.dtype, order="F")
+    check(L.hmgpu_matvec_host(H._h, xa.ctypes.data_as(C.c_void_p), yb.ctypes.data_as(C.c_void_p),
+                              nrhs, n, m))
+    if yb is not y:
+        y[...] = yb
+    return y
+
+
+def info(obj):
+    """info(tree) / info(hmatrix)."""
+    return obj.info()

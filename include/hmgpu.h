@@ -1,0 +1,214 @@
+/*
+ * hmgpu.h -- C ABI of libhmgpu, a CUDA (sm_103a) implementation of the
+ * H-matrix path of HMatrixGPU.jl: cluster tree, block tree, ACA+ with SVD
+ * recompression, H-matrix assembly and the product mul!(y, H, x) / H * x.
+ *
+ * Every function returns HMGPU_OK (0) or a negative status; the message of
+ * the last failure on the calling thread is available from hmgpu_last_error().
+ * Plain pointers and sizes only.  Index arguments follow the reference's
+ * conventions: 1-based, ranges inclusive, tables column-major as Julia stores
+ * them.  Device-side objects are bound to the CUDA device that was current
+ * when they were created.  A handle may be used by one stream at a time.
+ *
+ * Reference interfaces replaced (paths inside the HMatrixGPU.jl project):
+ *   ClusterTree(coords; max_points_per_leaf, dims)   src/tree.jl:45
+ *   info(::ClusterTree)                              src/tree.jl:153
+ *   BlockTree(X, Y; eta) + merge + traverse          src/block.jl:31, :98, :127
+ *   ACA_plus(n_rows, n_cols, rows, cols, eps)        src/aca.jl:36
+ *   SVD_recompress(U, V, eps)                        src/aca.jl:123
+ *   HMatrix(K, X, Y; eta, eps, ...)                  src/hmatrix.jl:72
+ *   HMatrix{T} flattened fields                      src/hmatrix.jl:46-57
+ *   info(::HMatrixCPU)                               src/hmatrix.jl:289
+ *   mul!(y, ::HMatrix{T}, x), *(::HMatrix{T}, x)     src/mult.jl:159, :203
+ */
+#ifndef HMGPU_H
+#define HMGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HMGPU_ABI_VERSION 1
+
+/* status codes */
+#define HMGPU_OK 0
+#define HMGPU_ERR_INVALID (-1)   /* an argument or an imported table is invalid     */
+#define HMGPU_ERR_CUDA (-2)      /* a CUDA runtime call failed                      */
+#define HMGPU_ERR_NOMEM (-3)     /* host or device allocation failed                */
+#define HMGPU_ERR_TREE (-4)      /* a cluster cannot be split (coincident points)   */
+#define HMGPU_ERR_TIMEOUT (-5)   /* a bounded device-side wait expired              */
+#define HMGPU_ERR_UNSUPPORTED (-6)
+
+/* storage / arithmetic modes of an H-matrix */
+#define HMGPU_F64 0   /* all factors FP64, FP64 arithmetic; x, y are double        */
+#define HMGPU_F32 1   /* all factors FP32, FP32 arithmetic; x, y are float         */
+#define HMGPU_MIXED 2 /* near field FP32; far field hi+lo BF16 with per-column
+                         FP32 scales (hi only where the block tolerance allows);
+                         compensated FP32 accumulation; x, y are float           */
+
+/* matrix entry generators for on-device assembly */
+#define HMGPU_KERNEL_EXPLICIT 0  /* entries of a given column-major matrix        */
+#define HMGPU_KERNEL_LAPLACE3D 1 /* 1/(4 pi r), 0 at r = 0                         */
+#define HMGPU_KERNEL_YUKAWA 2    /* exp(-r)/r, 0 at r = 0                          */
+#define HMGPU_KERNEL_LOG2D 3     /* -log(r)/(2 pi), 1 at r < 1e-12                 */
+#define HMGPU_KERNEL_VECTOR_R 4  /* R_c/r^2 over 3 columns per source point        */
+#define HMGPU_KERNEL_DIPOLAR 5   /* 3x3 demagnetising tensor per point pair        */
+
+/* Returns the message of the last failed call on this thread ("" if none). */
+const char *hmgpu_last_error(void);
+int hmgpu_abi_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* Cluster tree: replaces ClusterTree(coords; max_points_per_leaf, dims)     */
+/* (src/tree.jl:45-137) and info(::ClusterTree) (src/tree.jl:153-187).      */
+/* Host-side, bit-exact with the reference's bisection.                     */
+/* ---------------------------------------------------------------------- */
+typedef struct hmgpu_tree hmgpu_tree;
+
+/* coords: 3 x npts column-major (Julia's coordinates[:, i]). */
+int hmgpu_tree_build(const double *coords, int64_t npts, int64_t max_points_per_leaf,
+                     int64_t dims, hmgpu_tree **out);
+/* nnodes, index-map length (dims*npts), and info(): depth, max/min points. */
+int hmgpu_tree_info(const hmgpu_tree *t, int64_t *nnodes, int64_t *index_len, int64_t *depth,
+                    int64_t *max_points, int64_t *min_points);
+/* index_map (1-based), per node: start (1-based), end (exclusive, as
+ * ClusterNode.end_idx), leaf flag, children (node numbers, -1 if none; nodes
+ * are numbered in pre-order), center (3 per node), radius. Any pointer may be
+ * NULL. */
+int hmgpu_tree_export(const hmgpu_tree *t, int64_t *index_map, int64_t *start, int64_t *end,
+                      int8_t *is_leaf, int64_t *left, int64_t *right, double *center,
+                      double *radius);
+int hmgpu_tree_free(hmgpu_tree *t);
+
+/* ---------------------------------------------------------------------- */
+/* Block tree: replaces BlockTree(X, Y; eta) (src/block.jl:31-90),          */
+/* merge_dense_matrices! (:98-112) and traverse (:127-155).                 */
+/* ---------------------------------------------------------------------- */
+typedef struct hmgpu_blocks hmgpu_blocks;
+
+int hmgpu_blocks_build(const hmgpu_tree *X, const hmgpu_tree *Y, double eta, int merge,
+                       hmgpu_blocks **out);
+int hmgpu_blocks_counts(const hmgpu_blocks *b, int64_t *ndense, int64_t *napprox,
+                        int64_t *nnodes);
+/* (target node, source node) pairs of traverse()'s direct_list / approx_list. */
+int hmgpu_blocks_export(const hmgpu_blocks *b, int64_t *dense_pairs, int64_t *approx_pairs);
+/* Every block-tree node: target/source node, admissible and dense flags,
+ * children (-1 if none). */
+int hmgpu_blocks_export_nodes(const hmgpu_blocks *b, int64_t *target, int64_t *source,
+                              int8_t *admissible, int8_t *dense, int64_t *left,
+                              int64_t *right);
+int hmgpu_blocks_free(hmgpu_blocks *b);
+
+/* ---------------------------------------------------------------------- */
+/* H-matrix                                                                  */
+/* ---------------------------------------------------------------------- */
+typedef struct hmgpu_hmatrix hmgpu_hmatrix;
+
+typedef struct {
+  int32_t precision;   /* HMGPU_F64, HMGPU_F32 or HMGPU_MIXED                     */
+  int32_t compensated; /* FP32 modes: 1 = compensated (Dot2) accumulation        */
+  int32_t keep_factors;/* 1 = keep the FP64 block factors for export             */
+  int32_t reserved;
+} hmgpu_options;
+
+typedef struct {
+  int32_t kind;    /* HMGPU_KERNEL_*                                              */
+  int32_t reserved;
+  const double *X; /* target points, 3 x nX column-major (host)                   */
+  int64_t nX;
+  const double *Y; /* source points, 3 x nY column-major (host)                   */
+  int64_t nY;
+  const double *A; /* HMGPU_KERNEL_EXPLICIT: column-major matrix, host or device  */
+  int64_t lda;
+} hmgpu_kernel;
+
+/* Imports a reference-layout flattened HMatrix{Float64} (src/hmatrix.jl:46-57,
+ * built at :95-147): m x n operator, target/source index maps (1-based), dense
+ * index table 5 x nD (row_start,row_end,col_start,col_end,offset0), dense data
+ * (row-major blocks), U table 5 x nA (row_start,row_end,vx_start,vx_end,
+ * offset0), U data (row-major m x r), V table 3 x R (col_start,col_end,
+ * offset0), V data (row-major r x n).  Host or device pointers.  The tables
+ * are validated, the data is converted to the requested precision and
+ * re-laid out on the device; the caller keeps ownership of its arrays. */
+int hmgpu_hmatrix_import_flat(const hmgpu_options *opt, int64_t m, int64_t n,
+                              const int64_t *target_map, const int64_t *source_map,
+                              const int64_t *dense_idx, int64_t nD, const double *dense_data,
+                              int64_t dense_len, const int64_t *U_idx, int64_t nA,
+                              const double *U_data, int64_t U_len, const int64_t *V_idx,
+                              int64_t R, const double *V_data, int64_t V_len,
+                              hmgpu_hmatrix **out);
+
+/* HMatrix(K, X, Y; eta, eps, svd_recompress) (src/hmatrix.jl:72-217) with the
+ * entries generated on the device: dense blocks filled from K, admissible
+ * blocks compressed by batched ACA+ at eps/10 and recompressed by batched
+ * QR+SVD at eps (FP64), blocks that do not compress stored dense. */
+int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel *K, const hmgpu_tree *X,
+                        const hmgpu_tree *Y, double eta, double eps, int svd_recompress,
+                        hmgpu_hmatrix **out);
+
+/* mul!(y, H, x) (src/mult.jl:159-189) for nrhs right-hand sides: x is n x nrhs
+ * and y is m x nrhs, column-major with leading dimensions ldx >= n and
+ * ldy >= m, device pointers of the mode's element type (double for HMGPU_F64,
+ * float otherwise).  y is overwritten in the original (unpermuted) order.
+ * Stream-ordered on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream); returns without synchronising. */
+int hmgpu_matvec(hmgpu_hmatrix *H, const void *x, void *y, int64_t nrhs, int64_t ldx,
+                 int64_t ldy, void *stream);
+/* H * x (src/mult.jl:203-209) on host buffers: copies x to the device, runs
+ * hmgpu_matvec and copies y back, synchronously. */
+int hmgpu_matvec_host(hmgpu_hmatrix *H, const void *x, void *y, int64_t nrhs, int64_t ldx,
+                      int64_t ldy);
+
+typedef struct {
+  int64_t m, n;                  /* size(K)                                        */
+  int64_t n_dense, n_approx;     /* full_leaves, admissible_leaves                  */
+  int64_t min_rank, max_rank;
+  int64_t min_dense_size, max_dense_size;
+  int64_t total_rank;            /* R = length(Vx_buffer)                           */
+  int64_t dense_entries;         /* sum over dense blocks of m*n                    */
+  int64_t far_entries;           /* sum over low-rank blocks of r*(m+n)             */
+  double compression_ratio;      /* m*n / (dense_entries + far_entries)             */
+  int64_t matrix_bytes;          /* bytes of factor data one product streams        */
+  int64_t device_bytes;          /* bytes held on the device                        */
+  int64_t n_tiles;               /* row tiles of the near/U pass                    */
+  int32_t precision;
+  int32_t hi_only_blocks;        /* HMGPU_MIXED: blocks stored hi-only BF16         */
+  double build_seconds;          /* wall time of the last import/build              */
+} hmgpu_info;
+/* info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures. */
+int hmgpu_hmatrix_info(const hmgpu_hmatrix *H, hmgpu_info *info);
+
+/* Block lists of the H-matrix in the reference's order: dense blocks (tree
+ * dense leaves, then admissible leaves that did not compress) as 4 x nD
+ * (row_start,row_end,col_start,col_end), low-rank blocks as 5 x nA
+ * (row_start,row_end,col_start,col_end,rank). */
+int hmgpu_hmatrix_blocks(const hmgpu_hmatrix *H, int64_t *dense_idx, int64_t *approx_idx);
+/* Index maps (1-based) of the H-matrix. */
+int hmgpu_hmatrix_index_maps(const hmgpu_hmatrix *H, int64_t *target_map, int64_t *source_map);
+/* FP64 factors of low-rank block b (0-based, in approx_idx order) into host
+ * arrays U (m x r row-major) and V (r x n row-major); requires keep_factors. */
+int hmgpu_hmatrix_block_factors(const hmgpu_hmatrix *H, int64_t b, double *U, double *V);
+/* ACA ranks before recompression per admissible leaf of the block tree, in
+ * traversal order (builds only; -1 where not computed). */
+int hmgpu_hmatrix_aca_ranks(const hmgpu_hmatrix *H, int64_t *aca_rank, int64_t *final_rank);
+int hmgpu_hmatrix_free(hmgpu_hmatrix *H);
+
+/* ---------------------------------------------------------------------- */
+/* Single-block compression: ACA_plus (src/aca.jl:36-106) and                */
+/* SVD_recompress (src/aca.jl:123-143) on an explicit m x n block           */
+/* (column-major, host or device), run by the batched device kernels.       */
+/* ---------------------------------------------------------------------- */
+/* U: m x cap column-major, V: cap x n column-major (ld cap), host arrays;
+ * cap >= min(m, n, max_iter); max_iter <= 0 means n_rows. */
+int hmgpu_aca_plus(const double *A, int64_t lda, int64_t m, int64_t n, double eps,
+                   int64_t max_iter, int64_t cap, double *U, double *V, int64_t *rank);
+/* U: m x k (ld m), V: k x n (ld k) host arrays in; U_out m x r (ld m), V_out
+ * r x n (ld r) host arrays out (room for k columns/rows). */
+int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const double *V,
+                         double eps, double *U_out, double *V_out, int64_t *r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
