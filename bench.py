@@ -1,0 +1,288 @@
+"""H-matrix-vector product benchmark (one JSON line on stdout).
+
+Workload (the headline configuration): N = 2^20 cell centres of a 1024 x 1024 x 1
+thin-film grid, spacing 1 (coordinates in nm), Gaussian jitter sigma = 0.05
+spacing on every coordinate (seeded), Laplace kernel 1/(4 pi r) with G(x,x) = 0,
+leaf size 64, admissibility eta = 2 (the reference's dist > eta (rX + rY)), ACA+
+tolerance 1e-4 with SVD recompression, assembled on the device.  One step is one
+product y = H x with x ~ N(0,1) (FP32 storage and arithmetic, 1 right-hand side).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`value` is products per second over the whole job with x already in HBM;
+`e2e` is the same through the public API on pinned host buffers (x copied in,
+y copied out every step).  The reference arm (--impl reference) times the
+reference's CPU product (src/mult.jl:6-32) restated by the oracle, on all host
+cores, over a bounded sample of the same matrix's blocks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "hmatrixgpu.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "H-matvec/s at N=2^20, 1 & 32 RHS: mixed vs plain FP32 at equal err; HBM GB/s"
+WORKLOAD = "film-2^20 Laplace leaf64 eta2 tol1e-4, 1 RHS, FP32 storage"
+GRID, LEAF, ETA, TOL = 1024, 64, 2.0, 1e-4
+SAMPLE_STRIDE = 64  # the CPU legs time every 64th dense and admissible block
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def film_points():
+    from tests import geometry
+    return geometry.film(GRID, GRID, spacing=1.0, jitter=0.05, seed=1)
+
+
+def cpu_sample(threads, target_s=15.0):
+    """Times the oracle's restatement of the reference CPU mul! (src/mult.jl:6-32)
+    on every SAMPLE_STRIDE-th block of the workload's matrix; returns products/s
+    extrapolated to the whole matrix and a description."""
+    from oracle import oracle as O
+    P = film_points()
+    T = O.Tree(P.T, LEAF)
+    K = O.Kernel("laplace", P.T, P.T)
+    t0 = time.time()
+    H = O.HMatrix(K, T, T, eta=ETA, eps=TOL, sample_stride=SAMPLE_STRIDE,
+                  nthreads=os.cpu_count() or 1)
+    build_s = time.time() - t0
+    x = np.random.default_rng(0).standard_normal(H.n)
+    dt1 = H.mul_timed(x, threads, 1)
+    reps = max(1, int(target_s / max(dt1, 1e-6)))
+    dt = H.mul_timed(x, threads, reps) / reps
+    per_product = dt * SAMPLE_STRIDE
+    return 1.0 / per_product, {
+        "sample": f"every {SAMPLE_STRIDE}th dense and admissible block of the same partition "
+                  f"({H.nD} dense + {H.nA} low-rank blocks, FP64), {reps} timed repetitions, "
+                  f"time x {SAMPLE_STRIDE}; sample assembled by the oracle in {build_s:.0f}s",
+        "cores": threads, "seconds": dt * reps}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    v, d = cpu_sample(threads)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded film points)",
+            "config": {"workload": WORKLOAD, "N": GRID * GRID, "leaf": LEAF, "eta": ETA, "tol": TOL},
+            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": threads, "kind": "port",
+                             "sample": d["sample"]},
+            "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+
+    import hmgpu
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    P = film_points()
+    t0 = time.time()
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=LEAF)
+    H = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=ETA, eps=TOL, precision="f32")
+    torch.cuda.synchronize()
+    build_s = time.time() - t0
+    inf = H.info()
+    n = P.shape[1]
+    x = torch.randn(n, device=dev, generator=torch.Generator(dev).manual_seed(rank))
+    y = torch.empty(n, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    for _ in range(max(args.warmup, 3)):
+        hmgpu.mul_(y, H, x)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    lib = hmgpu._lib.lib()
+    hmgpu.check(lib.hmgpu_hmatrix_set_profiling(H._h, 1))
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        s.record(stream)
+        for _ in range(args.steps):
+            hmgpu.mul_(y, H, x)
+        e.record(stream)
+        torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / args.steps
+    import ctypes as C
+    ph = np.zeros(3)
+    nl, npd = C.c_int64(), C.c_int64()
+    hmgpu.check(lib.hmgpu_hmatrix_phase_times(H._h, hmgpu.ptr(ph), C.byref(nl), C.byref(npd)))
+    hmgpu.check(lib.hmgpu_hmatrix_set_profiling(H._h, 0))
+    ph = ph / max(npd.value, 1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # end to end: pinned host x in, host y out, every step
+    xh = torch.randn(n, generator=torch.Generator().manual_seed(rank + 7)).pin_memory()
+    yh = torch.empty(n).pin_memory()
+    xn, yn = xh.numpy(), yh.numpy()
+    for _ in range(3):
+        hmgpu.mul_(yn, H, xn)
+    ksteps = max(10, min(args.steps, 200))
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(ksteps):
+        hmgpu.mul_(yn, H, xn)
+    e2e_s = (time.perf_counter() - t1) / ksteps
+
+    # accuracy of this step against an FP64 H-matrix product on the device
+    H64 = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=ETA, eps=TOL, precision="f64")
+    y64 = H64 * x.double()
+    hmgpu.mul_(y, H, x)
+    rel_err = float(torch.linalg.norm(y.double() - y64) / torch.linalg.norm(y64))
+    del H64
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    hbm, src = peaks()
+    # algorithmic bytes (FP32): near field + low-rank factors + vectors
+    es = 4
+    dense_b = inf["dense_entries"] * es
+    far_b = inf["far_entries"] * es
+    R = inf["total_rank"]
+    vec_b = es * (2 * n + 2 * R)
+    alg_bytes = dense_b + far_b + vec_b
+    # the near/U pass: dense entries + U entries + y + gathered x and t
+    d, a = H.blocks()
+    u_entries = int(((a[:, 1] - a[:, 0] + 1) * a[:, 4]).sum()) if len(a) else 0
+    du_bytes = (inf["dense_entries"] + u_entries) * es + es * (2 * n + R)
+    du_ms = ph[2]
+    achieved = du_bytes / (du_ms * 1e-3) / 1e9
+    cpu_v, cpu_d = cpu_sample(1, target_s=12.0)
+    value = world * 1e3 / ms
+    line = {
+        "metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded film points, x ~ N(0,1))",
+        "config": {"workload": WORKLOAD, "N": n, "leaf": LEAF, "eta": ETA, "tol": TOL,
+                   "precision": "f32", "nrhs": 1,
+                   "l2": f"inputs larger than L2: {inf['matrix_bytes'] / 1e9:.1f} GB of factors streamed per step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "hbm_gbs": alg_bytes / (ms * 1e-3) / 1e9,
+        "rel_err_vs_fp64_hmatrix": rel_err,
+        "structure": {"dense_blocks": inf["full_leaves"], "lowrank_blocks": inf["admissible_leaves"],
+                      "dense_entries": inf["dense_entries"], "far_entries": inf["far_entries"],
+                      "total_rank": R, "max_rank": inf["max_rank"], "algorithmic_bytes": alg_bytes,
+                      "stored_bytes": inf["matrix_bytes"], "build_seconds": build_s},
+        "phases_ms": {"permute": ph[0], "v_pass": ph[1], "near_u_pass": ph[2]},
+        "roofline": {"bound": "hbm", "kernel": "du_pass_kernel (near field + U t)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": src, "traffic": None},
+        "cpu_baseline": {"value": cpu_v, "unit": "matvec/s", "cores": 1, "kind": "port",
+                         "sample": cpu_d["sample"]},
+        "e2e": {"value": world / e2e_s, "unit": "matvec/s", "h2d_bytes_per_step": n * es,
+                "d2h_bytes_per_step": n * es},
+        "gpu_launches": int(nl.value),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

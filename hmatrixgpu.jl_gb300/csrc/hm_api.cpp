@@ -13,7 +13,11 @@ int cuda_fail(cudaError_t e, const char *what) {
   return fail(HMGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-HMatrix::~HMatrix() { release(); }
+HMatrix::~HMatrix() {
+  for (auto &q : prof_ev)
+    for (cudaEvent_t e : q) cudaEventDestroy(e);
+  release();
+}
 
 void HMatrix::release() {
   for (void *p : dev_allocs) cudaFree(p);
@@ -59,7 +63,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
                     const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
                     const std::vector<int64_t> &v_src_off, DenseGenerator *gen) {
   const bool f64 = H.opt.precision == HMGPU_F64;
-  const bool comp = !f64 && H.opt.compensated;
+  const bool comp = !f64 && (H.opt.compensated || H.opt.precision == HMGPU_MIXED);
   cudaDeviceProp prop;
   cudaError_t e = cudaGetDeviceProperties(&prop, H.device);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
@@ -77,8 +81,12 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   cudaMemset(H.xt, 0, p.xt_len * es);
   cudaMemset(H.vdata, 0, p.v_len * es);
   if ((rc = upload(H, &H.dp.tiles, p.tiles))) return rc;
-  if ((rc = upload(H, &H.dp.order, p.order))) return rc;
+  if ((rc = upload(H, &H.dp.units, p.units))) return rc;
   if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
+  if ((rc = H.dalloc(&H.dp.part, std::max<int64_t>(p.part_len, 1) * es * (comp ? 2 : 1)))) return rc;
+  if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.tile_cnt), p.tiles.size() * sizeof(int32_t)))) return rc;
+  cudaMemset(H.dp.tile_cnt, 0, p.tiles.size() * sizeof(int32_t));
+  H.dp.nunits = static_cast<int32_t>(p.units.size());
   if ((rc = upload(H, &H.dp.vunits, p.vunits))) return rc;
   if ((rc = upload(H, &H.dp.warp_begin, p.warp_begin))) return rc;
   std::vector<int32_t> t0(H.bs.m), s0(H.bs.n);
@@ -90,6 +98,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   cudaMemset(H.dp.counter, 0, 64);
   H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
   H.dp.nwarps = p.nwarps;
+  H.dp.warp_begin_empty = p.vunits.empty();
   H.dp.m = H.bs.m;
   H.dp.n = H.bs.n;
   H.dp.x_len = p.x_len;
@@ -318,10 +327,23 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
   const size_t es = f64 ? 8 : 4;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   for (int64_t k = 0; k < nrhs; k++) {
+    cudaEvent_t *ev = nullptr;
+    if (H.profiling) {
+      if (H.prof_used == H.prof_ev.size()) {
+        std::array<cudaEvent_t, 4> q;
+        for (auto &e : q)
+          if (cudaEventCreate(&e) != cudaSuccess) return hm::fail(HMGPU_ERR_CUDA, "cudaEventCreate failed");
+        H.prof_ev.push_back(q);
+      }
+      ev = H.prof_ev[H.prof_used++].data();
+    }
+    int nl = 0;
     cudaError_t e = hm::launch_matvec(f64, comp, H.dp, H.panels, H.vdata, H.xt,
                                       static_cast<const char *>(x) + k * ldx * es,
-                                      static_cast<char *>(y) + k * ldy * es, H.grid_v, H.grid_du, s);
+                                      static_cast<char *>(y) + k * ldy * es, H.grid_v, H.grid_du, s,
+                                      ev, &nl);
     if (e != cudaSuccess) return hm::cuda_fail(e, "matvec launch");
+    if (H.profiling) H.prof_launches += nl;
   }
   return HMGPU_OK;
 }
@@ -382,6 +404,38 @@ extern "C" int hmgpu_hmatrix_info(const hmgpu_hmatrix *h, hmgpu_info *info) {
   info->n_tiles = static_cast<int64_t>(H.plan.tiles.size());
   info->precision = H.opt.precision;
   info->build_seconds = H.build_seconds;
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_set_profiling(hmgpu_hmatrix *h, int on) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  H.profiling = on != 0;
+  H.prof_used = 0;
+  H.prof_launches = 0;
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_phase_times(hmgpu_hmatrix *h, double *ms3, int64_t *launches,
+                                         int64_t *products) {
+  if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
+  HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (size_t i = 0; i < H.prof_used; i++) {
+    cudaError_t e = cudaEventSynchronize(H.prof_ev[i][3]);
+    if (e != cudaSuccess) return hm::cuda_fail(e, "cudaEventSynchronize");
+    for (int k = 0; k < 3; k++) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, H.prof_ev[i][k], H.prof_ev[i][k + 1]);
+      acc[k] += t;
+    }
+  }
+  if (ms3)
+    for (int k = 0; k < 3; k++) ms3[k] = acc[k];
+  if (launches) *launches = H.prof_launches;
+  if (products) *products = static_cast<int64_t>(H.prof_used);
+  H.prof_used = 0;
+  H.prof_launches = 0;
   return HMGPU_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <vector>
 
 #include "hm_device.h"
@@ -32,6 +33,11 @@ struct HMatrix {
   // staging of hmgpu_matvec_host
   void *io_x = nullptr, *io_y = nullptr;
   size_t io_x_bytes = 0, io_y_bytes = 0;
+  // phase profiling (hmgpu_hmatrix_set_profiling)
+  bool profiling = false;
+  std::vector<std::array<cudaEvent_t, 4>> prof_ev;
+  size_t prof_used = 0;
+  int64_t prof_launches = 0;
   double build_seconds = 0.0;
   int64_t device_bytes = 0;
   std::vector<void *> dev_allocs;

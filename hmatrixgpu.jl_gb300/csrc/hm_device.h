@@ -9,12 +9,16 @@ namespace hm {
 // Device copies of a Plan plus the per-product scratch.
 struct DevPlan {
   TileDesc *tiles = nullptr;
-  int32_t *order = nullptr;
   Seg *segs = nullptr;
   int32_t ntiles = 0;
+  DuUnit *units = nullptr;
+  int32_t nunits = 0;
+  void *part = nullptr;          // partial row sums of split tiles
+  int32_t *tile_cnt = nullptr;   // per-tile arrival counters (zero between products)
   VUnit *vunits = nullptr;
   int32_t *warp_begin = nullptr;
   int32_t nwarps = 0;
+  bool warp_begin_empty = true;  // no V units (no low-rank blocks)
   int32_t *tmap0 = nullptr;  // 0-based target map, length m
   int32_t *smap0 = nullptr;  // 0-based source map, length n
   int32_t *counter = nullptr;  // tile ticket of the near/U pass
@@ -29,9 +33,11 @@ int occupancy_du(bool f64, bool comp);
 
 // One product y = H x (single right-hand side) on `stream`:
 //   x permutation into XT, V pass (t = V x), near/U pass (y = D x + U t).
+// `ev` (optional) receives 4 events recorded before, between and after the
+// three phases; returns the number of kernels launched through *launches.
 cudaError_t launch_matvec(bool f64, bool comp, const DevPlan &p, const void *panels,
                           const void *vdata, void *xt, const void *x, void *y, int grid_v,
-                          int grid_du, cudaStream_t stream);
+                          int grid_du, cudaStream_t stream, cudaEvent_t *ev, int *launches);
 
 // Packing of FP64 row-major block factors into the product layout.
 cudaError_t launch_pack_panels(bool f64, const PackJob *jobs, int64_t njobs, const double *dsrc,

@@ -78,6 +78,19 @@ struct Seg {
   int32_t col0, ncols, vec_off, pad;
 };
 
+// A unit of the near/U pass: columns [c0, c1) of one tile. A tile split into
+// several units sums their partial rows in slot order (fixed, deterministic).
+struct DuUnit {
+  int32_t tile;
+  int32_t c0, c1;
+  int32_t seg0, nseg;  // segments overlapping [c0, c1)
+  int32_t slot;        // index of this unit within its tile
+  int32_t nslots;      // units of the tile
+  int32_t pad;
+  int64_t part_off;    // offset of this tile's partial rows (nslots * m values)
+};
+static_assert(sizeof(DuUnit) == 40, "DuUnit layout");
+
 // A unit of the V pass: rows [0, nrows) of one low-rank block, each row a
 // phase-aligned run of `stride` elements dotted with XT[x_off : x_off+stride).
 struct VUnit {
@@ -112,6 +125,8 @@ struct Plan {
   std::vector<int32_t> order;  // tiles by decreasing work
   std::vector<Seg> segs;
   int64_t panel_len = 0;
+  std::vector<DuUnit> units;   // near/U pass work, largest tiles first
+  int64_t part_len = 0;        // partial-row scratch (values) of split tiles
   std::vector<PackJob> pjobs;
   // V pass
   std::vector<int64_t> v_off, t_off;  // per low-rank block
@@ -130,3 +145,11 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
                const std::vector<int64_t> &u_src_off, Plan &p);
 
 }  // namespace hm
+
+// Definitions of the opaque handles declared in hmgpu.h.
+struct hmgpu_tree {
+  hm::Tree t;
+};
+struct hmgpu_blocks {
+  hm::Blocks b;
+};

@@ -127,103 +127,111 @@ __global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Near/U pass. CTAs take row tiles from a ticket counter (largest first).
-// A tile of m rows is a column-major panel; the CTA's threads form G groups of
-// m threads. Thread t of group g loads the 16-byte vectors f = t + m*q,
-// q = g (mod G). Because a vector holds VEC elements and the group spans VEC*m
-// elements per step, element u of every vector the thread loads belongs to
-// the same row (VEC*t + u) mod m: the thread keeps VEC fixed-row accumulators
-// and the column of element u is (VEC*t + u)/m + VEC*q. Vector entries of the
-// columns are gathered into shared memory per chunk of columns.
+// Near/U pass. CTAs take units (column slices of a row tile) from a ticket
+// counter, largest tiles first. A tile of m rows is a column-major panel; the
+// CTA's threads form G groups of m threads. Thread t of group g loads the
+// 16-byte vectors f = t + m*q, q = g (mod G). Because a vector holds VEC
+// elements and the group spans VEC*m elements per step, element u of every
+// vector the thread loads belongs to the same row (VEC*t + u) mod m: the
+// thread keeps VEC fixed-row accumulators, and the column of element u is
+// (VEC*t + u)/m + VEC*q. The vector entries of the unit's columns are
+// gathered into shared memory first. A tile cut into several units writes
+// one partial row-sum vector per unit; the unit that arrives last adds them
+// in slot order, so the result does not depend on the schedule.
 // ---------------------------------------------------------------------------
 template <typename T>
 struct DuArgs {
   const T *panels;
   const TileDesc *tiles;
-  const int32_t *order;
-  int32_t ntiles;
+  const DuUnit *units;
+  int32_t nunits;
   const Seg *segs;
   const T *xt;
   const int32_t *tmap0;
   T *y;
   int32_t *counter;
+  T *part;            // partial row sums of split tiles (x2 when compensated)
+  int32_t *tile_cnt;  // arrivals per tile, returned to zero by the last unit
 };
 
 template <typename T>
 struct DuChunk {
-  static constexpr int value = 16384 / sizeof(T);  // columns of vector entries per chunk
+  static constexpr int value = 16384 / sizeof(T);  // columns of vector entries per unit
 };
+constexpr int kDuSegs = 512;
 
 template <typename T, bool COMP>
 __global__ void __launch_bounds__(kThreads) du_pass_kernel(DuArgs<T> a) {
   using VT = typename Vec16<T>::type;
   constexpr int VEC = Vec16<T>::N;
-  constexpr int CHUNK = DuChunk<T>::value;
-  __shared__ T vals[CHUNK];
+  __shared__ T vals[DuChunk<T>::value];
+  __shared__ Seg ssegs[kDuSegs];
   __shared__ T part[kThreads * VEC];
   __shared__ T partc[COMP ? kThreads * VEC : 1];
-  __shared__ int32_t s_ticket;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ int32_t s_ticket, s_last;
+  const int tid = threadIdx.x;
   for (;;) {
     if (tid == 0) s_ticket = atomicAdd(a.counter, 1);
     __syncthreads();
     const int32_t ticket = s_ticket;
-    if (ticket >= a.ntiles) break;
-    const TileDesc d = a.tiles[a.order[ticket]];
-    const int m = d.m;
+    if (ticket >= a.nunits) break;
+    const DuUnit U = a.units[ticket];
+    const TileDesc d = a.tiles[U.tile];
+    const int m = d.m, c0 = U.c0, c1 = U.c1;
+    for (int s = tid; s < U.nseg; s += kThreads) ssegs[s] = a.segs[U.seg0 + s];
+    __syncthreads();
+    for (int c = c0 + tid; c < c1; c += kThreads) {
+      int lo = 0, hi = U.nseg - 1;  // last segment with col0 <= c
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ssegs[mid].col0 <= c)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      vals[c - c0] = a.xt[ssegs[lo].vec_off + (c - ssegs[lo].col0)];
+    }
+    __syncthreads();
     int G = kThreads / m;
     if (G > 16) G = 16;
     const int g = tid / m, t = tid - g * m;
     const bool active = g < G;
-    int base[VEC];
-#pragma unroll
-    for (int u = 0; u < VEC; u++) base[u] = (VEC * t + u) / m;
     T acc[VEC], cmp[VEC];
 #pragma unroll
     for (int u = 0; u < VEC; u++) acc[u] = cmp[u] = T(0);
-    const VT *P = reinterpret_cast<const VT *>(a.panels + d.data_off);
-    for (int c0 = 0; c0 < d.ncols; c0 += CHUNK) {
-      const int c1 = min(d.ncols, c0 + CHUNK);
-      __syncthreads();
-      for (int s = warp; s < d.nseg; s += kThreads / 32) {
-        const Seg sg = a.segs[d.seg0 + s];
-        const int lo = max(sg.col0, c0), hi = min(sg.col0 + sg.ncols, c1);
-        for (int c = lo + lane; c < hi; c += 32) vals[c - c0] = a.xt[sg.vec_off + (c - sg.col0)];
-      }
-      __syncthreads();
-      if (active) {
-        const int64_t f_lo = (static_cast<int64_t>(c0) * m) / VEC;
-        const int64_t f_hi = (static_cast<int64_t>(c1) * m + VEC - 1) / VEC;
-        int64_t q = f_lo > t ? (f_lo - t + m - 1) / m : 0;
-        q += ((g - static_cast<int>(q % G)) % G + G) % G;
-        auto consume = [&](const VT &v, int64_t qq) {
-          const T *e = reinterpret_cast<const T *>(&v);
-#pragma unroll
-          for (int u = 0; u < VEC; u++) {
-            const int c = base[u] + static_cast<int>(VEC * qq);
-            if (c >= c0 && c < c1) {
-              if (COMP)
-                dot2_step(acc[u], cmp[u], e[u], vals[c - c0]);
-              else
-                acc[u] = fma_(e[u], vals[c - c0], acc[u]);
-            }
-          }
-        };
-        const int64_t step = static_cast<int64_t>(m) * G;
-        int64_t f = t + m * q;
-        for (; f + 3 * step < f_hi; f += 4 * step, q += 4 * G) {
-          VT v0 = ld_stream(P + f), v1 = ld_stream(P + f + step);
-          VT v2 = ld_stream(P + f + 2 * step), v3 = ld_stream(P + f + 3 * step);
-          consume(v0, q);
-          consume(v1, q + G);
-          consume(v2, q + 2 * G);
-          consume(v3, q + 3 * G);
-        }
-        for (; f < f_hi; f += step, q += G) consume(ld_stream(P + f), q);
-      }
-    }
-    __syncthreads();
     if (active) {
+      int base[VEC];
+#pragma unroll
+      for (int u = 0; u < VEC; u++) base[u] = (VEC * t + u) / m;
+      const VT *P = reinterpret_cast<const VT *>(a.panels + d.data_off);
+      const int64_t f_lo = (static_cast<int64_t>(c0) * m) / VEC;
+      const int64_t f_hi = (static_cast<int64_t>(c1) * m + VEC - 1) / VEC;
+      int64_t q = f_lo > t ? (f_lo - t + m - 1) / m : 0;
+      q += ((g - static_cast<int>(q % G)) % G + G) % G;
+      auto consume = [&](const VT &v, int64_t qq) {
+        const T *e = reinterpret_cast<const T *>(&v);
+#pragma unroll
+        for (int u = 0; u < VEC; u++) {
+          const int c = base[u] + static_cast<int>(VEC * qq);
+          if (c >= c0 && c < c1) {
+            if (COMP)
+              dot2_step(acc[u], cmp[u], e[u], vals[c - c0]);
+            else
+              acc[u] = fma_(e[u], vals[c - c0], acc[u]);
+          }
+        }
+      };
+      const int64_t step = static_cast<int64_t>(m) * G;
+      int64_t f = t + m * q;
+      for (; f + 3 * step < f_hi; f += 4 * step, q += 4 * G) {
+        VT v0 = ld_stream(P + f), v1 = ld_stream(P + f + step);
+        VT v2 = ld_stream(P + f + 2 * step), v3 = ld_stream(P + f + 3 * step);
+        consume(v0, q);
+        consume(v1, q + G);
+        consume(v2, q + 2 * G);
+        consume(v3, q + 3 * G);
+      }
+      for (; f < f_hi; f += step, q += G) consume(ld_stream(P + f), q);
 #pragma unroll
       for (int u = 0; u < VEC; u++) {
         part[g * VEC * m + VEC * t + u] = acc[u];
@@ -231,21 +239,55 @@ __global__ void __launch_bounds__(kThreads) du_pass_kernel(DuArgs<T> a) {
       }
     }
     __syncthreads();
+    T s = T(0), c = T(0);
     if (tid < m) {
-      T s = T(0), c = T(0);
       for (int gg = 0; gg < G; gg++)
 #pragma unroll
         for (int k = 0; k < VEC; k++) {
           const int idx = gg * VEC * m + tid + k * m;
           if (COMP) {
-            T p = part[idx], tt = s + p, z = tt - s;
+            const T p = part[idx], tt = s + p, z = tt - s;
             c += ((s - (tt - z)) + (p - z)) + partc[idx];
             s = tt;
           } else {
             s += part[idx];
           }
         }
-      a.y[a.tmap0[d.row0 + tid]] = COMP ? s + c : s;
+    }
+    if (U.nslots == 1) {
+      if (tid < m) a.y[a.tmap0[d.row0 + tid]] = COMP ? s + c : s;
+      continue;  // the ticket read at the top of the loop is behind a barrier
+    }
+    const int64_t pbase = U.part_off + static_cast<int64_t>(U.slot) * m + tid;
+    if (tid < m) {
+      if (COMP) {
+        a.part[2 * pbase] = s;
+        a.part[2 * pbase + 1] = c;
+      } else {
+        a.part[pbase] = s;
+      }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&a.tile_cnt[U.tile], 1) == U.nslots - 1;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      if (tid < m) {
+        T ts = T(0), tc = T(0);
+        for (int sl = 0; sl < U.nslots; sl++) {
+          const int64_t idx = U.part_off + static_cast<int64_t>(sl) * m + tid;
+          if (COMP) {
+            const T p = __ldcg(a.part + 2 * idx), tt = ts + p, z = tt - ts;
+            tc += ((ts - (tt - z)) + (p - z)) + __ldcg(a.part + 2 * idx + 1);
+            ts = tt;
+          } else {
+            ts += __ldcg(a.part + idx);
+          }
+        }
+        a.y[a.tmap0[d.row0 + tid]] = COMP ? ts + tc : ts;
+      }
+      if (tid == 0) a.tile_cnt[U.tile] = 0;
     }
   }
 }
@@ -272,31 +314,43 @@ int occupancy_du(bool f64, bool comp) {
 
 template <typename T, bool COMP>
 static cudaError_t run(const DevPlan &p, const T *panels, const T *vdata, T *xt, const T *x, T *y,
-                       int grid_v, int grid_du, cudaStream_t s) {
+                       int grid_v, int grid_du, cudaStream_t s, cudaEvent_t *ev, int *launches) {
   int gp = static_cast<int>((p.x_len + kThreads - 1) / kThreads);
   if (gp > 4096) gp = 4096;
+  int nl = 0;
+  if (ev) cudaEventRecord(ev[0], s);
   permute_x_kernel<T><<<gp, kThreads, 0, s>>>(x, p.smap0, p.n, p.x_len, xt, p.counter);
-  if (p.nwarps > 0) v_pass_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.warp_begin, xt);
-  DuArgs<T> a{panels, p.tiles, p.order, p.ntiles, p.segs, xt, p.tmap0, y, p.counter};
+  nl++;
+  if (ev) cudaEventRecord(ev[1], s);
+  if (p.vunits && !p.warp_begin_empty) {
+    v_pass_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.warp_begin, xt);
+    nl++;
+  }
+  if (ev) cudaEventRecord(ev[2], s);
+  DuArgs<T> a{panels, p.tiles, p.units, p.nunits, p.segs, xt, p.tmap0, y, p.counter,
+              static_cast<T *>(p.part), p.tile_cnt};
   du_pass_kernel<T, COMP><<<grid_du, kThreads, 0, s>>>(a);
+  nl++;
+  if (ev) cudaEventRecord(ev[3], s);
+  if (launches) *launches = nl;
   return cudaGetLastError();
 }
 
 cudaError_t launch_matvec(bool f64, bool comp, const DevPlan &p, const void *panels,
                           const void *vdata, void *xt, const void *x, void *y, int grid_v,
-                          int grid_du, cudaStream_t stream) {
+                          int grid_du, cudaStream_t stream, cudaEvent_t *ev, int *launches) {
   if (f64)
     return run<double, false>(p, static_cast<const double *>(panels),
                               static_cast<const double *>(vdata), static_cast<double *>(xt),
                               static_cast<const double *>(x), static_cast<double *>(y), grid_v,
-                              grid_du, stream);
+                              grid_du, stream, ev, launches);
   if (comp)
     return run<float, true>(p, static_cast<const float *>(panels), static_cast<const float *>(vdata),
                             static_cast<float *>(xt), static_cast<const float *>(x),
-                            static_cast<float *>(y), grid_v, grid_du, stream);
+                            static_cast<float *>(y), grid_v, grid_du, stream, ev, launches);
   return run<float, false>(p, static_cast<const float *>(panels), static_cast<const float *>(vdata),
                            static_cast<float *>(xt), static_cast<const float *>(x),
-                           static_cast<float *>(y), grid_v, grid_du, stream);
+                           static_cast<float *>(y), grid_v, grid_du, stream, ev, launches);
 }
 
 // ---------------------------------------------------------------------------

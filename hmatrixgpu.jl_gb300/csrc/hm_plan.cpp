@@ -21,6 +21,9 @@ namespace hm {
 
 static constexpr int kMaxTileRows = 128;
 static constexpr int64_t kVUnitBytes = 64 * 1024;
+static constexpr int64_t kUnitBytes = 128 * 1024;
+static constexpr int32_t kUnitCols = 4096;  // == columns of the kernel's shared vector cache (FP32)
+static constexpr int32_t kUnitSegs = 512;   // == segment slots in shared memory
 
 static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
@@ -152,6 +155,46 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     return static_cast<int64_t>(p.tiles[a].m) * p.tiles[a].ncols >
            static_cast<int64_t>(p.tiles[b].m) * p.tiles[b].ncols;
   });
+
+  // ---- near/U units: column slices of at most kUnitBytes of panel, at most
+  // kUnitCols columns and kUnitSegs segments each ------------------------------
+  p.units.clear();
+  p.part_len = 0;
+  for (int32_t ti : p.order) {
+    const TileDesc &d = p.tiles[ti];
+    const int64_t bytes = static_cast<int64_t>(d.m) * d.ncols * esize;
+    int32_t want = static_cast<int32_t>(std::max<int64_t>(1, (bytes + kUnitBytes - 1) / kUnitBytes));
+    int32_t cols_per = std::max(1, (d.ncols + want - 1) / std::max(1, want));
+    cols_per = std::min(cols_per, vec == 4 ? kUnitCols : kUnitCols / 2);
+    std::vector<DuUnit> tu;
+    int32_t c0 = 0, s = d.seg0;
+    do {
+      int32_t c1 = std::min(d.ncols, c0 + cols_per);
+      while (s < d.seg0 + d.nseg && p.segs[s].col0 + p.segs[s].ncols <= c0) s++;
+      int32_t e = s;
+      while (e < d.seg0 + d.nseg && p.segs[e].col0 < c1) e++;
+      if (e - s > kUnitSegs) {  // too many segments: end the unit at a segment end
+        e = s + kUnitSegs;
+        c1 = std::min(c1, p.segs[e - 1].col0 + p.segs[e - 1].ncols);
+      }
+      DuUnit u{};
+      u.tile = ti;
+      u.c0 = c0;
+      u.c1 = c1;
+      u.seg0 = s;
+      u.nseg = e - s;
+      tu.push_back(u);
+      c0 = c1;
+    } while (c0 < d.ncols);
+    const int32_t ns = static_cast<int32_t>(tu.size());
+    for (int32_t q = 0; q < ns; q++) {
+      tu[q].slot = q;
+      tu[q].nslots = ns;
+      tu[q].part_off = ns > 1 ? p.part_len : -1;
+    }
+    if (ns > 1) p.part_len += static_cast<int64_t>(ns) * d.m;
+    p.units.insert(p.units.end(), tu.begin(), tu.end());
+  }
 
   // ---- V pass -----------------------------------------------------------------------
   p.v_off.assign(na, 0);

@@ -238,13 +238,6 @@ void build_blocks(const Tree &X, const Tree &Y, double eta, bool merge, Blocks &
 // ---------------------------------------------------------------------------
 // C ABI: trees and blocks
 // ---------------------------------------------------------------------------
-struct hmgpu_tree {
-  hm::Tree t;
-};
-struct hmgpu_blocks {
-  hm::Blocks b;
-};
-
 extern "C" {
 
 const char *hmgpu_last_error(void) { return hm::g_err.c_str(); }

@@ -27,9 +27,14 @@ def sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
+# Per-file flags: the assembly kernels must not contract a*b+c into an FMA, so
+# that matrix entries and ACA residuals round exactly as the reference's do.
+PER_FILE = {"hm_build.cu": ["--fmad=false"]}
+
+
 def _compile(src, extra):
     obj = os.path.join(BUILD, src + ".o")
-    cmd = [nvcc()] + ARCH + COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
+    cmd = [nvcc()] + ARCH + COMMON + PER_FILE.get(src, []) + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -70,6 +70,8 @@ SIGNATURES = {
     "hmgpu_matvec": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64, VP]),
     "hmgpu_matvec_host": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64]),
     "hmgpu_hmatrix_info": (C.c_int, [VP, C.POINTER(Info)]),
+    "hmgpu_hmatrix_set_profiling": (C.c_int, [VP, C.c_int]),
+    "hmgpu_hmatrix_phase_times": (C.c_int, [VP, F64P, I64P, I64P]),
     "hmgpu_hmatrix_blocks": (C.c_int, [VP, I64P, I64P]),
     "hmgpu_hmatrix_index_maps": (C.c_int, [VP, I64P, I64P]),
     "hmgpu_hmatrix_block_factors": (C.c_int, [VP, C.c_int64, F64P, F64P]),

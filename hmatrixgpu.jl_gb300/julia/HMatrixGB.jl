@@ -1,0 +1,215 @@
+"""
+    HMatrixGB
+
+Julia binding of libhmgpu (include/hmgpu.h): the H-matrix path of HMatrixGPU.jl
+— ClusterTree, BlockTree, HMatrix assembly and mul!(y, H, x) / H * x — running
+on a GB300 (sm_103a) through a C ABI. The API keeps the reference's names,
+keyword arguments and semantics (src/tree.jl:45, src/block.jl:31,
+src/hmatrix.jl:72, src/mult.jl:159, :203).
+
+Two ways in:
+  * `HMatrixGB.HMatrix(kernel, X, Y; eta, eps, precision)` assembles on the
+    device (batched ACA+ and QR/SVD recompression) for a named kernel;
+  * `HMatrixGB.HMatrix(H::HMatrixGPU.HMatrix{Float64})` imports a matrix the
+    reference already assembled, in its flattened layout, unchanged.
+
+`mul!(y::CuArray, H, x::CuArray)` is stream-ordered on CUDA.jl's task-local
+stream and returns without synchronising, as the reference's device mul! does.
+"""
+module HMatrixGB
+
+using LinearAlgebra
+import LinearAlgebra: mul!
+import Base: *
+
+const libhmgpu = get(ENV, "HMGPU_LIB",
+                     joinpath(@__DIR__, "..", "lib", "libhmgpu.so"))
+
+const HMGPU_F64 = Int32(0)
+const HMGPU_F32 = Int32(1)
+const HMGPU_MIXED = Int32(2)
+
+const KERNELS = Dict(:explicit => Int32(0), :laplace => Int32(1), :yukawa => Int32(2),
+                     :log2d => Int32(3), :vector_r => Int32(4), :dipolar => Int32(5))
+
+struct Options
+    precision::Int32
+    compensated::Int32
+    keep_factors::Int32
+    reserved::Int32
+end
+
+struct KernelDesc
+    kind::Int32
+    reserved::Int32
+    X::Ptr{Float64}
+    nX::Int64
+    Y::Ptr{Float64}
+    nY::Int64
+    A::Ptr{Float64}
+    lda::Int64
+end
+
+struct HMGPUError <: Exception
+    code::Int
+    msg::String
+end
+
+function check(rc)
+    if rc != 0
+        msg = unsafe_string(ccall((:hmgpu_last_error, libhmgpu), Cstring, ()))
+        throw(HMGPUError(rc, msg))
+    end
+    return nothing
+end
+
+# ---------------------------------------------------------------------------
+# ClusterTree(coordinates; max_points_per_leaf=32, dims=1)   (src/tree.jl:45)
+# ---------------------------------------------------------------------------
+mutable struct ClusterTree
+    handle::Ptr{Cvoid}
+    index_map::Vector{Int}
+    coordinates::Matrix{Float64}
+end
+
+function ClusterTree(coordinates::AbstractMatrix; max_points_per_leaf::Int=32, dims::Int=1)
+    dims <= 0 && error("Parameter `dims` must be a positive integer.")
+    c = Matrix{Float64}(coordinates)
+    size(c, 1) == 3 || error("coordinates must be 3 x N")
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hmgpu_tree_build, libhmgpu), Cint,
+                (Ptr{Float64}, Int64, Int64, Int64, Ref{Ptr{Cvoid}}),
+                c, size(c, 2), max_points_per_leaf, dims, h))
+    nn, il = Ref{Int64}(0), Ref{Int64}(0)
+    check(ccall((:hmgpu_tree_info, libhmgpu), Cint,
+                (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
+                h[], nn, il, C_NULL, C_NULL, C_NULL))
+    imap = Vector{Int}(undef, il[])
+    check(ccall((:hmgpu_tree_export, libhmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Int8}, Ptr{Int64},
+                 Ptr{Int64}, Ptr{Float64}, Ptr{Float64}),
+                h[], imap, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL))
+    t = ClusterTree(h[], imap, c)
+    finalizer(t) do t
+        ccall((:hmgpu_tree_free, libhmgpu), Cint, (Ptr{Cvoid},), t.handle)
+    end
+    return t
+end
+
+"""info(tree) (src/tree.jl:153-187)"""
+function info(t::ClusterTree)
+    d, mx, mn = Ref{Int64}(0), Ref{Int64}(0), Ref{Int64}(0)
+    check(ccall((:hmgpu_tree_info, libhmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}, Ref{Int64}, Ref{Int64}, Ref{Int64}),
+                t.handle, C_NULL, C_NULL, d, mx, mn))
+    return Dict(:depth => d[], :max_points => mx[], :min_points => mn[])
+end
+
+# ---------------------------------------------------------------------------
+# HMatrix
+# ---------------------------------------------------------------------------
+mutable struct HMatrix{T<:AbstractFloat}
+    handle::Ptr{Cvoid}
+    m::Int
+    n::Int
+end
+
+Base.size(H::HMatrix) = (H.m, H.n)
+Base.size(H::HMatrix, d) = size(H)[d]
+Base.eltype(::HMatrix{T}) where {T} = T
+
+_T(precision) = precision == :f64 ? Float64 : Float32
+_mode(precision) = precision == :f64 ? HMGPU_F64 : precision == :f32 ? HMGPU_F32 : HMGPU_MIXED
+
+function _wrap(::Type{T}, h) where {T}
+    info_buf = zeros(UInt8, 256)
+    check(ccall((:hmgpu_hmatrix_info, libhmgpu), Cint, (Ptr{Cvoid}, Ptr{UInt8}), h, info_buf))
+    m = reinterpret(Int64, info_buf[1:8])[1]
+    n = reinterpret(Int64, info_buf[9:16])[1]
+    H = HMatrix{T}(h, m, n)
+    finalizer(H) do H
+        ccall((:hmgpu_hmatrix_free, libhmgpu), Cint, (Ptr{Cvoid},), H.handle)
+    end
+    return H
+end
+
+"""
+    HMatrix(kind::Symbol, Xpts, Ypts, X::ClusterTree, Y::ClusterTree;
+            eta=1.5, eps=1e-5, svd_recompress=true, precision=:f64)
+
+HMatrix(K, X, Y; eta, eps) (src/hmatrix.jl:72) with K the named kernel over
+the target points `Xpts` and source points `Ypts` (3 x N), assembled on the GPU.
+"""
+function HMatrix(kind::Symbol, Xpts::AbstractMatrix, Ypts::AbstractMatrix, X::ClusterTree,
+                 Y::ClusterTree; eta=1.5, eps=1e-5, svd_recompress=true, precision=:f64)
+    xp, yp = Matrix{Float64}(Xpts), Matrix{Float64}(Ypts)
+    o = Ref(Options(_mode(precision), 0, 0, 0))
+    k = Ref(KernelDesc(KERNELS[kind], 0, pointer(xp), size(xp, 2), pointer(yp), size(yp, 2),
+                       C_NULL, 0))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve xp yp check(ccall((:hmgpu_hmatrix_build, libhmgpu), Cint,
+                                   (Ref{Options}, Ref{KernelDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Float64,
+                                    Float64, Cint, Ref{Ptr{Cvoid}}),
+                                   o, k, X.handle, Y.handle, eta, eps, svd_recompress, h))
+    return _wrap(_T(precision), h[])
+end
+
+"""
+    HMatrix(Hf; precision=:f64)
+
+Imports a flattened `HMatrixGPU.HMatrix{Float64}` (src/hmatrix.jl:46-57) as it
+is: index maps, dense/U/V tables and data (CPU or device arrays).
+"""
+function HMatrix(Hf; precision=:f64)
+    m, n = size(Hf.K)
+    A(x) = Array(x)
+    tm, sm = A(Hf.target_index_map), A(Hf.source_index_map)
+    di, ui, vi = A(Hf.dense_block_indices), A(Hf.U_block_indices), A(Hf.V_block_indices)
+    dd, ud, vd = A(Hf.dense_blocks), A(Hf.U_matrices), A(Hf.V_matrices)
+    o = Ref(Options(_mode(precision), 0, 0, 0))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    nA = size(ui, 1) == 5 ? size(ui, 2) : 0
+    R = size(vi, 1) == 3 ? size(vi, 2) : 0
+    check(ccall((:hmgpu_hmatrix_import_flat, libhmgpu), Cint,
+                (Ref{Options}, Int64, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Int64,
+                 Ptr{Float64}, Int64, Ptr{Int64}, Int64, Ptr{Float64}, Int64, Ptr{Int64}, Int64,
+                 Ptr{Float64}, Int64, Ref{Ptr{Cvoid}}),
+                o, m, n, tm, sm, di, size(di, 2), dd, length(dd), ui, nA, ud, length(ud), vi, R,
+                vd, length(vd), h))
+    return _wrap(_T(precision), h[])
+end
+
+# ---------------------------------------------------------------------------
+# mul!(y, H, x) and H * x   (src/mult.jl:159-209)
+# ---------------------------------------------------------------------------
+# Device arrays: any array type whose `pointer` is a device address (CuArray
+# via CUDA.jl's `CuPtr`); the stream is CUDA.jl's task-local stream.
+function mul!(y::AbstractVecOrMat{T}, H::HMatrix{T}, x::AbstractVecOrMat{T}) where {T}
+    nrhs = size(x, 2)
+    size(x, 1) == H.n && size(y, 1) == H.m && size(y, 2) == nrhs ||
+        throw(DimensionMismatch("H is $(size(H)), x is $(size(x)), y is $(size(y))"))
+    if y isa Array
+        check(ccall((:hmgpu_matvec_host, libhmgpu), Cint,
+                    (Ptr{Cvoid}, Ptr{T}, Ptr{T}, Int64, Int64, Int64),
+                    H.handle, x, y, nrhs, stride(x, 2), stride(y, 2)))
+    else
+        stream = _stream()
+        check(ccall((:hmgpu_matvec, libhmgpu), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int64, Int64, Int64, Ptr{Cvoid}),
+                    H.handle, _devptr(x), _devptr(y), nrhs, stride(x, 2), stride(y, 2), stream))
+    end
+    return y
+end
+
+function *(H::HMatrix{T}, x::AbstractVecOrMat{T}) where {T}
+    y = similar(x, T, size(x, 2) == 1 && x isa AbstractVector ? (H.m,) : (H.m, size(x, 2)))
+    return mul!(y, H, x)
+end
+
+# CUDA.jl hooks, resolved at run time so that this file loads without CUDA.jl.
+_devptr(a) = reinterpret(Ptr{Cvoid}, UInt(Base.unsafe_convert(Main.CUDA.CuPtr{eltype(a)}, a)))
+_stream() = reinterpret(Ptr{Cvoid}, Main.CUDA.stream().handle)
+
+export ClusterTree, HMatrix, info
+
+end # module

@@ -179,6 +179,15 @@ typedef struct {
 /* info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures. */
 int hmgpu_hmatrix_info(const hmgpu_hmatrix *H, hmgpu_info *info);
 
+/* Phase timing (no counterpart in the reference): while on, every product
+ * records CUDA events on its stream between its kernels.  phase_times
+ * synchronises, returns the summed device time in milliseconds of the phases
+ * [x permutation, V pass, near/U pass] and the kernel launches and products
+ * recorded since profiling was switched on, and clears them. */
+int hmgpu_hmatrix_set_profiling(hmgpu_hmatrix *H, int on);
+int hmgpu_hmatrix_phase_times(hmgpu_hmatrix *H, double *ms3, int64_t *launches,
+                              int64_t *products);
+
 /* Block lists of the H-matrix in the reference's order: dense blocks (tree
  * dense leaves, then admissible leaves that did not compress) as 4 x nD
  * (row_start,row_end,col_start,col_end), low-rank blocks as 5 x nA

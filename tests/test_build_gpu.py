@@ -1,0 +1,153 @@
+"""On-device assembly (batched ACA+, QR+SVD recompression, dense generation)
+against the oracle and the reference's own known answers."""
+import numpy as np
+import pytest
+
+import hmgpu
+from oracle import oracle as O
+from tests import geometry
+
+pytestmark = pytest.mark.gpu
+
+
+def _inv_sq_block():
+    N = 100
+    i = np.arange(1, N + 1, dtype=np.float64)
+    d = i[:, None] - i[None, :]
+    with np.errstate(divide="ignore"):
+        K = np.where(d != 0, N / d ** 2, 0.0)
+    return K[N - 30:, :30]
+
+
+def test_aca_plus_known_answer_and_oracle(gpu):
+    """test/test_aca.jl through the device ACA; pivots and factors equal the oracle's."""
+    blk = _inv_sq_block()
+    eps = 1e-6
+    U, V = hmgpu.ACA_plus(30, 30, lambda I: blk[I - 1, :], lambda J: blk[:, J - 1], eps / 10.0)
+    Uo, Vo = O.aca_plus(O.Kernel("explicit", A=blk), np.arange(1, 31), np.arange(1, 31), eps / 10.0)
+    x = np.random.default_rng(10).random(30)
+    assert U.shape[1] < 30
+    assert np.linalg.norm(U @ V - blk, 2) < eps / 100
+    assert np.max(np.abs(U @ (V @ x) - blk @ x)) < eps / 100
+    assert U.shape == Uo.shape and V.shape == Vo.shape
+    np.testing.assert_array_equal(U, Uo)  # same operations in the same order
+    np.testing.assert_array_equal(V, Vo)
+    Us, Vs = hmgpu.SVD_recompress(U, V, eps / 10)
+    Uso, Vso = O.svd_recompress(U, V, eps / 10)
+    assert Us.shape == Uso.shape and U.shape[1] >= Us.shape[1]
+    assert np.max(np.abs(Us @ (Vs @ x) - blk @ x)) < eps / 100
+    np.testing.assert_allclose(Us @ Vs, Uso @ Vso, rtol=0, atol=1e-13 * np.abs(blk).max())
+
+
+def test_svd_recompress_random(gpu):
+    rng = np.random.default_rng(5)
+    for m, n, k, eps in [(50, 40, 9, 1e-3), (7, 90, 7, 0.0), (64, 64, 30, 1e-8)]:
+        U = rng.standard_normal((m, k)) * np.logspace(0, -6, k)
+        V = rng.standard_normal((k, n))
+        Us, Vs = hmgpu.SVD_recompress(U, V, eps)
+        Uo, Vo = O.svd_recompress(U, V, eps)
+        assert Us.shape[1] == Uo.shape[1], (m, n, k, eps)
+        np.testing.assert_allclose(Us @ Vs, Uo @ Vo, rtol=0, atol=1e-12 * np.abs(U @ V).max())
+
+
+def _oracle_h(kind, P, leaf, eta, eps, dims=1):
+    K = O.Kernel(kind, P.T, P.T)
+    X = O.Tree(P.T, leaf)
+    Y = O.Tree(P.T, leaf, dims)
+    return K, O.HMatrix(K, X, Y, eta=eta, eps=eps, nthreads=8)
+
+
+def _dev_h(kind, P, leaf, eta, eps, dims=1, precision="f64", **kw):
+    X = hmgpu.ClusterTree(P, max_points_per_leaf=leaf)
+    Y = hmgpu.ClusterTree(P, max_points_per_leaf=leaf, dims=dims)
+    return hmgpu.HMatrix(hmgpu.Kernel(kind, P), X, Y, eta=eta, eps=eps, precision=precision, **kw)
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def test_circle_log_kernel_reference_checks(gpu):
+    """test/test_hmatrix.jl:27-50 and :160-165 with the device-built H-matrix."""
+    import torch
+    P = geometry.circle(1000)
+    K, Ho = _oracle_h("log2d", P, 64, 1.5, 1e-6)
+    H = _dev_h("log2d", P, 64, 1.5, 1e-6)
+    assert H.info()["compression_ratio"] > 3
+    x = np.random.default_rng(10).random(1000)
+    y = (H * torch.tensor(x, device=gpu)).cpu().numpy()
+    assert np.max(np.abs(K.matvec(x) - y)) < 1e-5            # isapprox(K*x, H*x; atol=1e-5)
+    assert np.max(np.abs(Ho.mul(x) - y)) < 1e-9              # GPU vs CPU H*x, atol 1e-9
+
+
+def test_partition_and_ranks_match_oracle(gpu):
+    P = geometry.cube(4096, seed=0)
+    K, Ho = _oracle_h("laplace", P, 32, 2.0, 1e-6)
+    H = _dev_h("laplace", P, 32, 2.0, 1e-6, keep_factors=True)
+    d, a = H.blocks()
+    # dense list: tree dense leaves, then admissible leaves that did not compress
+    np.testing.assert_array_equal(d, Ho.dense_block_indices[:, :4])
+    np.testing.assert_array_equal(a[:, :2], Ho.U_block_indices[:, :2])
+    ranks_o = Ho.U_block_indices[:, 3] - Ho.U_block_indices[:, 2] + 1
+    assert np.mean(a[:, 4] == ranks_o) > 0.99
+    x = np.random.default_rng(1).standard_normal(4096)
+    import torch
+    y = (H * torch.tensor(x, device=gpu)).cpu().numpy()
+    yo = Ho.mul(x)
+    yd = K.matvec(x)
+    assert rel(y, yd) < 1e-5 and rel(yo, yd) < 1e-5
+    assert rel(y, yo) < 1e-6
+    # factors of one block against the oracle's
+    U, V = H.block_factors(0)
+    r = a[0, 4]
+    uo = Ho.U_block_indices[0, 4]
+    Uo = Ho.U_matrices[uo:uo + U.size].reshape(U.shape)
+    vo = Ho.V_block_indices[Ho.U_block_indices[0, 2] - 1, 2]
+    Vo = Ho.V_matrices[vo:vo + V.size].reshape(V.shape)
+    np.testing.assert_allclose(U @ V, Uo @ Vo, rtol=0, atol=1e-12 * np.abs(Uo @ Vo).max())
+
+
+@pytest.mark.parametrize("kind,geom,leaf,eta,eps,dims", [
+    ("vector_r", "circle", 64, 1.5, 1e-6, 3),
+    ("yukawa", "sphere", 32, 1.0, 1e-5, 1),
+    ("dipolar", "cube", 16, 1.0, 1e-6, 3),
+    ("laplace", "film", 64, 2.0, 1e-4, 1),
+])
+def test_kernels_against_dense(gpu, kind, geom, leaf, eta, eps, dims):
+    import torch
+    P = {"circle": geometry.circle(1000), "sphere": geometry.sphere(3000, seed=2),
+         "cube": geometry.cube(700, seed=3), "film": geometry.film(60, 50)}[geom]
+    Kd = O.Kernel(kind, P.T, P.T)
+    X = hmgpu.ClusterTree(P, max_points_per_leaf=leaf, dims=3 if kind == "dipolar" else 1)
+    Y = hmgpu.ClusterTree(P, max_points_per_leaf=leaf, dims=dims)
+    H = hmgpu.HMatrix(hmgpu.Kernel(kind, P), X, Y, eta=eta, eps=eps, precision="f64")
+    assert H.shape == Kd.shape
+    x = np.random.default_rng(4).standard_normal(Kd.shape[1])
+    y = (H * torch.tensor(x, device=gpu)).cpu().numpy()
+    yd = Kd.matvec(x)
+    assert np.max(np.abs(y - yd)) < 50 * eps * max(1.0, np.abs(yd).max())
+    if kind == "vector_r":
+        assert H.info()["compression_ratio"] > 3  # test/test_hmatrix_vector.jl:39
+
+
+def test_explicit_matrix_and_f32(gpu):
+    import torch
+    P = geometry.cube(1500, seed=9)
+    Kd = O.Kernel("laplace", P.T, P.T)
+    A = Kd.dense()
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=32)
+    He = hmgpu.HMatrix(A, T, T, eta=2.0, eps=1e-6, precision="f64")
+    Hk = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=1e-6, precision="f64")
+    x = torch.randn(1500, dtype=torch.float64, device=gpu)
+    assert torch.equal(He * x, Hk * x)  # identical entries -> identical matrix
+    H32 = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=1e-6, precision="f32")
+    y32 = (H32 * x.float()).double()
+    assert rel(y32.cpu().numpy(), (Hk * x).cpu().numpy()) < 1e-5
+
+
+def test_build_rejects_mismatched_sizes(gpu):
+    P = geometry.cube(100)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=16)
+    T3 = hmgpu.ClusterTree(P, max_points_per_leaf=16, dims=3)
+    with pytest.raises(hmgpu.HMGPUError, match="does not match"):
+        hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T3, eta=2.0, eps=1e-6)

@@ -33,7 +33,7 @@ def _cases():
     yield "film_laplace", O.Kernel("laplace", f.T, f.T), O.Tree(f.T, 64), O.Tree(f.T, 64), 2.0, 1e-4
 
 
-CASES = {name: args for name, *args in [(c[0], c[1:]) for c in _cases()]}
+CASES = {c[0]: c[1:] for c in _cases()}
 
 
 @pytest.fixture(scope="module", params=sorted(CASES))
