@@ -105,6 +105,14 @@ def film_points():
     return geometry.film(GRID, GRID, spacing=1.0, jitter=0.05, seed=1)
 
 
+def set_grid(g):
+    """A smaller film (g x g) for profiling captures; the headline is g = 1024."""
+    global GRID, WORKLOAD
+    GRID = g
+    if g != 1024:
+        WORKLOAD = WORKLOAD.replace("film-2^20", f"film-{g}x{g}")
+
+
 def cpu_sample(threads, target_s=15.0):
     """Times the oracle's restatement of the reference CPU mul! (src/mult.jl:6-32)
     on every SAMPLE_STRIDE-th block of the workload's matrix; returns products/s
@@ -277,7 +285,9 @@ def main():
     ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--grid", type=int, default=1024, help="film side (1024 = the headline workload)")
     args = ap.parse_args()
+    set_grid(args.grid)
     if args.impl == "reference":
         run_reference(args)
     else:
