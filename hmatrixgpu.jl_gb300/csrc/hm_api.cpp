@@ -7,6 +7,10 @@
 
 #include "hm_api.h"
 
+// From this many right-hand sides on, one multi-RHS pass (matrix read once,
+// compute bound) beats repeated single-RHS passes (matrix read per column).
+static constexpr int64_t kMultiRhsFrom = 3;
+
 namespace hm {
 
 int cuda_fail(cudaError_t e, const char *what) {
@@ -326,17 +330,47 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
   const bool comp = !f64 && (H.opt.compensated || H.opt.precision == HMGPU_MIXED);
   const size_t es = f64 ? 8 : 4;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  for (int64_t k = 0; k < nrhs; k++) {
-    cudaEvent_t *ev = nullptr;
-    if (H.profiling) {
-      if (H.prof_used == H.prof_ev.size()) {
-        std::array<cudaEvent_t, 4> q;
-        for (auto &e : q)
-          if (cudaEventCreate(&e) != cudaSuccess) return hm::fail(HMGPU_ERR_CUDA, "cudaEventCreate failed");
-        H.prof_ev.push_back(q);
-      }
-      ev = H.prof_ev[H.prof_used++].data();
+  auto next_events = [&](cudaEvent_t **ev) -> int {
+    *ev = nullptr;
+    if (!H.profiling) return HMGPU_OK;
+    if (H.prof_used == H.prof_ev.size()) {
+      std::array<cudaEvent_t, 4> q;
+      for (auto &e : q)
+        if (cudaEventCreate(&e) != cudaSuccess) return hm::fail(HMGPU_ERR_CUDA, "cudaEventCreate failed");
+      H.prof_ev.push_back(q);
     }
+    *ev = H.prof_ev[H.prof_used++].data();
+    return HMGPU_OK;
+  };
+  if (nrhs >= kMultiRhsFrom) {
+    // several right-hand sides: one pass per rhs_per_pass() columns, the
+    // matrix read once per pass (hm_multi.cu)
+    const int per = hm::rhs_per_pass();
+    if (!H.xt_multi) {
+      int rc;
+      if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es)) ||
+          (rc = H.dalloc(&H.part_multi, std::max<int64_t>(H.plan.part_len, 1) * per * es)))
+        return rc;
+      cudaMemset(H.xt_multi, 0, H.plan.xt_len * per * es);
+      H.grid_du_multi = H.num_sms * hm::occupancy_du_multi(f64);
+    }
+    for (int64_t k0 = 0; k0 < nrhs; k0 += per) {
+      cudaEvent_t *ev;
+      if (int rc = next_events(&ev)) return rc;
+      const int nr = static_cast<int>(std::min<int64_t>(per, nrhs - k0));
+      int nl = 0;
+      cudaError_t e = hm::launch_matvec_multi(
+          f64, H.dp, H.panels, H.vdata, H.xt_multi, H.part_multi,
+          static_cast<const char *>(x) + k0 * ldx * es, ldx, nr,
+          static_cast<char *>(y) + k0 * ldy * es, ldy, H.grid_v, H.grid_du_multi, s, ev, &nl);
+      if (e != cudaSuccess) return hm::cuda_fail(e, "multi-RHS matvec launch");
+      if (H.profiling) H.prof_launches += nl;
+    }
+    return HMGPU_OK;
+  }
+  for (int64_t k = 0; k < nrhs; k++) {
+    cudaEvent_t *ev;
+    if (int rc = next_events(&ev)) return rc;
     int nl = 0;
     cudaError_t e = hm::launch_matvec(f64, comp, H.dp, H.panels, H.vdata, H.xt,
                                       static_cast<const char *>(x) + k * ldx * es,

@@ -50,3 +50,15 @@ cudaError_t launch_pack_v(bool f64, const VPackJob *jobs, int64_t njobs, const d
                           void *vdata, cudaStream_t stream);
 
 }  // namespace hm
+
+namespace hm {
+// Multi-right-hand-side plain product (hm_multi.cu): up to rhs_per_pass()
+// right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values
+// and part the split-tile partials (part_len rows of rhs_per_pass() values).
+int rhs_per_pass();
+int occupancy_du_multi(bool f64);
+cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,
+                                void *xt, void *part, const void *X, int64_t ldx, int nr, void *Y,
+                                int64_t ldy, int grid_v, int grid_du, cudaStream_t s,
+                                cudaEvent_t *ev, int *launches);
+}  // namespace hm

@@ -110,3 +110,22 @@ def test_import_rejects_bad_tables(gpu):
     vi[0, 2] += 1
     with pytest.raises(hmgpu.HMGPUError, match="inconsistent|out of range"):
         hmgpu.HMatrix.from_flat(**dict(f, V_block_indices=vi))
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-5)])
+def test_many_rhs_two_passes(case, gpu, prec, tol):
+    """40 right-hand sides: one 32-wide pass and one 8-wide pass of the multi-RHS kernels."""
+    import torch
+    _, _, Ho = case
+    H = hmgpu.HMatrix.from_flat(**_flat(Ho), precision=prec)
+    X = np.random.default_rng(7).standard_normal((Ho.n, 40))
+    dt = torch.float64 if prec == "f64" else torch.float32
+    Xd = torch.tensor(X, dtype=dt, device=gpu).t().contiguous().t()
+    Y = (H * Xd).double().cpu().numpy()
+    Xr = X.astype(np.float32).astype(np.float64) if prec == "f32" else X
+    ref = np.stack([Ho.mul(Xr[:, k]) for k in range(40)], 1)
+    for k in range(40):
+        assert rel(Y[:, k], ref[:, k]) <= tol, k
+    # a single column of the batch equals the single-RHS product up to rounding
+    y0 = (H * Xd[:, 0].contiguous()).double().cpu().numpy()
+    assert rel(Y[:, 0], y0) <= tol
