@@ -160,6 +160,21 @@ int hmgpu_matvec(hmgpu_hmatrix *H, const void *x, void *y, int64_t nrhs, int64_t
 int hmgpu_matvec_host(hmgpu_hmatrix *H, const void *x, void *y, int64_t nrhs, int64_t ldx,
                       int64_t ldy);
 
+/* No counterpart in the reference. The single-right-hand-side product of
+ * hmgpu_matvec (y = H x, device pointers, stream-ordered) for callers that
+ * cannot allocate device memory while they run it -- code being captured into
+ * a CUDA graph where plain allocation is not allowed, loops that fix their
+ * memory up front, hosts whose allocator belongs to another framework. Its
+ * scratch (permuted x, t = V x, partial sums, counters) lives in one
+ * statically sized device array of HMGPU_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this library holds until the process exits; the call allocates
+ * nothing. An H-matrix needing more scratch is rejected with HMGPU_ERR_INVALID.
+ * The first call on a device looks up the array's address (make that first
+ * call before any stream capture). All calls share the array: calls that
+ * overlap on the GPU (other streams, other threads, other H-matrices) race. */
+#define HMGPU_NOALLOC_SCRATCH_BYTES (32u << 20)
+int hmgpu_matvec_noalloc(hmgpu_hmatrix *H, const void *x, void *y, void *stream);
+
 typedef struct {
   int64_t m, n;                  /* size(K)                                        */
   int64_t n_dense, n_approx;     /* full_leaves, admissible_leaves                  */
