@@ -1,6 +1,7 @@
 // C ABI of libhmgpu: H-matrix objects, import of the reference's flattened
 // layout, the product entry points and the info/export queries.
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -100,6 +101,9 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   if ((rc = upload(H, &H.dp.smap0, s0))) return rc;
   if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.counter), 64))) return rc;
   cudaMemset(H.dp.counter, 0, 64);
+  H.dp.status = H.dp.counter + 4;  // its own 16-byte slot of the same allocation
+  H.dp.grid_tma = H.num_sms * occupancy_du_tma(f64, comp);
+  if (const char *v = std::getenv("HMGPU_DU_VARIANT")) H.dp.du_variant = std::atoi(v) == 0 ? 0 : 1;
   H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
   H.dp.nwarps = p.nwarps;
   H.dp.warp_begin_empty = p.vunits.empty();
@@ -470,6 +474,23 @@ extern "C" int hmgpu_hmatrix_phase_times(hmgpu_hmatrix *h, double *ms3, int64_t 
   if (products) *products = static_cast<int64_t>(H.prof_used);
   H.prof_used = 0;
   H.prof_launches = 0;
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_status(hmgpu_hmatrix *h, int *status) {
+  if (!h || !status) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
+  HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return hm::cuda_fail(e, "cudaDeviceSynchronize");
+  int32_t v = 0;
+  e = cudaMemcpy(&v, H.dp.status, sizeof v, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return hm::cuda_fail(e, "reading the device status");
+  *status = v;
+  if (v != 0) {
+    cudaMemset(H.dp.status, 0, sizeof v);
+    return hm::fail(HMGPU_ERR_TIMEOUT, "a bounded device wait expired in a product (code " +
+                                           std::to_string(v) + ")");
+  }
   return HMGPU_OK;
 }
 

@@ -22,6 +22,9 @@ struct DevPlan {
   int32_t *tmap0 = nullptr;  // 0-based target map, length m
   int32_t *smap0 = nullptr;  // 0-based source map, length n
   int32_t *counter = nullptr;  // tile ticket of the near/U pass
+  int32_t *status = nullptr;   // device error word (0 = ok), see hmgpu_hmatrix_status
+  int du_variant = 1;          // near/U pass: 0 per-thread 16-byte loads, 1 bulk-copy pipeline
+  int grid_tma = 0;
   int64_t m = 0, n = 0, x_len = 0, xt_len = 0;
 };
 
@@ -56,6 +59,10 @@ namespace hm {
 // right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values
 // and part the split-tile partials (part_len rows of rhs_per_pass() values).
 int rhs_per_pass();
+// Bulk-copy pipelined near/U pass (hm_du_tma.cu).
+int occupancy_du_tma(bool f64, bool comp);
+cudaError_t launch_du_tma(bool f64, bool comp, const DevPlan &p, const void *panels, void *xt,
+                          void *y, int grid, cudaStream_t s);
 int occupancy_du_multi(bool f64);
 cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,
                                 void *xt, void *part, const void *X, int64_t ldx, int nr, void *Y,

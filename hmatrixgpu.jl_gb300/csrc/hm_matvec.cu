@@ -102,6 +102,19 @@ __global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ 
       if (k < U.nrows) {
         const VT *row = reinterpret_cast<const VT *>(V + U.v_off + static_cast<int64_t>(k) * U.stride);
         int p = sub;
+        for (; p + 3 * g < nv; p += 4 * g) {  // four 16-byte loads in flight per lane
+          VT a[4], b[4];
+#pragma unroll
+          for (int s = 0; s < 4; s++) a[s] = ld_stream(row + p + s * g);
+#pragma unroll
+          for (int s = 0; s < 4; s++) b[s] = __ldg(X + p + s * g);
+#pragma unroll
+          for (int s = 0; s < 4; s++) {
+            const T *ea = reinterpret_cast<const T *>(&a[s]), *eb = reinterpret_cast<const T *>(&b[s]);
+#pragma unroll
+            for (int q = 0; q < VEC; q++) acc = fma_(ea[q], eb[q], acc);
+          }
+        }
         for (; p + g < nv; p += 2 * g) {
           VT a0 = ld_stream(row + p), a1 = ld_stream(row + p + g);
           VT b0 = __ldg(X + p), b1 = __ldg(X + p + g);
@@ -327,9 +340,14 @@ static cudaError_t run(const DevPlan &p, const T *panels, const T *vdata, T *xt,
     nl++;
   }
   if (ev) cudaEventRecord(ev[2], s);
-  DuArgs<T> a{panels, p.tiles, p.units, p.nunits, p.segs, xt, p.tmap0, y, p.counter,
-              static_cast<T *>(p.part), p.tile_cnt};
-  du_pass_kernel<T, COMP><<<grid_du, kThreads, 0, s>>>(a);
+  if (p.du_variant == 1) {
+    cudaError_t e = launch_du_tma(sizeof(T) == 8, COMP, p, panels, xt, y, p.grid_tma, s);
+    if (e != cudaSuccess) return e;
+  } else {
+    DuArgs<T> a{panels, p.tiles, p.units, p.nunits, p.segs, xt, p.tmap0, y, p.counter,
+                static_cast<T *>(p.part), p.tile_cnt};
+    du_pass_kernel<T, COMP><<<grid_du, kThreads, 0, s>>>(a);
+  }
   nl++;
   if (ev) cudaEventRecord(ev[3], s);
   if (launches) *launches = nl;

@@ -194,6 +194,12 @@ typedef struct {
 /* info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures. */
 int hmgpu_hmatrix_info(const hmgpu_hmatrix *H, hmgpu_info *info);
 
+/* Device status of the products run so far (no counterpart in the reference):
+ * synchronises the device; *status = 0 if every bounded wait inside the
+ * kernels completed, else the code of the first one that expired (then
+ * returns HMGPU_ERR_TIMEOUT and clears the code). */
+int hmgpu_hmatrix_status(hmgpu_hmatrix *H, int *status);
+
 /* Phase timing (no counterpart in the reference): while on, every product
  * records CUDA events on its stream between its kernels.  phase_times
  * synchronises, returns the summed device time in milliseconds of the phases
