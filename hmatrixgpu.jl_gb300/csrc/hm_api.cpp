@@ -88,9 +88,6 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   if ((rc = upload(H, &H.dp.tiles, p.tiles))) return rc;
   if ((rc = upload(H, &H.dp.units, p.units))) return rc;
   if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
-  if ((rc = H.dalloc(&H.dp.part, std::max<int64_t>(p.part_len, 1) * es * (comp ? 2 : 1)))) return rc;
-  if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.tile_cnt), p.tiles.size() * sizeof(int32_t)))) return rc;
-  cudaMemset(H.dp.tile_cnt, 0, p.tiles.size() * sizeof(int32_t));
   H.dp.nunits = static_cast<int32_t>(p.units.size());
   if ((rc = upload(H, &H.dp.vunits, p.vunits))) return rc;
   if ((rc = upload(H, &H.dp.warp_begin, p.warp_begin))) return rc;
@@ -102,8 +99,6 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.counter), 64))) return rc;
   cudaMemset(H.dp.counter, 0, 64);
   H.dp.status = H.dp.counter + 4;  // its own 16-byte slot of the same allocation
-  H.dp.grid_tma = H.num_sms * occupancy_du_tma(f64, comp);
-  if (const char *v = std::getenv("HMGPU_DU_VARIANT")) H.dp.du_variant = std::atoi(v) == 0 ? 0 : 1;
   H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
   H.dp.nwarps = p.nwarps;
   H.dp.warp_begin_empty = p.vunits.empty();
@@ -352,9 +347,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
     const int per = hm::rhs_per_pass();
     if (!H.xt_multi) {
       int rc;
-      if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es)) ||
-          (rc = H.dalloc(&H.part_multi, std::max<int64_t>(H.plan.part_len, 1) * per * es)))
-        return rc;
+      if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es))) return rc;
       cudaMemset(H.xt_multi, 0, H.plan.xt_len * per * es);
       H.grid_du_multi = H.num_sms * hm::occupancy_du_multi(f64);
     }
@@ -364,7 +357,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
       const int nr = static_cast<int>(std::min<int64_t>(per, nrhs - k0));
       int nl = 0;
       cudaError_t e = hm::launch_matvec_multi(
-          f64, H.dp, H.panels, H.vdata, H.xt_multi, H.part_multi,
+          f64, H.dp, H.panels, H.vdata, H.xt_multi,
           static_cast<const char *>(x) + k0 * ldx * es, ldx, nr,
           static_cast<char *>(y) + k0 * ldy * es, ldy, H.grid_v, H.grid_du_multi, s, ev, &nl);
       if (e != cudaSuccess) return hm::cuda_fail(e, "multi-RHS matvec launch");

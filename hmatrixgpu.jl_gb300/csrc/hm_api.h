@@ -31,7 +31,7 @@ struct HMatrix {
   double *u64 = nullptr, *v64 = nullptr;
   std::vector<int64_t> u_src_off, v_src_off;
   // multi-right-hand-side scratch, allocated on first use
-  void *xt_multi = nullptr, *part_multi = nullptr;
+  void *xt_multi = nullptr;
   int grid_du_multi = 0;
   // staging of hmgpu_matvec_host
   void *io_x = nullptr, *io_y = nullptr;

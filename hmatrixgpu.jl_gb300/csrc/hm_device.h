@@ -11,10 +11,8 @@ struct DevPlan {
   TileDesc *tiles = nullptr;
   Seg *segs = nullptr;
   int32_t ntiles = 0;
-  DuUnit *units = nullptr;
+  RowUnit *units = nullptr;      // near/U pass work
   int32_t nunits = 0;
-  void *part = nullptr;          // partial row sums of split tiles
-  int32_t *tile_cnt = nullptr;   // per-tile arrival counters (zero between products)
   VUnit *vunits = nullptr;
   int32_t *warp_begin = nullptr;
   int32_t nwarps = 0;
@@ -23,8 +21,6 @@ struct DevPlan {
   int32_t *smap0 = nullptr;  // 0-based source map, length n
   int32_t *counter = nullptr;  // tile ticket of the near/U pass
   int32_t *status = nullptr;   // device error word (0 = ok), see hmgpu_hmatrix_status
-  int du_variant = 1;          // near/U pass: 0 per-thread 16-byte loads, 1 bulk-copy pipeline
-  int grid_tma = 0;
   int64_t m = 0, n = 0, x_len = 0, xt_len = 0;
 };
 
@@ -56,16 +52,12 @@ cudaError_t launch_pack_v(bool f64, const VPackJob *jobs, int64_t njobs, const d
 
 namespace hm {
 // Multi-right-hand-side plain product (hm_multi.cu): up to rhs_per_pass()
-// right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values
-// and part the split-tile partials (part_len rows of rhs_per_pass() values).
+// right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values.
 int rhs_per_pass();
-// Bulk-copy pipelined near/U pass (hm_du_tma.cu).
-int occupancy_du_tma(bool f64, bool comp);
-cudaError_t launch_du_tma(bool f64, bool comp, const DevPlan &p, const void *panels, void *xt,
-                          void *y, int grid, cudaStream_t s);
+
 int occupancy_du_multi(bool f64);
 cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,
-                                void *xt, void *part, const void *X, int64_t ldx, int nr, void *Y,
-                                int64_t ldy, int grid_v, int grid_du, cudaStream_t s,
-                                cudaEvent_t *ev, int *launches);
+                                void *xt, const void *X, int64_t ldx, int nr, void *Y, int64_t ldy,
+                                int grid_v, int grid_du, cudaStream_t s, cudaEvent_t *ev,
+                                int *launches);
 }  // namespace hm

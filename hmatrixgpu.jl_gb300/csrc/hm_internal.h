@@ -59,17 +59,19 @@ struct BlockSet {
 
 // ---- matvec layout ------------------------------------------------------------------
 // A row tile is a run of permuted rows that every block either covers or misses.
-// Its panel stores, column-major, all columns that touch those rows: the
-// columns of the covering dense blocks (vector entries from the permuted x)
-// and the rank columns of the covering low-rank blocks (entries from t = V x).
+// Its panel stores, row-major, every column that touches those rows: the
+// columns of the covering dense blocks (vector entries from the permuted x),
+// then the rank columns of the covering low-rank blocks (entries from t = V x).
+// Rows are padded with zeros to a 16-byte multiple, so each row is one aligned
+// stream of 16-byte vectors.
 struct TileDesc {
   int64_t data_off;  // element offset of the panel (multiple of the 16-byte vector)
   int32_t row0;      // first permuted row
   int32_t m;         // rows
   int32_t ncols;     // columns
+  int32_t ld;        // row stride in elements (ncols rounded up to 16 bytes)
   int32_t seg0;      // first segment
   int32_t nseg;      // segment count
-  int32_t pad;
 };
 static_assert(sizeof(TileDesc) == 32, "TileDesc layout");
 
@@ -78,18 +80,11 @@ struct Seg {
   int32_t col0, ncols, vec_off, pad;
 };
 
-// A unit of the near/U pass: columns [c0, c1) of one tile. A tile split into
-// several units sums their partial rows in slot order (fixed, deterministic).
-struct DuUnit {
-  int32_t tile;
-  int32_t c0, c1;
-  int32_t seg0, nseg;  // segments overlapping [c0, c1)
-  int32_t slot;        // index of this unit within its tile
-  int32_t nslots;      // units of the tile
-  int32_t pad;
-  int64_t part_off;    // offset of this tile's partial rows (nslots * m values)
+// A unit of the near/U pass: rows [i0, i1) of one tile, each row a complete
+// dot product, so units never share an output.
+struct RowUnit {
+  int32_t tile, i0, i1, pad;
 };
-static_assert(sizeof(DuUnit) == 40, "DuUnit layout");
 
 // A unit of the V pass: rows [0, nrows) of one low-rank block, each row a
 // phase-aligned run of `stride` elements dotted with XT[x_off : x_off+stride).
@@ -104,16 +99,18 @@ struct VUnit {
 };
 static_assert(sizeof(VUnit) == 32, "VUnit layout");
 
-// Copy job of the packing pass: a row-major source slice -> column-major panel.
+// Copy job of the packing pass: a row-major source slice -> rows of a tile panel.
 struct PackJob {
   int64_t src_off;   // element offset in the source array
-  int64_t dst_off;   // element offset in the panel array
+  int64_t dst_off;   // element offset of (first row, first column) in the panel array
   int32_t src_ld;    // source row stride
+  int32_t dst_ld;    // panel row stride
   int32_t ncols;
   int32_t m;         // rows
   int32_t kind;      // 0 dense source, 1 U source, 2 dense generated from the kernel
   int32_t row0;      // generated: first permuted row
   int32_t col0;      // generated: first permuted column
+  int32_t pad;
 };
 
 struct Plan {
@@ -122,11 +119,9 @@ struct Plan {
   int64_t R = 0;          // total rank
   int64_t xt_len = 0;     // x_len + R rounded up
   std::vector<TileDesc> tiles;
-  std::vector<int32_t> order;  // tiles by decreasing work
   std::vector<Seg> segs;
   int64_t panel_len = 0;
-  std::vector<DuUnit> units;   // near/U pass work, largest tiles first
-  int64_t part_len = 0;        // partial-row scratch (values) of split tiles
+  std::vector<RowUnit> units;  // near/U pass work, largest first
   std::vector<PackJob> pjobs;
   // V pass
   std::vector<int64_t> v_off, t_off;  // per low-rank block

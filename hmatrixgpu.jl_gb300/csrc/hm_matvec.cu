@@ -3,9 +3,11 @@
 // Replaces the reference's device product (src/mult.jl:41-189):
 //   V_mult_vec_kernel!  (:41-78)  -> v_pass_kernel: t = V x, one 16-byte-load
 //                                    stream per rank row, sub-warp shuffle sums.
-//   DU_mult_vec_kernel! (:80-146) -> du_pass_kernel: y = D x + U t over row
-//                                    tiles; each tile owns its rows of y, so the
-//                                    sums have a fixed order and need no atomics.
+//   DU_mult_vec_kernel! (:80-146) -> du_rows_kernel: y = D x + U t, one warp per
+//                                    row of a row tile; the row concatenates the
+//                                    row's dense and low-rank columns, so each
+//                                    output is one dot product with a fixed
+//                                    summation order and no atomics.
 // Both passes are bound by HBM bandwidth: every matrix byte is read once with
 // 16-byte non-allocating loads; the vectors (x permuted into XT, t) are small
 // and stay in L2.
@@ -61,9 +63,42 @@ __device__ __forceinline__ void dot2_step(T &s, T &c, T a, T b) {
   c += e + pe;
 }
 
+// Lane partials of a row: plain or compensated.
+template <typename T, bool COMP>
+struct RowAcc {
+  T s = T(0), c = T(0);
+  __device__ __forceinline__ void add(const typename Vec16<T>::type &a,
+                                      const typename Vec16<T>::type &b) {
+    const T *ea = reinterpret_cast<const T *>(&a), *eb = reinterpret_cast<const T *>(&b);
+#pragma unroll
+    for (int q = 0; q < Vec16<T>::N; q++) {
+      if (COMP)
+        dot2_step(s, c, ea[q], eb[q]);
+      else
+        s = fma_(ea[q], eb[q], s);
+    }
+  }
+  // Butterfly over the warp (fixed order); every lane ends with the total.
+  __device__ __forceinline__ T total() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T s2 = __shfl_xor_sync(0xffffffffu, s, o);
+      if (COMP) {
+        const T c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        const T t = s + s2, z = t - s;
+        c += c2 + ((s - (t - z)) + (s2 - z));
+        s = t;
+      } else {
+        s += s2;
+      }
+    }
+    return COMP ? s + c : s;
+  }
+};
+
 // ---------------------------------------------------------------------------
 // x permutation: XT[j] = x[smap[j]] for j < n, zero padding up to x_len.
-// Also re-arms the tile ticket of the near/U pass.
+// Also re-arms the unit ticket of the near/U pass.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void permute_x_kernel(const T *__restrict__ x, const int32_t *__restrict__ smap0,
@@ -102,19 +137,6 @@ __global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ 
       if (k < U.nrows) {
         const VT *row = reinterpret_cast<const VT *>(V + U.v_off + static_cast<int64_t>(k) * U.stride);
         int p = sub;
-        for (; p + 3 * g < nv; p += 4 * g) {  // four 16-byte loads in flight per lane
-          VT a[4], b[4];
-#pragma unroll
-          for (int s = 0; s < 4; s++) a[s] = ld_stream(row + p + s * g);
-#pragma unroll
-          for (int s = 0; s < 4; s++) b[s] = __ldg(X + p + s * g);
-#pragma unroll
-          for (int s = 0; s < 4; s++) {
-            const T *ea = reinterpret_cast<const T *>(&a[s]), *eb = reinterpret_cast<const T *>(&b[s]);
-#pragma unroll
-            for (int q = 0; q < VEC; q++) acc = fma_(ea[q], eb[q], acc);
-          }
-        }
         for (; p + g < nv; p += 2 * g) {
           VT a0 = ld_stream(row + p), a1 = ld_stream(row + p + g);
           VT b0 = __ldg(X + p), b1 = __ldg(X + p + g);
@@ -140,167 +162,112 @@ __global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// Near/U pass. CTAs take units (column slices of a row tile) from a ticket
-// counter, largest tiles first. A tile of m rows is a column-major panel; the
-// CTA's threads form G groups of m threads. Thread t of group g loads the
-// 16-byte vectors f = t + m*q, q = g (mod G). Because a vector holds VEC
-// elements and the group spans VEC*m elements per step, element u of every
-// vector the thread loads belongs to the same row (VEC*t + u) mod m: the
-// thread keeps VEC fixed-row accumulators, and the column of element u is
-// (VEC*t + u)/m + VEC*q. The vector entries of the unit's columns are
-// gathered into shared memory first. A tile cut into several units writes
-// one partial row-sum vector per unit; the unit that arrives last adds them
-// in slot order, so the result does not depend on the schedule.
+// Near/U pass. CTAs take row units (<= 16 rows of one tile) from a ticket
+// counter, tiles with the most columns first. The CTA gathers the tile's
+// vector entries (x for dense columns, t for rank columns) into shared memory
+// once per unit; then each warp streams one or two whole rows of the tile's
+// row-major panel with 16-byte loads against 16-byte shared-memory loads of
+// the entries, and reduces across lanes with a fixed butterfly.
 // ---------------------------------------------------------------------------
 template <typename T>
 struct DuArgs {
   const T *panels;
   const TileDesc *tiles;
-  const DuUnit *units;
+  const RowUnit *units;
   int32_t nunits;
   const Seg *segs;
   const T *xt;
   const int32_t *tmap0;
   T *y;
   int32_t *counter;
-  T *part;            // partial row sums of split tiles (x2 when compensated)
-  int32_t *tile_cnt;  // arrivals per tile, returned to zero by the last unit
 };
 
 template <typename T>
-struct DuChunk {
-  static constexpr int value = 16384 / sizeof(T);  // columns of vector entries per unit
+struct DuCols {
+  static constexpr int value = 16384 / sizeof(T);  // vector entries cached per column chunk
 };
 constexpr int kDuSegs = 512;
 
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(kThreads) du_pass_kernel(DuArgs<T> a) {
+__global__ void __launch_bounds__(kThreads) du_rows_kernel(DuArgs<T> a) {
   using VT = typename Vec16<T>::type;
   constexpr int VEC = Vec16<T>::N;
-  __shared__ T vals[DuChunk<T>::value];
+  constexpr int CH = DuCols<T>::value;
+  __shared__ __align__(16) T vals[CH];
   __shared__ Seg ssegs[kDuSegs];
-  __shared__ T part[kThreads * VEC];
-  __shared__ T partc[COMP ? kThreads * VEC : 1];
-  __shared__ int32_t s_ticket, s_last;
-  const int tid = threadIdx.x;
-  for (;;) {
-    if (tid == 0) s_ticket = atomicAdd(a.counter, 1);
+  __shared__ int32_t s_ticket[2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int it = 0;; it++) {
+    if (tid == 0) s_ticket[it & 1] = atomicAdd(a.counter, 1);
     __syncthreads();
-    const int32_t ticket = s_ticket;
-    if (ticket >= a.nunits) break;
-    const DuUnit U = a.units[ticket];
+    const int32_t u = s_ticket[it & 1];
+    if (u >= a.nunits) break;
+    const RowUnit U = a.units[u];
     const TileDesc d = a.tiles[U.tile];
-    const int m = d.m, c0 = U.c0, c1 = U.c1;
-    for (int s = tid; s < U.nseg; s += kThreads) ssegs[s] = a.segs[U.seg0 + s];
-    __syncthreads();
-    for (int c = c0 + tid; c < c1; c += kThreads) {
-      int lo = 0, hi = U.nseg - 1;  // last segment with col0 <= c
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (ssegs[mid].col0 <= c)
-          lo = mid;
-        else
-          hi = mid - 1;
-      }
-      vals[c - c0] = a.xt[ssegs[lo].vec_off + (c - ssegs[lo].col0)];
-    }
-    __syncthreads();
-    int G = kThreads / m;
-    if (G > 16) G = 16;
-    const int g = tid / m, t = tid - g * m;
-    const bool active = g < G;
-    T acc[VEC], cmp[VEC];
-#pragma unroll
-    for (int u = 0; u < VEC; u++) acc[u] = cmp[u] = T(0);
-    if (active) {
-      int base[VEC];
-#pragma unroll
-      for (int u = 0; u < VEC; u++) base[u] = (VEC * t + u) / m;
-      const VT *P = reinterpret_cast<const VT *>(a.panels + d.data_off);
-      const int64_t f_lo = (static_cast<int64_t>(c0) * m) / VEC;
-      const int64_t f_hi = (static_cast<int64_t>(c1) * m + VEC - 1) / VEC;
-      int64_t q = f_lo > t ? (f_lo - t + m - 1) / m : 0;
-      q += ((g - static_cast<int>(q % G)) % G + G) % G;
-      auto consume = [&](const VT &v, int64_t qq) {
-        const T *e = reinterpret_cast<const T *>(&v);
-#pragma unroll
-        for (int u = 0; u < VEC; u++) {
-          const int c = base[u] + static_cast<int>(VEC * qq);
-          if (c >= c0 && c < c1) {
-            if (COMP)
-              dot2_step(acc[u], cmp[u], e[u], vals[c - c0]);
+    const bool seg_smem = d.nseg <= kDuSegs;
+    if (seg_smem)
+      for (int s = tid; s < d.nseg; s += kThreads) ssegs[s] = a.segs[d.seg0 + s];
+    const Seg *S = seg_smem ? ssegs : a.segs + d.seg0;
+    const int ia = U.i0 + warp, ib = ia + kThreads / 32;
+    const bool ha = ia < U.i1, hb = ib < U.i1;
+    RowAcc<T, COMP> ra, rb;
+    for (int c0 = 0; c0 < d.ld; c0 += CH) {
+      const int cn = min(CH, d.ld - c0);
+      __syncthreads();  // segments loaded / previous chunk's entries no longer read
+      for (int j = tid; j < cn; j += kThreads) {
+        const int c = c0 + j;
+        T v = T(0);
+        if (c < d.ncols) {
+          int lo = 0, hi = d.nseg - 1;  // last segment with col0 <= c
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S[mid].col0 <= c)
+              lo = mid;
             else
-              acc[u] = fma_(e[u], vals[c - c0], acc[u]);
+              hi = mid - 1;
           }
+          v = a.xt[S[lo].vec_off + (c - S[lo].col0)];
         }
-      };
-      const int64_t step = static_cast<int64_t>(m) * G;
-      int64_t f = t + m * q;
-      for (; f + 3 * step < f_hi; f += 4 * step, q += 4 * G) {
-        VT v0 = ld_stream(P + f), v1 = ld_stream(P + f + step);
-        VT v2 = ld_stream(P + f + 2 * step), v3 = ld_stream(P + f + 3 * step);
-        consume(v0, q);
-        consume(v1, q + G);
-        consume(v2, q + 2 * G);
-        consume(v3, q + 3 * G);
+        vals[j] = v;
       }
-      for (; f < f_hi; f += step, q += G) consume(ld_stream(P + f), q);
-#pragma unroll
-      for (int u = 0; u < VEC; u++) {
-        part[g * VEC * m + VEC * t + u] = acc[u];
-        if (COMP) partc[g * VEC * m + VEC * t + u] = cmp[u];
-      }
-    }
-    __syncthreads();
-    T s = T(0), c = T(0);
-    if (tid < m) {
-      for (int gg = 0; gg < G; gg++)
-#pragma unroll
-        for (int k = 0; k < VEC; k++) {
-          const int idx = gg * VEC * m + tid + k * m;
-          if (COMP) {
-            const T p = part[idx], tt = s + p, z = tt - s;
-            c += ((s - (tt - z)) + (p - z)) + partc[idx];
-            s = tt;
-          } else {
-            s += part[idx];
-          }
+      __syncthreads();
+      const int nv = cn / VEC;
+      const VT *E = reinterpret_cast<const VT *>(vals);
+      const VT *RA = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ia) * d.ld + c0);
+      const VT *RB = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ib) * d.ld + c0);
+      if (ha && hb) {
+        int p = lane;
+        for (; p + 32 < nv; p += 64) {
+          const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
+          const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
+          const VT e0 = E[p], e1 = E[p + 32];
+          ra.add(x0, e0);
+          ra.add(x1, e1);
+          rb.add(z0, e0);
+          rb.add(z1, e1);
         }
-    }
-    if (U.nslots == 1) {
-      if (tid < m) a.y[a.tmap0[d.row0 + tid]] = COMP ? s + c : s;
-      continue;  // the ticket read at the top of the loop is behind a barrier
-    }
-    const int64_t pbase = U.part_off + static_cast<int64_t>(U.slot) * m + tid;
-    if (tid < m) {
-      if (COMP) {
-        a.part[2 * pbase] = s;
-        a.part[2 * pbase + 1] = c;
-      } else {
-        a.part[pbase] = s;
-      }
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&a.tile_cnt[U.tile], 1) == U.nslots - 1;
-    __syncthreads();
-    if (s_last) {
-      __threadfence();
-      if (tid < m) {
-        T ts = T(0), tc = T(0);
-        for (int sl = 0; sl < U.nslots; sl++) {
-          const int64_t idx = U.part_off + static_cast<int64_t>(sl) * m + tid;
-          if (COMP) {
-            const T p = __ldcg(a.part + 2 * idx), tt = ts + p, z = tt - ts;
-            tc += ((ts - (tt - z)) + (p - z)) + __ldcg(a.part + 2 * idx + 1);
-            ts = tt;
-          } else {
-            ts += __ldcg(a.part + idx);
-          }
+        if (p < nv) {
+          const VT e0 = E[p];
+          ra.add(ld_stream(RA + p), e0);
+          rb.add(ld_stream(RB + p), e0);
         }
-        a.y[a.tmap0[d.row0 + tid]] = COMP ? ts + tc : ts;
+      } else if (ha) {
+        int p = lane;
+        for (; p + 96 < nv; p += 128) {
+          const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
+          const VT x2 = ld_stream(RA + p + 64), x3 = ld_stream(RA + p + 96);
+          ra.add(x0, E[p]);
+          ra.add(x1, E[p + 32]);
+          ra.add(x2, E[p + 64]);
+          ra.add(x3, E[p + 96]);
+        }
+        for (; p < nv; p += 32) ra.add(ld_stream(RA + p), E[p]);
       }
-      if (tid == 0) a.tile_cnt[U.tile] = 0;
+    }
+    const T ya = ra.total(), yb = rb.total();
+    if (lane == 0) {
+      if (ha) a.y[a.tmap0[d.row0 + ia]] = ya;
+      if (hb) a.y[a.tmap0[d.row0 + ib]] = yb;
     }
   }
 }
@@ -317,11 +284,11 @@ int occupancy_v(bool f64) {
 int occupancy_du(bool f64, bool comp) {
   int n = 0;
   if (f64)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_pass_kernel<double, false>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_rows_kernel<double, false>, kThreads, 0);
   else if (comp)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_pass_kernel<float, true>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_rows_kernel<float, true>, kThreads, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_pass_kernel<float, false>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_rows_kernel<float, false>, kThreads, 0);
   return n > 0 ? n : 1;
 }
 
@@ -335,19 +302,13 @@ static cudaError_t run(const DevPlan &p, const T *panels, const T *vdata, T *xt,
   permute_x_kernel<T><<<gp, kThreads, 0, s>>>(x, p.smap0, p.n, p.x_len, xt, p.counter);
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
-  if (p.vunits && !p.warp_begin_empty) {
+  if (!p.warp_begin_empty) {
     v_pass_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.warp_begin, xt);
     nl++;
   }
   if (ev) cudaEventRecord(ev[2], s);
-  if (p.du_variant == 1) {
-    cudaError_t e = launch_du_tma(sizeof(T) == 8, COMP, p, panels, xt, y, p.grid_tma, s);
-    if (e != cudaSuccess) return e;
-  } else {
-    DuArgs<T> a{panels, p.tiles, p.units, p.nunits, p.segs, xt, p.tmap0, y, p.counter,
-                static_cast<T *>(p.part), p.tile_cnt};
-    du_pass_kernel<T, COMP><<<grid_du, kThreads, 0, s>>>(a);
-  }
+  DuArgs<T> a{panels, p.tiles, p.units, p.nunits, p.segs, xt, p.tmap0, y, p.counter};
+  du_rows_kernel<T, COMP><<<grid_du, kThreads, 0, s>>>(a);
   nl++;
   if (ev) cudaEventRecord(ev[3], s);
   if (launches) *launches = nl;
@@ -385,11 +346,10 @@ __global__ void pack_panels_kernel(const PackJob *__restrict__ jobs, int64_t njo
     const PackJob j = jobs[w];
     if (j.kind == 2) continue;
     const double *src = (j.kind == 0 ? dsrc : usrc) + j.src_off;
-    const int64_t total = static_cast<int64_t>(j.m) * j.ncols;
-    for (int64_t e = lane; e < total; e += 32) {
-      const int64_t c = e / j.m, i = e - c * j.m;
-      panels[j.dst_off + e] = static_cast<T>(src[i * j.src_ld + c]);
-    }
+    for (int i = 0; i < j.m; i++)
+      for (int c = lane; c < j.ncols; c += 32)
+        panels[j.dst_off + static_cast<int64_t>(i) * j.dst_ld + c] =
+            static_cast<T>(src[static_cast<int64_t>(i) * j.src_ld + c]);
   }
 }
 

@@ -1,9 +1,9 @@
 // Allocation-free single-right-hand-side product.
 //
-// hmgpu_matvec keeps its scratch (the permuted x and t = V x, the partial row
-// sums of split tiles and the ticket/arrival counters) in buffers the H-matrix
-// handle allocates. hmgpu_matvec_noalloc runs the same three kernels with that
-// scratch placed in the array below instead, for callers that must not
+// hmgpu_matvec keeps its scratch (the permuted x and t = V x, and the unit
+// ticket of the near/U pass) in buffers the H-matrix handle allocates.
+// hmgpu_matvec_noalloc runs the same three kernels with that scratch placed
+// in the array below instead, for callers that must not
 // allocate device memory while they run products: code being captured into a
 // CUDA graph with plain (non-async) allocation forbidden, real-time loops that
 // fix their memory footprint up front, and hosts whose allocator is owned by
@@ -55,11 +55,9 @@ extern "C" int hmgpu_matvec_noalloc(hmgpu_hmatrix *h, const void *x, void *y, vo
   const bool f64 = H.opt.precision == HMGPU_F64;
   const bool comp = !f64 && (H.opt.compensated || H.opt.precision == HMGPU_MIXED);
   const size_t es = f64 ? 8 : 4;
-  // scratch layout: ticket | tile arrival counters | XT | partial row sums
-  const size_t cnt_bytes = hm::up256(H.plan.tiles.size() * sizeof(int32_t));
+  // scratch layout: unit ticket (256 bytes) | XT (permuted x, then t)
   const size_t xt_bytes = hm::up256(static_cast<size_t>(H.plan.xt_len) * es);
-  const size_t part_bytes = hm::up256(static_cast<size_t>(H.plan.part_len) * es * (comp ? 2 : 1));
-  const size_t need = 256 + cnt_bytes + xt_bytes + part_bytes;
+  const size_t need = 256 + xt_bytes;
   if (need > hm::kNoAllocBytes)
     return hm::fail(HMGPU_ERR_INVALID,
                     "this H-matrix needs " + std::to_string(need) +
@@ -70,13 +68,12 @@ extern "C" int hmgpu_matvec_noalloc(hmgpu_hmatrix *h, const void *x, void *y, vo
   char *b = static_cast<char *>(base);
   hm::DevPlan dp = H.dp;
   dp.counter = reinterpret_cast<int32_t *>(b);
-  dp.tile_cnt = reinterpret_cast<int32_t *>(b + 256);
-  void *xt = b + 256 + cnt_bytes;
-  dp.part = b + 256 + cnt_bytes + xt_bytes;
+  void *xt = b + 256;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // The array keeps whatever the previous call left; the arrival counters must
-  // start at zero. (The ticket and the x padding are reset by the first kernel.)
-  e = cudaMemsetAsync(dp.tile_cnt, 0, H.plan.tiles.size() * sizeof(int32_t), s);
+  // The array keeps whatever the previous call left. The ticket must start at
+  // zero (the permutation kernel re-arms it too); the x padding is rewritten by
+  // the permutation and every t entry by the V pass before it is read.
+  e = cudaMemsetAsync(dp.counter, 0, 256, s);
   if (e != cudaSuccess) return hm::cuda_fail(e, "clearing the product scratch");
   int nl = 0;
   e = hm::launch_matvec(f64, comp, dp, H.panels, H.vdata, xt, x, y, H.grid_v, H.grid_du, s,

@@ -6,9 +6,11 @@
 //   * row tiles: maximal runs of permuted rows that every block either fully
 //     covers or misses (at most kMaxTileRows rows each).  Each tile owns its
 //     rows of y, which makes the product deterministic without atomics;
-//   * one column-major panel per tile holding every column that touches those
-//     rows (dense-block columns, then low-rank U columns), with a list of
-//     segments telling where each column's vector entry lives in XT = [x | t];
+//   * one row-major panel per tile holding every column that touches those
+//     rows (dense-block columns, then low-rank U columns), rows padded to 16
+//     bytes, with a list of segments telling where each column's vector entry
+//     lives in XT = [x | t];
+//   * row units: runs of at most kUnitRows rows of one tile, largest first;
 //   * the V factors row by row, each row phase-aligned with the permuted x so
 //     that a 16-byte load of V pairs with a 16-byte load of x;
 //   * a static, byte-balanced split of the V rows over the resident warps.
@@ -21,9 +23,10 @@ namespace hm {
 
 static constexpr int kMaxTileRows = 128;
 static constexpr int64_t kVUnitBytes = 64 * 1024;
-static constexpr int64_t kUnitBytes = 128 * 1024;
-static constexpr int32_t kUnitCols = 4096;  // == columns of the kernel's shared vector cache (FP32)
-static constexpr int32_t kUnitSegs = 512;   // == segment slots in shared memory
+static constexpr int32_t kUnitRows = 16;  // rows per near/U unit (2 per warp of 8)
+// Row strides are multiples of 4 elements (16 bytes in FP32, 32 in FP64): the
+// multi-RHS micro-kernel reads 4 columns per step.
+static constexpr int32_t kRowPad = 4;
 
 static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
@@ -107,13 +110,20 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     d.m = trows[t];
     d.data_off = off;
     d.seg0 = static_cast<int32_t>(p.segs.size());
+    int32_t ncols_total = 0;
+    for (int64_t q = cnt[t]; q < cnt[t + 1]; q++) {
+      int64_t b = contrib[q];
+      ncols_total += b < static_cast<int64_t>(nd) ? bs.d_ce[b] - bs.d_cs[b] : bs.a_r[b - nd];
+    }
+    d.ld = static_cast<int32_t>(round_up(ncols_total, kRowPad));
     int32_t col = 0;
     for (int64_t q = cnt[t]; q < cnt[t + 1]; q++) {
       int64_t b = contrib[q];
       int32_t ncols, vec_off;
       PackJob j{};
       j.m = d.m;
-      j.dst_off = off + static_cast<int64_t>(col) * d.m;
+      j.dst_off = off + col;
+      j.dst_ld = d.ld;
       if (b < static_cast<int64_t>(nd)) {
         ncols = bs.d_ce[b] - bs.d_cs[b];
         vec_off = bs.d_cs[b];
@@ -136,7 +146,7 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
       }
       j.ncols = ncols;
       p.pjobs.push_back(j);
-      if (!p.segs.empty() && static_cast<int32_t>(p.segs.size()) > d.seg0 &&
+      if (static_cast<int32_t>(p.segs.size()) > d.seg0 &&
           p.segs.back().vec_off + p.segs.back().ncols == vec_off) {
         p.segs.back().ncols += ncols;  // contiguous in XT: extend the segment
       } else {
@@ -146,54 +156,26 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     }
     d.ncols = col;
     d.nseg = static_cast<int32_t>(p.segs.size()) - d.seg0;
-    off += round_up(static_cast<int64_t>(d.m) * col, vec);
+    off += static_cast<int64_t>(d.m) * d.ld;
   }
-  p.panel_len = off;
-  p.order.resize(nt);
-  std::iota(p.order.begin(), p.order.end(), 0);
-  std::stable_sort(p.order.begin(), p.order.end(), [&](int32_t a, int32_t b) {
-    return static_cast<int64_t>(p.tiles[a].m) * p.tiles[a].ncols >
-           static_cast<int64_t>(p.tiles[b].m) * p.tiles[b].ncols;
-  });
+  p.panel_len = std::max<int64_t>(off, vec);
 
-  // ---- near/U units: column slices of at most kUnitBytes of panel, at most
-  // kUnitCols columns and kUnitSegs segments each ------------------------------
+  // ---- near/U units: row runs, tiles with more work first ---------------------------
+  std::vector<int32_t> order(nt);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+    return static_cast<int64_t>(p.tiles[a].ncols) > static_cast<int64_t>(p.tiles[b].ncols);
+  });
   p.units.clear();
-  p.part_len = 0;
-  for (int32_t ti : p.order) {
+  for (int32_t ti : order) {
     const TileDesc &d = p.tiles[ti];
-    const int64_t bytes = static_cast<int64_t>(d.m) * d.ncols * esize;
-    int32_t want = static_cast<int32_t>(std::max<int64_t>(1, (bytes + kUnitBytes - 1) / kUnitBytes));
-    int32_t cols_per = std::max(1, (d.ncols + want - 1) / std::max(1, want));
-    cols_per = std::min(cols_per, vec == 4 ? kUnitCols : kUnitCols / 2);
-    std::vector<DuUnit> tu;
-    int32_t c0 = 0, s = d.seg0;
-    do {
-      int32_t c1 = std::min(d.ncols, c0 + cols_per);
-      while (s < d.seg0 + d.nseg && p.segs[s].col0 + p.segs[s].ncols <= c0) s++;
-      int32_t e = s;
-      while (e < d.seg0 + d.nseg && p.segs[e].col0 < c1) e++;
-      if (e - s > kUnitSegs) {  // too many segments: end the unit at a segment end
-        e = s + kUnitSegs;
-        c1 = std::min(c1, p.segs[e - 1].col0 + p.segs[e - 1].ncols);
-      }
-      DuUnit u{};
-      u.tile = ti;
-      u.c0 = c0;
-      u.c1 = c1;
-      u.seg0 = s;
-      u.nseg = e - s;
-      tu.push_back(u);
-      c0 = c1;
-    } while (c0 < d.ncols);
-    const int32_t ns = static_cast<int32_t>(tu.size());
-    for (int32_t q = 0; q < ns; q++) {
-      tu[q].slot = q;
-      tu[q].nslots = ns;
-      tu[q].part_off = ns > 1 ? p.part_len : -1;
+    const int32_t parts = (d.m + kUnitRows - 1) / kUnitRows;
+    for (int32_t q = 0; q < parts; q++) {
+      // near-equal row runs
+      int32_t i0 = static_cast<int32_t>(static_cast<int64_t>(d.m) * q / parts);
+      int32_t i1 = static_cast<int32_t>(static_cast<int64_t>(d.m) * (q + 1) / parts);
+      p.units.push_back(RowUnit{ti, i0, i1, 0});
     }
-    if (ns > 1) p.part_len += static_cast<int64_t>(ns) * d.m;
-    p.units.insert(p.units.end(), tu.begin(), tu.end());
   }
 
   // ---- V pass -----------------------------------------------------------------------
@@ -205,7 +187,7 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   for (size_t a = 0; a < na; a++) {
     int32_t nb = bs.a_ce[a] - bs.a_cs[a], r = bs.a_r[a];
     int32_t ph = bs.a_cs[a] % vec;
-    int32_t stride = static_cast<int32_t>(round_up(ph + nb, vec));
+    int32_t stride = static_cast<int32_t>(round_up(ph + nb, kRowPad));
     p.v_off[a] = voff;
     p.v_stride[a] = stride;
     p.v_phase[a] = ph;

@@ -1,0 +1,62 @@
+"""Golden fixtures (tests/golden/, written by gen_golden.py from the oracle on the
+reference's RNG-free test inputs): the oracle and the library's host code must
+keep reproducing them; the GPU path is checked against them in -m gpu."""
+import os
+
+import numpy as np
+import pytest
+
+import hmgpu
+from oracle import oracle as O
+from tests import geometry
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name + ".npz"))
+
+
+def test_aca_golden():
+    g = load("aca_inv_sq")
+    U, V = O.aca_plus(O.Kernel("explicit", A=g["block"]), np.arange(1, 31), np.arange(1, 31), 1e-7)
+    np.testing.assert_array_equal(U, g["U"])
+    np.testing.assert_array_equal(V, g["V"])
+    assert U.shape[1] < 30 and np.linalg.norm(U @ V - g["block"], 2) < 1e-8  # test/test_aca.jl:39-40
+
+
+@pytest.mark.parametrize("name,kind,dims", [("circle_log2d", "log2d", 1), ("circle_vector_r", "vector_r", 3)])
+def test_circle_golden_oracle_and_host_tree(name, kind, dims):
+    g = load(name)
+    pts = geometry.circle(1000)
+    X = O.Tree(pts.T, 64)
+    Y = O.Tree(pts.T, 64, dims)
+    np.testing.assert_array_equal(X.index_map, g["target_index_map"])
+    np.testing.assert_array_equal(Y.index_map, g["source_index_map"])
+    H = O.HMatrix(O.Kernel(kind, pts.T, pts.T), X, Y, eta=1.5, eps=1e-6)
+    np.testing.assert_array_equal(H.dense_block_indices, g["dense_block_indices"])
+    np.testing.assert_array_equal(H.U_block_indices, g["U_block_indices"])
+    np.testing.assert_array_equal(H.aca_ranks, g["aca_ranks"])
+    np.testing.assert_allclose(H.mul(g["x"]), g["y"], rtol=0, atol=1e-13 * np.abs(g["y"]).max())
+    assert g["compression_ratio"] > 3 and np.max(np.abs(g["y"] - g["y_dense"])) < 1e-5
+    # the library's own host tree gives the same permutation
+    Th = hmgpu.ClusterTree(pts, max_points_per_leaf=64, dims=dims)
+    np.testing.assert_array_equal(Th.index_map, g["source_index_map"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,kind,dims", [("circle_log2d", "log2d", 1), ("circle_vector_r", "vector_r", 3)])
+def test_circle_golden_device(gpu, name, kind, dims):
+    import torch
+    g = load(name)
+    pts = geometry.circle(1000)
+    X = hmgpu.ClusterTree(pts, max_points_per_leaf=64)
+    Y = hmgpu.ClusterTree(pts, max_points_per_leaf=64, dims=dims)
+    H = hmgpu.HMatrix(hmgpu.Kernel(kind, pts), X, Y, eta=1.5, eps=1e-6, precision="f64")
+    d, a = H.blocks()
+    np.testing.assert_array_equal(d, g["dense_block_indices"][:, :4])
+    ranks = g["U_block_indices"][:, 3] - g["U_block_indices"][:, 2] + 1
+    assert np.mean(a[:, 4] == ranks) >= 0.99
+    y = (H * torch.tensor(g["x"], device=gpu)).cpu().numpy()
+    assert np.max(np.abs(y - g["y"])) < 1e-9             # test/test_hmatrix.jl:164 (GPU vs CPU)
+    assert np.max(np.abs(y - g["y_dense"])) < 1e-5       # test/test_hmatrix.jl:199

@@ -131,19 +131,15 @@ def test_many_rhs_two_passes(case, gpu, prec, tol):
     assert rel(Y[:, 0], y0) <= tol
 
 
-def test_near_pass_variants_agree_bitwise(case, gpu, monkeypatch):
-    """The bulk-copy pipeline and the per-thread-load near/U pass sum in the same
-    order, so their products are bitwise equal; no bounded wait may expire."""
+def test_device_status_clean(case, gpu):
+    """No bounded device wait expires in a product, plain or compensated."""
     import ctypes as C
     import torch
     _, _, Ho = case
-    ys = []
-    for variant in ("0", "1"):
-        monkeypatch.setenv("HMGPU_DU_VARIANT", variant)
-        for comp in (False, True):
-            H = hmgpu.HMatrix.from_flat(**_flat(Ho), precision="f32", compensated=comp)
-            x = torch.arange(Ho.n, device=gpu, dtype=torch.float32).sin()
-            ys.append(H * x)
-            st = C.c_int(-1)
-            assert hmgpu._lib.lib().hmgpu_hmatrix_status(H._h, C.byref(st)) == 0 and st.value == 0
-    assert torch.equal(ys[0], ys[2]) and torch.equal(ys[1], ys[3])
+    for comp in (False, True):
+        H = hmgpu.HMatrix.from_flat(**_flat(Ho), precision="f32", compensated=comp)
+        x = torch.arange(Ho.n, device=gpu, dtype=torch.float32).sin()
+        y = H * x
+        st = C.c_int(-1)
+        assert hmgpu._lib.lib().hmgpu_hmatrix_status(H._h, C.byref(st)) == 0 and st.value == 0
+        assert torch.isfinite(y).all()
