@@ -87,6 +87,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   cudaMemset(H.vdata, 0, p.v_len * es);
   if ((rc = upload(H, &H.dp.tiles, p.tiles))) return rc;
   if ((rc = upload(H, &H.dp.units, p.units))) return rc;
+  if ((rc = upload(H, &H.dp.tile_order, p.tile_order))) return rc;
   if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
   H.dp.nunits = static_cast<int32_t>(p.units.size());
   if ((rc = upload(H, &H.dp.vunits, p.vunits))) return rc;
@@ -435,6 +436,9 @@ extern "C" int hmgpu_hmatrix_info(const hmgpu_hmatrix *h, hmgpu_info *info) {
   info->n_tiles = static_cast<int64_t>(H.plan.tiles.size());
   info->precision = H.opt.precision;
   info->build_seconds = H.build_seconds;
+  info->aca_batches = H.aca_batches;
+  info->aca_reruns = H.aca_reruns;
+  info->aca_workspace_bytes = H.aca_ws_bytes;
   return HMGPU_OK;
 }
 

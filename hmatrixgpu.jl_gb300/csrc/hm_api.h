@@ -42,6 +42,7 @@ struct HMatrix {
   size_t prof_used = 0;
   int64_t prof_launches = 0;
   double build_seconds = 0.0;
+  int64_t aca_batches = 0, aca_reruns = 0, aca_ws_bytes = 0;
   int64_t device_bytes = 0;
   std::vector<void *> dev_allocs;
 
@@ -53,6 +54,8 @@ struct HMatrix {
 };
 
 int cuda_fail(cudaError_t e, const char *what);
+// The 8 rank-predictor features of admissible block (x, y) at tolerance eps.
+void block_features(const Node &x, const Node &y, double eps, float *f);
 int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
                     const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
                     const std::vector<int64_t> &v_src_off, DenseGenerator *gen);

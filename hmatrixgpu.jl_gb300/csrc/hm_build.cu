@@ -510,10 +510,10 @@ __global__ void gen_dense_kernel(KDev K, const int32_t *__restrict__ tmap0,
   for (int64_t wi = w0; wi < njobs; wi += nw) {
     const PackJob j = jobs[wi];
     if (j.kind != 2) continue;
-    const int64_t total = static_cast<int64_t>(j.m) * j.ncols;
-    for (int64_t e = lane; e < total; e += 32) {
-      const int64_t c = e / j.m, i = e - c * j.m;
-      panels[j.dst_off + e] = static_cast<T>(kentry(K, tmap0[j.row0 + i], smap0[j.col0 + c]));
+    for (int i = 0; i < j.m; i++) {  // rows of the row-major tile panel
+      const int64_t ti = tmap0[j.row0 + i];
+      T *dst = panels + j.dst_off + static_cast<int64_t>(i) * j.dst_ld;
+      for (int c = lane; c < j.ncols; c += 32) dst[c] = static_cast<T>(kentry(K, ti, smap0[j.col0 + c]));
     }
   }
 }
@@ -581,6 +581,7 @@ struct Compressor {
   int svd;
   int64_t budget;  // doubles of workspace per batch
   int grid;
+  int64_t batches = 0, ws_bytes = 0;  // statistics of all run() calls
 
   // Processes jobs[idx] for idx in `sel`, writing results into res (indexed like jobs).
   // keep(jj, k, r) -> bool decides whether low-rank factors are written; factors
@@ -606,6 +607,8 @@ struct Compressor {
         pos++;
       }
       const int nb = static_cast<int>(batch.size());
+      batches++;
+      ws_bytes += used * static_cast<int64_t>(sizeof(double));
       int rc;
       if ((rc = ws.alloc(used * sizeof(double))) || (rc = djobs.alloc(nb * sizeof(AcaJob))) ||
           (rc = dres.alloc(nb * sizeof(AcaRes))))
@@ -761,10 +764,31 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   }
   std::vector<int> order(na);
   for (size_t a = 0; a < na; a++) order[a] = static_cast<int>(a);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    return static_cast<int64_t>(jobs[a].m + jobs[a].n) * jobs[a].kcap >
-           static_cast<int64_t>(jobs[b].m + jobs[b].n) * jobs[b].kcap;
-  });
+  if (o.rank_model && na > 0) {
+    // learned bucketing: workspace for 1.25 x the predicted rank + 4 terms,
+    // blocks of equal predicted workspace batched together
+    std::vector<float> feats(na * HMGPU_RANK_FEATURES), pred(na);
+    for (size_t a = 0; a < na; a++)
+      block_features(X.nodes[blk.approx[2 * a]], Y.nodes[blk.approx[2 * a + 1]], eps,
+                     &feats[a * HMGPU_RANK_FEATURES]);
+    if ((rc = hmgpu_rank_model_predict(const_cast<hmgpu_rank_model *>(o.rank_model), feats.data(),
+                                       static_cast<int64_t>(na), pred.data())))
+      return rc;
+    for (size_t a = 0; a < na; a++) {
+      const float p = std::isfinite(pred[a]) ? std::max(pred[a], 0.0f) : 1e9f;
+      const int64_t cap = static_cast<int64_t>(std::ceil(1.25 * p)) + 4;
+      jobs[a].kcap = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(cap, jobs[a].max_iter)));
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      if (jobs[a].kcap != jobs[b].kcap) return jobs[a].kcap > jobs[b].kcap;
+      return jobs[a].m + jobs[a].n > jobs[b].m + jobs[b].n;
+    });
+  } else {
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return static_cast<int64_t>(jobs[a].m + jobs[a].n) * jobs[a].kcap >
+             static_cast<int64_t>(jobs[b].m + jobs[b].n) * jobs[b].kcap;
+    });
+  }
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   Compressor C;
@@ -815,6 +839,9 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
       again.push_back(a);
     }
   if (!again.empty() && (rc = C.run(jobs, res, again, keep, place))) return rc;
+  H.aca_batches = C.batches;
+  H.aca_reruns = static_cast<int64_t>(again.size());
+  H.aca_ws_bytes = C.ws_bytes;
 
   // block lists in the reference's order (src/hmatrix.jl:180-213)
   for (size_t d = 0; d < blk.dense.size() / 2; d++) {

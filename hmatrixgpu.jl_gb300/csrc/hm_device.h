@@ -13,6 +13,7 @@ struct DevPlan {
   int32_t ntiles = 0;
   RowUnit *units = nullptr;      // near/U pass work
   int32_t nunits = 0;
+  int32_t *tile_order = nullptr; // tiles by decreasing work (multi-RHS pass)
   VUnit *vunits = nullptr;
   int32_t *warp_begin = nullptr;
   int32_t nwarps = 0;

@@ -122,6 +122,7 @@ struct Plan {
   std::vector<Seg> segs;
   int64_t panel_len = 0;
   std::vector<RowUnit> units;  // near/U pass work, largest first
+  std::vector<int32_t> tile_order;  // tiles by decreasing columns
   std::vector<PackJob> pjobs;
   // V pass
   std::vector<int64_t> v_off, t_off;  // per low-rank block

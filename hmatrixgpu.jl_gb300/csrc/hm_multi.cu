@@ -6,21 +6,16 @@
 // is read once per pass and every element feeds kRhs FMAs, so this form is
 // bound by the CUDA cores' FMA rate, not by HBM.
 //
-// Both passes run the same register-tiled micro-kernel: a thread owns 4 matrix
-// rows x 8 right-hand sides (32 accumulators) over one of 16 column slices;
-// per step it loads 4 columns of its 4 rows (four 16-byte loads) and the 4
-// matching XT rows from shared memory (eight 16-byte loads) for 128 FMAs. The
-// 16 slices of an output sit in 16 lanes of one warp and meet in a fixed
-// shuffle butterfly, so results are deterministic.
+// Both passes run the same register-tiled micro-kernel over panels of at most
+// 128 rows (multi_panel below); partial sums of the column slices meet in
+// shared memory in a fixed order, so results are deterministic.
 #include <cuda_runtime.h>
 
 #include "hm_device.h"
 
 namespace hm {
 
-constexpr int kRhs = 32;   // right-hand sides per pass (row length of XT)
-constexpr int kSl = 16;    // column slices (lanes of a half-warp)
-constexpr int kRows = 16;  // matrix rows per step of the micro-kernel (4 quads)
+constexpr int kRhs = 32;  // right-hand sides per pass (row length of XT)
 
 template <typename T>
 struct Cols {
@@ -89,99 +84,107 @@ __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int n
   }
 }
 
-// The micro-kernel over columns [c0, c0 + cn) of `nrows` (<= 16) rows starting
-// at A (row stride lda, 16-byte aligned, columns padded with zeros to a
-// multiple of 4), against XT rows staged in xs (cn rows of kRhs values).
-template <typename T>
-struct Tile4x8 {
+// One panel of m <= 128 rows (row-major, stride lda, rows padded with zeros to
+// a multiple of 4 columns) times the kRhs-wide XT rows of its columns. Thread
+// layout: RQ = ceil(m / 4) row quads x 4 groups of 8 right-hand sides x S
+// column slices (S = 256 / (4 RQ)); a thread keeps 4 x 8 accumulators and
+// steps 4 columns at a time (four 16-byte loads of A, eight 16-byte shared
+// loads of XT rows, 128 FMAs). `stage(c0, cn, xs)` fills xs with the XT rows
+// of columns [c0, c0 + cn). The slices meet in shared memory in slice order.
+template <typename T, typename Stage, typename Emit>
+__device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int ncols_pad, T *xs,
+                                            T *red, Stage stage, Emit emit) {
+  constexpr int CC = Cols<T>::value;
+  const int tid = threadIdx.x;
+  const int RQ = (m + 3) / 4, per = RQ * 4;
+  int S = kThreads / per;
+  if (S < 1) S = 1;
+  const int ks = tid / per, r = tid - ks * per, rq = r % RQ, rg = r / RQ;
+  const bool active = ks < S;
   T acc[4][8];
-  __device__ __forceinline__ void zero() {
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 8; j++) acc[i][j] = T(0);
+  bool ok[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) ok[i] = rq * 4 + i < m;
+  for (int c0 = 0; c0 < ncols_pad; c0 += CC) {
+    const int cn = min(CC, ncols_pad - c0);
+    __syncthreads();  // xs free
+    stage(c0, cn, xs);
+    __syncthreads();
+    if (active)
+      for (int c = 4 * ks; c < cn; c += 4 * S) {
+        T a[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          if (ok[i])
+            ld4(A + static_cast<int64_t>(rq * 4 + i) * lda + c0 + c, a[i]);
+          else
+            a[i][0] = a[i][1] = a[i][2] = a[i][3] = T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          T b[8];
+          lds8(xs + (c + k) * kRhs + rg * 8, b);
+#pragma unroll
+          for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) acc[i][j] = fma(a[i][k], b[j], acc[i][j]);
+        }
+      }
+  }
+  __syncthreads();  // red aliases xs
+  if (active)
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
-      for (int j = 0; j < 8; j++) acc[i][j] = T(0);
+      for (int j = 0; j < 8; j++) red[((ks * RQ + rq) * 4 + i) * kRhs + rg * 8 + j] = acc[i][j];
+  __syncthreads();
+  for (int o = tid; o < m * kRhs; o += kThreads) {
+    const int row = o / kRhs, q = o % kRhs;
+    T s = T(0);
+    for (int sl = 0; sl < S; sl++) s += red[(sl * RQ * 4 + row) * kRhs + q];
+    emit(row, q, s);
   }
-  __device__ __forceinline__ void run(const T *A, int64_t lda, int nrows, int rq, int rg, int ks,
-                                      const T *xs, int cn) {
-    const bool ok[4] = {rq * 4 + 0 < nrows, rq * 4 + 1 < nrows, rq * 4 + 2 < nrows, rq * 4 + 3 < nrows};
-    for (int c = 4 * ks; c < cn; c += 4 * kSl) {
-      T a[4][4];
-#pragma unroll
-      for (int i = 0; i < 4; i++) {
-        if (ok[i])
-          ld4(A + static_cast<int64_t>(rq * 4 + i) * lda + c, a[i]);
-        else
-          a[i][0] = a[i][1] = a[i][2] = a[i][3] = T(0);
-      }
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        T b[8];
-        lds8(xs + (c + k) * kRhs + rg * 8, b);
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-          for (int j = 0; j < 8; j++) acc[i][j] = fma(a[i][k], b[j], acc[i][j]);
-      }
-    }
-  }
-  // Sums the 16 slices (lanes ks = 0..15 of a half-warp) in a fixed butterfly.
-  __device__ __forceinline__ void reduce() {
-#pragma unroll
-    for (int o = kSl / 2; o > 0; o >>= 1)
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 8; j++) acc[i][j] += __shfl_xor_sync(0xffffffffu, acc[i][j], o);
-  }
-};
+}
 
-// V pass: t[(t_off + k) * kRhs + r] = sum_j V[k, j] XT[(x_off + j) * kRhs + r].
-// CTA b works through units [warp_begin[8b], warp_begin[8b + 8]), the same
-// byte-balanced split as the single-right-hand-side pass.
+// V pass: t[(t_off + k) * kRhs + r] = sum_j V[k, j] XT[(x_off + j) * kRhs + r];
+// CTA b works through the V units of warps [8b, 8b + 8) of the single-RHS
+// pass's byte-balanced split, 128 rows of a unit at a time.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) v_multi_kernel(const T *__restrict__ V,
                                                            const VUnit *__restrict__ units,
                                                            const int32_t *__restrict__ warp_begin,
                                                            int nwarps, T *__restrict__ xt) {
-  constexpr int CC = Cols<T>::value;
-  __shared__ __align__(16) T xs[CC * kRhs];
-  const int tid = threadIdx.x, ks = tid % kSl, rg = (tid / kSl) % 4, rq = tid / (kSl * 4);
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  T *buf = reinterpret_cast<T *>(dyn_smem);  // XT rows while streaming, slice sums after
   const int w0 = blockIdx.x * (kThreads / 32);
   if (w0 >= nwarps) return;
   const int u0 = warp_begin[w0], u1 = warp_begin[min(w0 + kThreads / 32, nwarps)];
   for (int u = u0; u < u1; u++) {
     const VUnit U = units[u];
-    for (int k0 = 0; k0 < U.nrows; k0 += kRows) {
-      const int rows = min(kRows, U.nrows - k0);
-      Tile4x8<T> t;
-      t.zero();
-      for (int c0 = 0; c0 < U.stride; c0 += CC) {
-        const int cn = min(CC, U.stride - c0);
-        __syncthreads();
-        const T *src = xt + static_cast<int64_t>(U.x_off + c0) * kRhs;
-        for (int e = tid; e < cn * kRhs; e += kThreads) xs[e] = src[e];
-        __syncthreads();
-        t.run(V + U.v_off + static_cast<int64_t>(k0) * U.stride + c0, U.stride, rows, rq, rg, ks, xs, cn);
-      }
-      t.reduce();
-      if (ks == 0)
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-          if (rq * 4 + i < rows)
-#pragma unroll
-            for (int j = 0; j < 8; j++)
-              xt[static_cast<int64_t>(U.t_off + k0 + rq * 4 + i) * kRhs + rg * 8 + j] = t.acc[i][j];
+    for (int k0 = 0; k0 < U.nrows; k0 += 128) {
+      const int rows = min(128, U.nrows - k0);
+      const T *src = xt + static_cast<int64_t>(U.x_off) * kRhs;
+      multi_panel<T>(
+          V + U.v_off + static_cast<int64_t>(k0) * U.stride, U.stride, rows, U.stride, buf, buf,
+          [&](int c0, int cn, T *xs) {
+            for (int e = threadIdx.x; e < cn * kRhs; e += kThreads) xs[e] = src[static_cast<int64_t>(c0) * kRhs + e];
+          },
+          [&](int row, int q, T s) { xt[static_cast<int64_t>(U.t_off + k0 + row) * kRhs + q] = s; });
     }
   }
 }
 
-// Near/U pass over the row units of the single-RHS pass.
+// Near/U pass: one whole row tile per CTA (tiles from a ticket counter).
 template <typename T>
 struct DuMultiArgs {
   const T *panels;
   const TileDesc *tiles;
-  const RowUnit *units;
-  int32_t nunits;
+  const int32_t *order;  // tiles by decreasing work
+  int32_t ntiles;
   const Seg *segs;
   const T *xt;
   const int32_t *tmap0;
@@ -194,60 +197,75 @@ struct DuMultiArgs {
 template <typename T>
 __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
   constexpr int CC = Cols<T>::value;
-  __shared__ __align__(16) T xs[CC * kRhs];
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  T *buf = reinterpret_cast<T *>(dyn_smem);  // kThreads * 32 values
+  __shared__ int32_t cmap[CC];
   __shared__ int32_t s_ticket[2];
-  const int tid = threadIdx.x, ks = tid % kSl, rg = (tid / kSl) % 4, rq = tid / (kSl * 4);
+  const int tid = threadIdx.x;
   for (int it = 0;; it++) {
     if (tid == 0) s_ticket[it & 1] = atomicAdd(a.counter, 1);
     __syncthreads();
     const int32_t u = s_ticket[it & 1];
-    if (u >= a.nunits) break;
-    const RowUnit U = a.units[u];
-    const TileDesc d = a.tiles[U.tile];
-    const int rows = U.i1 - U.i0;
-    Tile4x8<T> t;
-    t.zero();
-    for (int c0 = 0; c0 < d.ld; c0 += CC) {
-      const int cn = min(CC, d.ld - c0);
-      __syncthreads();
-      for (int e = tid; e < cn * kRhs; e += kThreads) {
-        const int c = c0 + e / kRhs;
-        T v = T(0);
-        if (c < d.ncols) {
-          int lo = 0, hi = d.nseg - 1;
-          const Seg *S = a.segs + d.seg0;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (S[mid].col0 <= c)
-              lo = mid;
-            else
-              hi = mid - 1;
+    if (u >= a.ntiles) break;
+    const TileDesc d = a.tiles[a.order[u]];
+    const Seg *S = a.segs + d.seg0;
+    multi_panel<T>(
+        a.panels + d.data_off, d.ld, d.m, d.ld, buf, buf,
+        [&](int c0, int cn, T *xs) {
+          for (int j = threadIdx.x; j < cn; j += kThreads) {  // column -> XT row
+            const int c = c0 + j;
+            int v = -1;
+            if (c < d.ncols) {
+              int lo = 0, hi = d.nseg - 1;
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (S[mid].col0 <= c)
+                  lo = mid;
+                else
+                  hi = mid - 1;
+              }
+              v = S[lo].vec_off + (c - S[lo].col0);
+            }
+            cmap[j] = v;
           }
-          v = a.xt[static_cast<int64_t>(S[lo].vec_off + (c - S[lo].col0)) * kRhs + (e % kRhs)];
-        }
-        xs[e] = v;
-      }
-      __syncthreads();
-      t.run(a.panels + d.data_off + static_cast<int64_t>(U.i0) * d.ld + c0, d.ld, rows, rq, rg, ks,
-            xs, cn);
-    }
-    t.reduce();
-    if (ks == 0)
+          __syncthreads();
+          for (int e = threadIdx.x; e < cn * (kRhs / 4); e += kThreads) {  // 16-byte copies
+            const int j = e / (kRhs / 4), q = (e % (kRhs / 4)) * 4;
+            const int v = cmap[j];
 #pragma unroll
-      for (int i = 0; i < 4; i++)
-        if (rq * 4 + i < rows) {
-          const int64_t yrow = a.tmap0[d.row0 + U.i0 + rq * 4 + i];
-#pragma unroll
-          for (int j = 0; j < 8; j++)
-            if (rg * 8 + j < a.nr) a.y[yrow + (rg * 8 + j) * a.ldy] = t.acc[i][j];
-        }
+            for (int w = 0; w < 4; w++)
+              xs[j * kRhs + q + w] = v >= 0 ? a.xt[static_cast<int64_t>(v) * kRhs + q + w] : T(0);
+          }
+        },
+        [&](int row, int q, T s) {
+          if (q < a.nr) a.y[a.tmap0[d.row0 + row] + q * a.ldy] = s;
+        });
   }
+}
+
+// Dynamic shared memory of the multi-RHS kernels: 32 accumulators per thread
+// for the slice reduction (also holds the staged XT rows).
+template <typename T>
+constexpr size_t multi_smem() {
+  return static_cast<size_t>(kThreads) * 32 * sizeof(T);
+}
+
+template <typename T>
+static void multi_attrs() {
+  static bool done = false;  // once per process (the attribute is per function)
+  if (done) return;
+  cudaFuncSetAttribute(v_multi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(multi_smem<T>()));
+  cudaFuncSetAttribute(du_multi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(multi_smem<T>()));
+  done = true;
 }
 
 template <typename T>
 static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, T *xt, const T *X,
                              int64_t ldx, int nr, T *Y, int64_t ldy, int grid_v, int grid_du,
                              cudaStream_t s, cudaEvent_t *ev, int *launches) {
+  multi_attrs<T>();
   int gp = static_cast<int>((p.x_len + 63) / 64);
   if (gp > 2048) gp = 2048;
   int nl = 0;
@@ -256,12 +274,12 @@ static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, 
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
   if (!p.warp_begin_empty) {
-    v_multi_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.warp_begin, p.nwarps, xt);
+    v_multi_kernel<T><<<grid_v, kThreads, multi_smem<T>(), s>>>(vdata, p.vunits, p.warp_begin, p.nwarps, xt);
     nl++;
   }
   if (ev) cudaEventRecord(ev[2], s);
-  DuMultiArgs<T> a{panels, p.tiles, p.units, p.nunits, p.segs, xt, p.tmap0, Y, ldy, nr, p.counter};
-  du_multi_kernel<T><<<grid_du, kThreads, 0, s>>>(a);
+  DuMultiArgs<T> a{panels, p.tiles, p.tile_order, p.ntiles, p.segs, xt, p.tmap0, Y, ldy, nr, p.counter};
+  du_multi_kernel<T><<<grid_du, kThreads, multi_smem<T>(), s>>>(a);
   nl++;
   if (ev) cudaEventRecord(ev[3], s);
   if (launches) *launches = nl;
@@ -272,10 +290,13 @@ int rhs_per_pass() { return kRhs; }
 
 int occupancy_du_multi(bool f64) {
   int n = 0;
-  if (f64)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<double>, kThreads, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<float>, kThreads, 0);
+  if (f64) {
+    multi_attrs<double>();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<double>, kThreads, multi_smem<double>());
+  } else {
+    multi_attrs<float>();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<float>, kThreads, multi_smem<float>());
+  }
   return n > 0 ? n : 1;
 }
 

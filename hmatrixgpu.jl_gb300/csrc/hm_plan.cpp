@@ -39,10 +39,38 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   const size_t nd = bs.d_rs.size(), na = bs.a_rs.size();
   p.x_len = round_up(n + 4, vec);
 
-  // ---- t offsets (ranks, reference order) -----------------------------------
+  // ---- source groups: low-rank blocks sharing a source cluster multiply the
+  // same x segment, so their V rows are stored (and their t entries numbered)
+  // one after another, group by group in order of first appearance ----------
+  std::vector<int32_t> gorder;  // low-rank blocks, grouped
+  std::vector<int32_t> gstart;  // group boundaries in gorder
+  {
+    std::vector<int32_t> idx(na);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::vector<int32_t> first(na);
+    {
+      std::vector<std::pair<int64_t, int32_t>> key(na);
+      for (size_t b = 0; b < na; b++)
+        key[b] = {(static_cast<int64_t>(bs.a_cs[b]) << 32) | static_cast<uint32_t>(bs.a_ce[b]),
+                  static_cast<int32_t>(b)};
+      std::vector<std::pair<int64_t, int32_t>> sorted = key;
+      std::sort(sorted.begin(), sorted.end());
+      for (size_t i = 0; i < na;) {  // first appearance of each key
+        size_t j = i;
+        while (j < na && sorted[j].first == sorted[i].first) j++;
+        for (size_t q = i; q < j; q++) first[sorted[q].second] = sorted[i].second;
+        i = j;
+      }
+    }
+    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return first[a] < first[b]; });
+    gorder = idx;
+    for (size_t i = 0; i < na; i++)
+      if (i == 0 || first[gorder[i]] != first[gorder[i - 1]]) gstart.push_back(static_cast<int32_t>(i));
+    gstart.push_back(static_cast<int32_t>(na));
+  }
   p.t_off.assign(na, 0);
   int64_t R = 0;
-  for (size_t b = 0; b < na; b++) {
+  for (int32_t b : gorder) {
     p.t_off[b] = p.x_len + R;
     R += bs.a_r[b];
   }
@@ -166,6 +194,7 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
     return static_cast<int64_t>(p.tiles[a].ncols) > static_cast<int64_t>(p.tiles[b].ncols);
   });
+  p.tile_order = order;
   p.units.clear();
   for (int32_t ti : order) {
     const TileDesc &d = p.tiles[ti];
@@ -184,30 +213,38 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   p.v_phase.assign(na, 0);
   int64_t voff = 0;
   std::vector<int64_t> uweight;
-  for (size_t a = 0; a < na; a++) {
-    int32_t nb = bs.a_ce[a] - bs.a_cs[a], r = bs.a_r[a];
-    int32_t ph = bs.a_cs[a] % vec;
-    int32_t stride = static_cast<int32_t>(round_up(ph + nb, kRowPad));
-    p.v_off[a] = voff;
-    p.v_stride[a] = stride;
-    p.v_phase[a] = ph;
-    if (r == 0) continue;
+  for (size_t gi = 0; gi + 1 < gstart.size(); gi++) {
+    const int32_t a0 = gorder[gstart[gi]];
+    const int32_t nb = bs.a_ce[a0] - bs.a_cs[a0];
+    const int32_t ph = bs.a_cs[a0] % vec;
+    const int32_t stride = static_cast<int32_t>(round_up(ph + nb, kRowPad));
+    const int64_t gbase = voff;
+    int32_t rows = 0;
+    for (int32_t q = gstart[gi]; q < gstart[gi + 1]; q++) {  // rows of the group, block by block
+      const int32_t a = gorder[q];
+      p.v_off[a] = voff;
+      p.v_stride[a] = stride;
+      p.v_phase[a] = ph;
+      voff += static_cast<int64_t>(stride) * bs.a_r[a];
+      rows += bs.a_r[a];
+    }
+    if (rows == 0) continue;
     int32_t nv = stride / vec, lanes = 1;
     while (lanes < nv && lanes < 32) lanes *= 2;
-    int64_t row_bytes = static_cast<int64_t>(stride) * esize;
-    int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, kVUnitBytes / row_bytes));
-    for (int32_t k0 = 0; k0 < r; k0 += rows_per) {
+    const int64_t row_bytes = static_cast<int64_t>(stride) * esize;
+    const int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, kVUnitBytes / row_bytes));
+    const int64_t t0 = p.t_off[a0];  // the group's t entries are contiguous
+    for (int32_t k0 = 0; k0 < rows; k0 += rows_per) {
       VUnit u{};
-      u.v_off = voff + static_cast<int64_t>(k0) * stride;
+      u.v_off = gbase + static_cast<int64_t>(k0) * stride;
       u.stride = stride;
-      u.nrows = std::min(rows_per, r - k0);
-      u.x_off = bs.a_cs[a] - ph;
-      u.t_off = static_cast<int32_t>(p.t_off[a] + k0);
+      u.nrows = std::min(rows_per, rows - k0);
+      u.x_off = bs.a_cs[a0] - ph;
+      u.t_off = static_cast<int32_t>(t0 + k0);
       u.lanes = lanes;
       p.vunits.push_back(u);
       uweight.push_back(row_bytes * u.nrows + 256);
     }
-    voff += static_cast<int64_t>(stride) * r;
   }
   p.v_len = round_up(std::max<int64_t>(voff, vec), vec);
   p.nwarps = std::max(1, nwarps);

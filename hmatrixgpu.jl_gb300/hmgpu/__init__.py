@@ -21,11 +21,11 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (F64, F32, MIXED, PRECISIONS, KERNEL_IDS, HMGPUError, Info, KernelDesc,
-                   Options, I64P, I8P, F64P, check, lib, ptr)
+                   Options, I64P, I8P, F32P, F64P, check, lib, ptr)
 from . import _build
 
 __all__ = ["ClusterTree", "BlockTree", "ACA_plus", "SVD_recompress", "HMatrix", "Kernel", "info",
-           "traverse", "mul_", "HMGPUError", "build"]
+           "traverse", "mul_", "HMGPUError", "build", "RankModel", "block_features"]
 
 
 def build(verbose=False):
@@ -237,12 +237,74 @@ class Kernel:
         return self.shape
 
 
-def _opts(precision, compensated, keep_factors):
+def _opts(precision, compensated, keep_factors, rank_model=None):
     o = Options()
     o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.compensated = int(bool(compensated))
     o.keep_factors = int(bool(keep_factors))
+    o.rank_model = rank_model._h if rank_model is not None else None
     return o
+
+
+def block_features(X, Y, eta, eps):
+    """Rank-predictor features (n, 8) of the admissible leaves of BlockTree(X, Y; eta)
+    in traversal order (the order of HMatrix.aca_ranks())."""
+    n = C.c_int64()
+    check(lib().hmgpu_block_features(X._h, Y._h, float(eta), float(eps), None, C.byref(n)))
+    out = np.zeros((n.value, 8), np.float32)
+    check(lib().hmgpu_block_features(X._h, Y._h, float(eta), float(eps), ptr(out, F32P), C.byref(n)))
+    return out
+
+
+class RankModel:
+    """The learned ACA-rank predictor (8 -> 64 -> 64 -> 1 ReLU MLP, FP32), trained
+    and evaluated by libhmgpu's kernels; passed to HMatrix(..., rank_model=M) it
+    sizes and batches the ACA work (results never depend on it)."""
+
+    NPARAMS = 4801
+
+    def __init__(self, seed=0):
+        h = C.c_void_p()
+        check(lib().hmgpu_rank_model_create(int(seed), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().hmgpu_rank_model_free(h)
+            self._h = None
+
+    def train(self, X, y, epochs=50, batch=1024, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        loss = C.c_float()
+        check(lib().hmgpu_rank_model_train(self._h, ptr(X, F32P), ptr(y, F32P), len(y), int(epochs),
+                                           int(batch), float(lr), int(seed), C.byref(loss)))
+        return loss.value
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        out = np.zeros(len(X), np.float32)
+        check(lib().hmgpu_rank_model_predict(self._h, ptr(X, F32P), len(X), ptr(out, F32P)))
+        return out
+
+    def gradients(self, X, y):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        g = np.zeros(self.NPARAMS, np.float32)
+        loss = C.c_float()
+        check(lib().hmgpu_rank_model_gradients(self._h, ptr(X, F32P), ptr(y, F32P), len(y), ptr(g, F32P),
+                                               C.byref(loss)))
+        return g, loss.value
+
+    def params(self, set_params=None, set_norm=None):
+        p = np.zeros(self.NPARAMS, np.float32)
+        nm = np.zeros(16, np.float32)
+        sp = np.ascontiguousarray(set_params, np.float32) if set_params is not None else None
+        sn = np.ascontiguousarray(set_norm, np.float32) if set_norm is not None else None
+        check(lib().hmgpu_rank_model_params(self._h, ptr(p, F32P), ptr(sp, F32P) if sp is not None else None,
+                                            ptr(nm, F32P), ptr(sn, F32P) if sn is not None else None))
+        return p, nm
 
 
 class HMatrix:
@@ -250,7 +312,7 @@ class HMatrix:
     assembled on the device, stored in `precision` ('f64', 'f32' or 'mixed')."""
 
     def __init__(self, K, X, Y, eta=1.5, eps=1e-5, svd_recompress=True, precision="f64",
-                 compensated=False, keep_factors=False, _handle=None):
+                 compensated=False, keep_factors=False, rank_model=None, _handle=None):
         self._h = None
         if _handle is not None:
             self._h = _handle
@@ -258,7 +320,7 @@ class HMatrix:
             if not isinstance(K, Kernel):
                 K = Kernel("explicit", A=K)
             self.K = K
-            o = _opts(precision, compensated, keep_factors)
+            o = _opts(precision, compensated, keep_factors, rank_model)
             h = C.c_void_p()
             d = K.desc()
             check(lib().hmgpu_hmatrix_build(C.byref(o), C.byref(d), X._h, Y._h, float(eta),
@@ -311,7 +373,8 @@ class HMatrix:
                 "dense_entries": i.dense_entries, "far_entries": i.far_entries,
                 "matrix_bytes": i.matrix_bytes, "device_bytes": i.device_bytes,
                 "n_tiles": i.n_tiles, "hi_only_blocks": i.hi_only_blocks,
-                "build_seconds": i.build_seconds}
+                "build_seconds": i.build_seconds, "aca_batches": i.aca_batches,
+                "aca_reruns": i.aca_reruns, "aca_workspace_bytes": i.aca_workspace_bytes}
 
     def blocks(self):
         """(dense (nD, 4), approx (nA, 5)) block tables: 1-based inclusive ranges, rank last."""
@@ -336,9 +399,13 @@ class HMatrix:
         check(lib().hmgpu_hmatrix_block_factors(self._h, int(b), ptr(U), ptr(V)))
         return U, V
 
-    def aca_ranks(self):
-        n = getattr(self, "_ncand", None)
-        raise NotImplementedError if n is None else None
+    def aca_ranks(self, count):
+        """(ACA rank, final rank or -1 if stored dense) per admissible leaf of the
+        block tree in traversal order (device builds; `count` = number of leaves)."""
+        a = np.full(count, -1, np.int64)
+        f = np.full(count, -1, np.int64)
+        check(lib().hmgpu_hmatrix_aca_ranks(self._h, ptr(a, I64P), ptr(f, I64P)))
+        return a, f
 
     # ---- products ------------------------------------------------------------------
     def mul(self, y, x, stream=None):

@@ -7,6 +7,7 @@ from . import _build
 
 I64P = C.POINTER(C.c_int64)
 F64P = C.POINTER(C.c_double)
+F32P = C.POINTER(C.c_float)
 I8P = C.POINTER(C.c_int8)
 VP = C.c_void_p
 
@@ -29,7 +30,7 @@ class HMGPUError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("compensated", C.c_int32),
-                ("keep_factors", C.c_int32), ("reserved", C.c_int32)]
+                ("keep_factors", C.c_int32), ("reserved", C.c_int32), ("rank_model", C.c_void_p)]
 
 
 class KernelDesc(C.Structure):
@@ -45,7 +46,8 @@ class Info(C.Structure):
                 ("far_entries", C.c_int64), ("compression_ratio", C.c_double),
                 ("matrix_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("n_tiles", C.c_int64), ("precision", C.c_int32), ("hi_only_blocks", C.c_int32),
-                ("build_seconds", C.c_double)]
+                ("build_seconds", C.c_double), ("aca_batches", C.c_int64),
+                ("aca_reruns", C.c_int64), ("aca_workspace_bytes", C.c_int64)]
 
 
 # name -> (restype, argtypes); every entry point returns an int status unless noted
@@ -83,6 +85,14 @@ SIGNATURES = {
                                  C.c_int64, F64P, F64P, I64P]),
     "hmgpu_svd_recompress": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, F64P, F64P, C.c_double,
                                        F64P, F64P, I64P]),
+    "hmgpu_rank_model_create": (C.c_int, [C.c_uint64, C.POINTER(VP)]),
+    "hmgpu_rank_model_train": (C.c_int, [VP, F32P, F32P, C.c_int64, C.c_int64, C.c_int64, C.c_float,
+                                         C.c_uint64, F32P]),
+    "hmgpu_rank_model_predict": (C.c_int, [VP, F32P, C.c_int64, F32P]),
+    "hmgpu_rank_model_gradients": (C.c_int, [VP, F32P, F32P, C.c_int64, F32P, F32P]),
+    "hmgpu_rank_model_params": (C.c_int, [VP, F32P, F32P, F32P, F32P]),
+    "hmgpu_rank_model_free": (C.c_int, [VP]),
+    "hmgpu_block_features": (C.c_int, [VP, VP, C.c_double, C.c_double, F32P, I64P]),
 }
 
 

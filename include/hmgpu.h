@@ -105,11 +105,18 @@ int hmgpu_blocks_free(hmgpu_blocks *b);
 /* ---------------------------------------------------------------------- */
 typedef struct hmgpu_hmatrix hmgpu_hmatrix;
 
+typedef struct hmgpu_rank_model hmgpu_rank_model;
+
 typedef struct {
   int32_t precision;   /* HMGPU_F64, HMGPU_F32 or HMGPU_MIXED                     */
   int32_t compensated; /* FP32 modes: 1 = compensated (Dot2) accumulation        */
   int32_t keep_factors;/* 1 = keep the FP64 block factors for export             */
   int32_t reserved;
+  /* Optional learned rank predictor (see below): when set, hmgpu_hmatrix_build
+   * sizes each admissible block's ACA workspace from the predicted rank and
+   * batches blocks of similar predicted rank together; blocks that need more
+   * terms are rerun with room for min(m, n). NULL = fixed workspace. */
+  const hmgpu_rank_model *rank_model;
 } hmgpu_options;
 
 typedef struct {
@@ -190,6 +197,9 @@ typedef struct {
   int32_t precision;
   int32_t hi_only_blocks;        /* HMGPU_MIXED: blocks stored hi-only BF16         */
   double build_seconds;          /* wall time of the last import/build              */
+  int64_t aca_batches;           /* device ACA batches of the build                 */
+  int64_t aca_reruns;            /* blocks rerun after outgrowing their workspace   */
+  int64_t aca_workspace_bytes;   /* workspace bytes summed over the batches         */
 } hmgpu_info;
 /* info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures. */
 int hmgpu_hmatrix_info(const hmgpu_hmatrix *H, hmgpu_info *info);
@@ -237,6 +247,37 @@ int hmgpu_aca_plus(const double *A, int64_t lda, int64_t m, int64_t n, double ep
  * r x n (ld r) host arrays out (room for k columns/rows). */
 int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const double *V,
                          double eps, double *U_out, double *V_out, int64_t *r);
+
+/* ---------------------------------------------------------------------- */
+/* Learned ACA-rank predictor (no counterpart in the reference): an          */
+/* 8 -> 64 -> 64 -> 1 ReLU MLP in FP32 mapping block features to the rank    */
+/* plain ACA+ reaches, trained and evaluated by the library's own kernels.   */
+/* Used only to size and batch ACA work; results never depend on it.         */
+/* ---------------------------------------------------------------------- */
+#define HMGPU_RANK_MODEL_PARAMS 4801
+#define HMGPU_RANK_FEATURES 8
+int hmgpu_rank_model_create(uint64_t seed, hmgpu_rank_model **out);
+/* Adam on the mean squared error over n samples (X: n x 8 row-major, Y: ACA
+ * ranks), mini-batches of `batch`; features are standardised with the
+ * training set's mean and deviation. final_loss: 0.5 * mean squared error. */
+int hmgpu_rank_model_train(hmgpu_rank_model *M, const float *X, const float *Y, int64_t n,
+                           int64_t epochs, int64_t batch, float lr, uint64_t seed,
+                           float *final_loss);
+int hmgpu_rank_model_predict(hmgpu_rank_model *M, const float *X, int64_t n, float *out);
+/* Gradient of 0.5 * mean((f(x) - y)^2) with respect to the parameters. */
+int hmgpu_rank_model_gradients(hmgpu_rank_model *M, const float *X, const float *Y, int64_t n,
+                               float *grad, float *loss);
+/* Read and/or write the parameters (W1 64x8, b1, W2 64x64, b2, W3 1x64, b3,
+ * row-major, concatenated) and the feature scaling (8 means, 8 deviations). */
+int hmgpu_rank_model_params(hmgpu_rank_model *M, float *get, const float *set, float *norm_get,
+                            const float *norm_set);
+int hmgpu_rank_model_free(hmgpu_rank_model *M);
+/* Features of the admissible leaves of BlockTree(X, Y; eta) in traversal order
+ * (the order of hmgpu_hmatrix_aca_ranks): log m, log n, log diameters of the
+ * target and source clusters, log centre distance, distance / (rX + rY),
+ * log10 eps, log min(m, n). out: count x 8 (may be NULL to count). */
+int hmgpu_block_features(const hmgpu_tree *X, const hmgpu_tree *Y, double eta, double eps,
+                         float *out, int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,74 @@
+"""The learned ACA-rank predictor: its forward and backward kernels against an
+FP64 NumPy restatement (oracle/mlp.py), training on ranks the device ACA
+produced, and what it buys the assembly while leaving the H-matrix unchanged."""
+import numpy as np
+import pytest
+
+import hmgpu
+from oracle import mlp as M
+from tests import geometry
+
+pytestmark = pytest.mark.gpu
+
+
+def test_forward_and_gradients_match_fp64(gpu):
+    rng = np.random.default_rng(0)
+    model = hmgpu.RankModel(seed=3)
+    p = (rng.standard_normal(M.NPARAMS) * 0.2).astype(np.float32)
+    norm = np.concatenate([rng.standard_normal(8), rng.uniform(0.5, 2.0, 8)]).astype(np.float32)
+    model.params(set_params=p, set_norm=norm)
+    X = rng.standard_normal((777, 8)).astype(np.float32) * norm[8:] + norm[:8]
+    y = rng.uniform(1, 30, 777).astype(np.float32)
+    out = model.predict(X)
+    ref, _ = M.forward(p, norm.astype(np.float64), X)
+    np.testing.assert_allclose(out, ref, rtol=2e-4, atol=2e-4 * np.abs(ref).max())
+    g, loss = model.gradients(X, y)
+    lref, gref = M.loss_and_grad(p, norm.astype(np.float64), X, y)
+    assert abs(loss - lref) <= 1e-4 * lref
+    assert np.linalg.norm(g - gref) <= 1e-4 * np.linalg.norm(gref)
+    # each parameter block separately, so that a small block cannot hide
+    off = 0
+    for name, shape in M.SIZES:
+        k = int(np.prod(shape))
+        gb, rb = g[off:off + k], gref[off:off + k]
+        assert np.linalg.norm(gb - rb) <= 1e-3 * max(np.linalg.norm(rb), 1e-6), name
+        off += k
+
+
+def _training_set(eps_list=(1e-4, 1e-6)):
+    feats, ranks = [], []
+    geoms = [geometry.cube(6000, seed=1), geometry.film(80, 80), geometry.sphere(6000, seed=2)]
+    for P in geoms:
+        T = hmgpu.ClusterTree(P, max_points_per_leaf=32)
+        for eps in eps_list:
+            H = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=eps, precision="f32")
+            f = hmgpu.block_features(T, T, 2.0, eps)
+            a, _ = H.aca_ranks(len(f))
+            feats.append(f)
+            ranks.append(a.astype(np.float32))
+    return np.concatenate(feats), np.concatenate(ranks)
+
+
+def test_training_and_learned_bucketing(gpu):
+    import torch
+    X, y = _training_set()
+    assert len(y) > 5000 and y.min() >= 1
+    model = hmgpu.RankModel(seed=1)
+    loss0 = model.gradients(X, y)[1]
+    loss = model.train(X, y, epochs=60, batch=512, lr=2e-3, seed=1)
+    assert loss < 0.05 * loss0, (loss0, loss)
+    pred = model.predict(X)
+    mae = float(np.mean(np.abs(pred - y)))
+    assert mae < 0.25 * float(np.mean(y)), mae
+    # a geometry the network has not seen
+    P = geometry.cube(12000, seed=9)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=32)
+    K = hmgpu.Kernel("laplace", P)
+    plain = hmgpu.HMatrix(K, T, T, eta=2.0, eps=1e-5, precision="f32")
+    learned = hmgpu.HMatrix(K, T, T, eta=2.0, eps=1e-5, precision="f32", rank_model=model)
+    x = torch.randn(12000, device=gpu)
+    assert torch.equal(plain * x, learned * x)  # the network never changes the matrix
+    ip, il = plain.info(), learned.info()
+    nblocks = len(hmgpu.block_features(T, T, 2.0, 1e-5))
+    assert il["aca_workspace_bytes"] < 0.6 * ip["aca_workspace_bytes"], (ip, il)
+    assert il["aca_reruns"] <= 0.05 * nblocks, il["aca_reruns"]
