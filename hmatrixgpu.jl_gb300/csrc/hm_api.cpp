@@ -90,6 +90,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   if ((rc = upload(H, &H.dp.tile_order, p.tile_order))) return rc;
   if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
   H.dp.nunits = static_cast<int32_t>(p.units.size());
+  H.dp.nvunits = static_cast<int32_t>(p.vunits.size());
   if ((rc = upload(H, &H.dp.vunits, p.vunits))) return rc;
   if ((rc = upload(H, &H.dp.warp_begin, p.warp_begin))) return rc;
   std::vector<int32_t> t0(H.bs.m), s0(H.bs.n);
@@ -352,11 +353,28 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
       cudaMemset(H.xt_multi, 0, H.plan.xt_len * per * es);
       H.grid_du_multi = H.num_sms * hm::occupancy_du_multi(f64);
     }
+    const bool tc = H.opt.precision == HMGPU_MIXED;
+    if (tc && !H.grid_tc) H.grid_tc = H.num_sms * hm::occupancy_tc();
     for (int64_t k0 = 0; k0 < nrhs; k0 += per) {
       cudaEvent_t *ev;
       if (int rc = next_events(&ev)) return rc;
       const int nr = static_cast<int>(std::min<int64_t>(per, nrhs - k0));
       int nl = 0;
+      if (tc) {  // BF16x3 splits on the tensor cores (hm_tc.cu)
+        if (ev) cudaEventRecord(ev[0], s);
+        cudaError_t e = hm::launch_permute_multi(false, H.dp, static_cast<const char *>(x) + k0 * ldx * es,
+                                                 ldx, nr, H.xt_multi, s);
+        if (ev) cudaEventRecord(ev[1], s);
+        if (e == cudaSuccess)
+          e = hm::launch_matvec_tc(H.dp, static_cast<const float *>(H.panels),
+                                   static_cast<const float *>(H.vdata), static_cast<float *>(H.xt_multi),
+                                   H.grid_tc, s, reinterpret_cast<float *>(static_cast<char *>(y) + k0 * ldy * es),
+                                   ldy, nr, ev ? ev[2] : nullptr);
+        if (ev) cudaEventRecord(ev[3], s);
+        if (e != cudaSuccess) return hm::cuda_fail(e, "tensor-core matvec launch");
+        if (H.profiling) H.prof_launches += H.dp.warp_begin_empty ? 2 : 3;
+        continue;
+      }
       cudaError_t e = hm::launch_matvec_multi(
           f64, H.dp, H.panels, H.vdata, H.xt_multi,
           static_cast<const char *>(x) + k0 * ldx * es, ldx, nr,

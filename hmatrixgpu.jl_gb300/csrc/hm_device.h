@@ -15,6 +15,7 @@ struct DevPlan {
   int32_t nunits = 0;
   int32_t *tile_order = nullptr; // tiles by decreasing work (multi-RHS pass)
   VUnit *vunits = nullptr;
+  int32_t nvunits = 0;
   int32_t *warp_begin = nullptr;
   int32_t nwarps = 0;
   bool warp_begin_empty = true;  // no V units (no low-rank blocks)
@@ -55,6 +56,15 @@ namespace hm {
 // Multi-right-hand-side plain product (hm_multi.cu): up to rhs_per_pass()
 // right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values.
 int rhs_per_pass();
+// Permutation of up to rhs_per_pass() right-hand sides into XT rows (also
+// re-arms both ticket counters).
+cudaError_t launch_permute_multi(bool f64, const DevPlan &p, const void *X, int64_t ldx, int nr,
+                                 void *xt, cudaStream_t s);
+// Mixed-precision tensor-core passes (hm_tc.cu), FP32 storage, 32 RHS per pass.
+int occupancy_tc();
+cudaError_t launch_matvec_tc(const DevPlan &p, const float *panels, const float *vdata, float *xt,
+                             int grid, cudaStream_t s, float *Y, int64_t ldy, int nr,
+                             cudaEvent_t ev_mid);
 
 int occupancy_du_multi(bool f64);
 cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,

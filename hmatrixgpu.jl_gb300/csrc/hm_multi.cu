@@ -68,7 +68,7 @@ __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int n
                                      const int32_t *__restrict__ smap0, int64_t n, int64_t x_len,
                                      T *__restrict__ xt, int32_t *__restrict__ counter) {
   __shared__ T tile[64][kRhs + 1];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *counter = 0;
+  if (blockIdx.x == 0 && threadIdx.x < 2) counter[threadIdx.x] = 0;  // both ticket slots
   for (int64_t c0 = blockIdx.x * 64ll; c0 < x_len; c0 += gridDim.x * 64ll) {
     for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {
       const int r = e / 64, cc = e % 64;  // consecutive threads: consecutive c
@@ -287,6 +287,19 @@ static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, 
 }
 
 int rhs_per_pass() { return kRhs; }
+
+cudaError_t launch_permute_multi(bool f64, const DevPlan &p, const void *X, int64_t ldx, int nr,
+                                 void *xt, cudaStream_t s) {
+  int gp = static_cast<int>((p.x_len + 63) / 64);
+  if (gp > 2048) gp = 2048;
+  if (f64)
+    permute_multi_kernel<double><<<gp, kThreads, 0, s>>>(static_cast<const double *>(X), ldx, nr, p.smap0,
+                                                         p.n, p.x_len, static_cast<double *>(xt), p.counter);
+  else
+    permute_multi_kernel<float><<<gp, kThreads, 0, s>>>(static_cast<const float *>(X), ldx, nr, p.smap0,
+                                                        p.n, p.x_len, static_cast<float *>(xt), p.counter);
+  return cudaGetLastError();
+}
 
 int occupancy_du_multi(bool f64) {
   int n = 0;

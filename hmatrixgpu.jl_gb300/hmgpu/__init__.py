@@ -407,6 +407,15 @@ class HMatrix:
         check(lib().hmgpu_hmatrix_aca_ranks(self._h, ptr(a, I64P), ptr(f, I64P)))
         return a, f
 
+    def status(self):
+        """Device error word of the products so far (0 = clean; synchronises the
+        device). Non-zero values name the bounded wait that ran out."""
+        st = C.c_int32(0)
+        rc = lib().hmgpu_hmatrix_status(self._h, C.byref(st))
+        if rc not in (0, -5):  # HMGPU_ERR_TIMEOUT carries the code in st
+            check(rc)
+        return st.value
+
     # ---- products ------------------------------------------------------------------
     def mul(self, y, x, stream=None):
         """mul!(y, H, x): y and x are torch CUDA tensors (stream-ordered on the

@@ -143,3 +143,23 @@ def test_device_status_clean(case, gpu):
         st = C.c_int(-1)
         assert hmgpu._lib.lib().hmgpu_hmatrix_status(H._h, C.byref(st)) == 0 and st.value == 0
         assert torch.isfinite(y).all()
+
+
+def test_mixed_tensor_core_many_rhs(case, gpu):
+    """HMGPU_MIXED with 32+ right-hand sides runs on the tensor cores (BF16
+    hi/lo splits, FP32 accumulation); its error budget is 2e-4 relative to
+    the FP64 product of the same H-matrix."""
+    import ctypes as C
+    import torch
+    _, _, Ho = case
+    H = hmgpu.HMatrix.from_flat(**_flat(Ho), precision="mixed")
+    for nr in (32, 40, 3):
+        X = np.random.default_rng(nr).standard_normal((Ho.n, nr))
+        Xd = torch.tensor(X, dtype=torch.float32, device=gpu).t().contiguous().t()
+        Y = (H * Xd).double().cpu().numpy()
+        Xr = X.astype(np.float32).astype(np.float64)
+        ref = np.stack([Ho.mul(Xr[:, k]) for k in range(nr)], 1)
+        err = max(rel(Y[:, k], ref[:, k]) for k in range(nr))
+        assert err <= 1e-4, (nr, err)
+    st = C.c_int(-1)
+    assert hmgpu._lib.lib().hmgpu_hmatrix_status(H._h, C.byref(st)) == 0 and st.value == 0
