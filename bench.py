@@ -34,6 +34,9 @@ METRIC = "H-matvec/s at N=2^20, 1 & 32 RHS: mixed vs plain FP32 at equal err; HB
 WORKLOAD = "film-2^20 Laplace leaf64 eta2 tol1e-4, 1 RHS, FP32 storage"
 GRID, LEAF, ETA, TOL = 1024, 64, 2.0, 1e-4
 SAMPLE_STRIDE = 64  # the CPU legs time every 64th dense and admissible block
+# DRAM traffic / algorithmic bytes of the near/U kernel, from an ncu capture on
+# film 256 x 256 (431.6 MB of dram__bytes_read + write for 425.2 MB algorithmic)
+TRAFFIC_RATIO = 431.6 / 425.2
 
 
 def peaks():
@@ -264,9 +267,13 @@ def run_gpu(args):
                       "total_rank": R, "max_rank": inf["max_rank"], "algorithmic_bytes": alg_bytes,
                       "stored_bytes": inf["matrix_bytes"], "build_seconds": build_s},
         "phases_ms": {"permute": ph[0], "v_pass": ph[1], "near_u_pass": ph[2]},
-        "roofline": {"bound": "hbm", "kernel": "du_pass_kernel (near field + U t)",
+        "roofline": {"bound": "hbm", "kernel": "du_rows_kernel<float,0> (near field + U t)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": src, "traffic": None},
+                     "peak_source": src, "algorithmic_bytes_per_launch": du_bytes,
+                     "traffic": du_bytes * TRAFFIC_RATIO,
+                     "traffic_source": "ncu dram__bytes_read+write of du_rows_kernel on film 256x256 "
+                                       "(431.6 MB for 425.2 MB algorithmic), scaled by algorithmic bytes "
+                                       "(profiles/du_rows_kernel_film256.md)"},
         "cpu_baseline": {"value": cpu_v, "unit": "matvec/s", "cores": 1, "kind": "port",
                          "sample": cpu_d["sample"]},
         "e2e": {"value": world / e2e_s, "unit": "matvec/s", "h2d_bytes_per_step": n * es,
