@@ -229,7 +229,37 @@ def run_gpu(args):
     y64 = H64 * x.double()
     hmgpu.mul_(y, H, x)
     rel_err = float(torch.linalg.norm(y.double() - y64) / torch.linalg.norm(y64))
-    del H64
+
+    # 32 right-hand sides: plain FP32 (CUDA cores) against mixed precision
+    # (BF16 hi/lo pairs on the tensor cores), same matrix, errors against the
+    # FP64 product of the same 32 vectors
+    rhs32 = None
+    if not args.skip_rhs32:
+        X = torch.randn(32, n, device=dev, generator=torch.Generator(dev).manual_seed(rank + 3)).t()
+        Y64 = torch.empty(32, n, dtype=torch.float64, device=dev).t()
+        hmgpu.mul_(Y64, H64, X.double())
+        del H64
+        Hm = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=ETA, eps=TOL, precision="mixed")
+        Y = torch.empty(32, n, device=dev).t()
+        rhs32 = {"nrhs": 32, "errors": "max over the 32 columns of ||y - y64|| / ||y64||"}
+        for name, HH in (("plain_f32", H), ("mixed_tensor_cores", Hm)):
+            for _ in range(3):
+                hmgpu.mul_(Y, HH, X)
+            reps = max(5, min(args.steps // 10, 50))
+            torch.cuda.synchronize()
+            s.record(stream)
+            for _ in range(reps):
+                hmgpu.mul_(Y, HH, X)
+            e.record(stream)
+            torch.cuda.synchronize()
+            t32 = s.elapsed_time(e) / reps
+            err = float(((Y.double() - Y64).norm(dim=0) / Y64.norm(dim=0)).max())
+            rhs32[name] = {"ms_per_32rhs_product": t32, "matvec_per_s": 32e3 / t32, "rel_err": err}
+        rhs32["mixed_speedup_vs_plain_f32"] = rhs32["plain_f32"]["ms_per_32rhs_product"] / \
+            rhs32["mixed_tensor_cores"]["ms_per_32rhs_product"]
+        del Hm
+    else:
+        del H64
 
     if rank != 0:
         if dist:
@@ -279,6 +309,7 @@ def run_gpu(args):
         "e2e": {"value": world / e2e_s, "unit": "matvec/s", "h2d_bytes_per_step": n * es,
                 "d2h_bytes_per_step": n * es},
         "gpu_launches": int(nl.value),
+        "rhs32": rhs32,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -293,6 +324,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--grid", type=int, default=1024, help="film side (1024 = the headline workload)")
+    ap.add_argument("--skip-rhs32", action="store_true", help="leave out the 32-RHS plain / mixed lines")
     args = ap.parse_args()
     set_grid(args.grid)
     if args.impl == "reference":

@@ -53,6 +53,8 @@ void HMatrix::dfree(void *p) {
   cudaFree(p);
 }
 
+int build_tc(HMatrix &H);
+
 template <typename V>
 static int upload(HMatrix &H, V **dst, const std::vector<V> &src) {
   int rc = H.dalloc(reinterpret_cast<void **>(dst), src.size() * sizeof(V));
@@ -104,6 +106,11 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
   H.dp.nwarps = p.nwarps;
   H.dp.warp_begin_empty = p.vunits.empty();
+  if ((rc = upload(H, &H.dp.mv_items, p.mv_items))) return rc;
+  if ((rc = upload(H, &H.dp.mv_reduce, p.mv_reduce))) return rc;
+  H.dp.nmv = static_cast<int32_t>(p.mv_items.size());
+  H.dp.nmvr = static_cast<int32_t>(p.mv_reduce.size());
+  H.dp.p_rows = p.p_rows;
   H.dp.m = H.bs.m;
   H.dp.n = H.bs.n;
   H.dp.x_len = p.x_len;
@@ -140,6 +147,47 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   H.dfree(djobs);
   H.dfree(dvj);
   H.device_bytes -= static_cast<int64_t>(p.pjobs.size() * sizeof(PackJob) + vj.size() * sizeof(VPackJob));
+  if (H.opt.precision == HMGPU_MIXED) return build_tc(H);
+  return HMGPU_OK;
+}
+
+// Tensor-core copy of a FP32 layout: canonical BF16 (hi, lo) chunks of every
+// multi-RHS V item and every row tile (hm_tc.cu), packed from the FP32 panels.
+int build_tc(HMatrix &H) {
+  TcPlan tp;
+  make_tc_plan(H.plan, tp);
+  DevTc &t = H.tc;
+  int rc;
+  if ((rc = H.dalloc(&t.adata, tp.bytes))) return rc;
+  H.tc_bytes = tp.bytes;
+  if ((rc = upload(H, &t.v_items, tp.v_items)) || (rc = upload(H, &t.du_items, tp.du_items)) ||
+      (rc = upload(H, &t.colmap, tp.colmap)))
+    return rc;
+  t.reduce = H.dp.mv_reduce;
+  t.n_v = static_cast<int32_t>(tp.v_items.size());
+  t.n_du = static_cast<int32_t>(tp.du_items.size());
+  t.n_reduce = H.dp.nmvr;
+  t.ctas = H.num_sms;
+  std::vector<TcPack> vj, dj;
+  for (size_t i = 0; i < tp.v_items.size(); i++) {
+    const MVItem &it = H.plan.mv_items[i];
+    vj.push_back(TcPack{tp.v_src[i], tp.v_items[i].a_off, it.stride, it.nrows, it.ncols, 0});
+  }
+  for (size_t i = 0; i < tp.du_items.size(); i++) {
+    const TcItem &t = tp.du_items[i];
+    dj.push_back(TcPack{tp.du_src[i], t.a_off, H.plan.tiles[t.out].ld, t.m, t.ncols, 0});
+  }
+  TcPack *dvj = nullptr, *ddj = nullptr;
+  if ((rc = upload(H, &dvj, vj)) || (rc = upload(H, &ddj, dj))) return rc;
+  cudaError_t e = launch_pack_tc(dvj, static_cast<int64_t>(vj.size()), static_cast<const float *>(H.vdata),
+                                 t.adata, 0);
+  if (e == cudaSuccess)
+    e = launch_pack_tc(ddj, static_cast<int64_t>(dj.size()), static_cast<const float *>(H.panels), t.adata, 0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "tensor-core packing");
+  H.dfree(dvj);
+  H.dfree(ddj);
+  H.device_bytes -= static_cast<int64_t>((vj.size() + dj.size()) * sizeof(TcPack));
   return HMGPU_OK;
 }
 
@@ -345,40 +393,37 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
   };
   if (nrhs >= kMultiRhsFrom) {
     // several right-hand sides: one pass per rhs_per_pass() columns, the
-    // matrix read once per pass (hm_multi.cu)
+    // matrix read once per pass (hm_multi.cu; hm_tc.cu for mixed precision)
     const int per = hm::rhs_per_pass();
-    if (!H.xt_multi) {
-      int rc;
-      if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es))) return rc;
+    const bool tc = H.opt.precision == HMGPU_MIXED;
+    int rc;
+    if (tc && !H.tc.xts) {
+      if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts), H.plan.xt_len * 2 * per * 2)) ||
+          (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.prow), std::max<int64_t>(H.plan.p_rows, 1) * per * 4)))
+        return rc;
+      cudaMemset(H.tc.xts, 0, H.plan.xt_len * 2 * per * 2);
+    }
+    if (!tc && !H.xt_multi) {
+      if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es)) ||
+          (rc = H.dalloc(&H.p_multi, std::max<int64_t>(H.plan.p_rows, 1) * per * es)))
+        return rc;
       cudaMemset(H.xt_multi, 0, H.plan.xt_len * per * es);
       H.grid_du_multi = H.num_sms * hm::occupancy_du_multi(f64);
     }
-    const bool tc = H.opt.precision == HMGPU_MIXED;
-    if (tc && !H.grid_tc) H.grid_tc = H.num_sms * hm::occupancy_tc();
     for (int64_t k0 = 0; k0 < nrhs; k0 += per) {
       cudaEvent_t *ev;
-      if (int rc = next_events(&ev)) return rc;
+      if ((rc = next_events(&ev))) return rc;
       const int nr = static_cast<int>(std::min<int64_t>(per, nrhs - k0));
       int nl = 0;
-      if (tc) {  // BF16x3 splits on the tensor cores (hm_tc.cu)
-        if (ev) cudaEventRecord(ev[0], s);
-        cudaError_t e = hm::launch_permute_multi(false, H.dp, static_cast<const char *>(x) + k0 * ldx * es,
-                                                 ldx, nr, H.xt_multi, s);
-        if (ev) cudaEventRecord(ev[1], s);
-        if (e == cudaSuccess)
-          e = hm::launch_matvec_tc(H.dp, static_cast<const float *>(H.panels),
-                                   static_cast<const float *>(H.vdata), static_cast<float *>(H.xt_multi),
-                                   H.grid_tc, s, reinterpret_cast<float *>(static_cast<char *>(y) + k0 * ldy * es),
-                                   ldy, nr, ev ? ev[2] : nullptr);
-        if (ev) cudaEventRecord(ev[3], s);
-        if (e != cudaSuccess) return hm::cuda_fail(e, "tensor-core matvec launch");
-        if (H.profiling) H.prof_launches += H.dp.warp_begin_empty ? 2 : 3;
-        continue;
-      }
-      cudaError_t e = hm::launch_matvec_multi(
-          f64, H.dp, H.panels, H.vdata, H.xt_multi,
-          static_cast<const char *>(x) + k0 * ldx * es, ldx, nr,
-          static_cast<char *>(y) + k0 * ldy * es, ldy, H.grid_v, H.grid_du_multi, s, ev, &nl);
+      cudaError_t e;
+      if (tc)  // BF16 (hi, lo) splits on the tensor cores
+        e = hm::launch_matvec_tc(H.dp, H.tc, reinterpret_cast<const float *>(static_cast<const char *>(x) + k0 * ldx * es),
+                                 ldx, nr, reinterpret_cast<float *>(static_cast<char *>(y) + k0 * ldy * es), ldy,
+                                 s, ev, &nl);
+      else
+        e = hm::launch_matvec_multi(f64, H.dp, H.panels, H.vdata, H.xt_multi, H.p_multi,
+                                    static_cast<const char *>(x) + k0 * ldx * es, ldx, nr,
+                                    static_cast<char *>(y) + k0 * ldy * es, ldy, H.grid_du_multi, s, ev, &nl);
       if (e != cudaSuccess) return hm::cuda_fail(e, "multi-RHS matvec launch");
       if (H.profiling) H.prof_launches += nl;
     }

@@ -31,8 +31,11 @@ struct HMatrix {
   double *u64 = nullptr, *v64 = nullptr;
   std::vector<int64_t> u_src_off, v_src_off;
   // multi-right-hand-side scratch, allocated on first use
-  void *xt_multi = nullptr;
-  int grid_du_multi = 0, grid_tc = 0;
+  void *xt_multi = nullptr, *p_multi = nullptr;
+  int grid_du_multi = 0;
+  // tensor-core copy of the matrix (mixed precision)
+  DevTc tc;
+  int64_t tc_bytes = 0;
   // staging of hmgpu_matvec_host
   void *io_x = nullptr, *io_y = nullptr;
   size_t io_x_bytes = 0, io_y_bytes = 0;

@@ -19,9 +19,14 @@ struct DevPlan {
   int32_t *warp_begin = nullptr;
   int32_t nwarps = 0;
   bool warp_begin_empty = true;  // no V units (no low-rank blocks)
+  MVItem *mv_items = nullptr;  // multi-RHS V items, largest first
+  int32_t nmv = 0;
+  MVReduce *mv_reduce = nullptr;
+  int32_t nmvr = 0;
+  int64_t p_rows = 0;
   int32_t *tmap0 = nullptr;  // 0-based target map, length m
   int32_t *smap0 = nullptr;  // 0-based source map, length n
-  int32_t *counter = nullptr;  // tile ticket of the near/U pass
+  int32_t *counter = nullptr;  // ticket counters of the passes (16 slots)
   int32_t *status = nullptr;   // device error word (0 = ok), see hmgpu_hmatrix_status
   int64_t m = 0, n = 0, x_len = 0, xt_len = 0;
 };
@@ -56,19 +61,31 @@ namespace hm {
 // Multi-right-hand-side plain product (hm_multi.cu): up to rhs_per_pass()
 // right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values.
 int rhs_per_pass();
-// Permutation of up to rhs_per_pass() right-hand sides into XT rows (also
-// re-arms both ticket counters).
-cudaError_t launch_permute_multi(bool f64, const DevPlan &p, const void *X, int64_t ldx, int nr,
-                                 void *xt, cudaStream_t s);
-// Mixed-precision tensor-core passes (hm_tc.cu), FP32 storage, 32 RHS per pass.
-int occupancy_tc();
-cudaError_t launch_matvec_tc(const DevPlan &p, const float *panels, const float *vdata, float *xt,
-                             int grid, cudaStream_t s, float *Y, int64_t ldy, int nr,
-                             cudaEvent_t ev_mid);
+// Mixed-precision tensor-core product (hm_tc.cu), 32 right-hand sides per pass.
+struct TcPack {  // one item's FP32 row-major source -> canonical BF16 chunks
+  int64_t src_off, a_off;
+  int32_t ld, m, ncols, pad;
+};
+struct DevTc {
+  void *adata = nullptr;  // canonical BF16 (hi, lo) chunks of every item
+  TcItem *v_items = nullptr, *du_items = nullptr;
+  int32_t *colmap = nullptr;
+  MVReduce *reduce = nullptr;
+  uint16_t *xts = nullptr;  // xt_len rows of 32 BF16 hi + 32 BF16 lo
+  float *prow = nullptr;    // partial rows of split V items
+  int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;
+};
+size_t tc_smem_bytes();
+cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s);
+// permutation + split of X, V pass, reduction of pieces, near/U pass; ev
+// (optional) gets 4 events as launch_matvec_multi.
+cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr,
+                             float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches);
 
 int occupancy_du_multi(bool f64);
+// P: partial rows of cut V groups (p_rows x rhs_per_pass() values).
 cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,
-                                void *xt, const void *X, int64_t ldx, int nr, void *Y, int64_t ldy,
-                                int grid_v, int grid_du, cudaStream_t s, cudaEvent_t *ev,
+                                void *xt, void *P, const void *X, int64_t ldx, int nr, void *Y,
+                                int64_t ldy, int grid_du, cudaStream_t s, cudaEvent_t *ev,
                                 int *launches);
 }  // namespace hm

@@ -99,6 +99,46 @@ struct VUnit {
 };
 static_assert(sizeof(VUnit) == 32, "VUnit layout");
 
+// A work item of the multi-right-hand-side V pass: at most 128 rows of one
+// source group times one column piece [c, c + ncols) of the group's stored
+// columns. Wide groups are cut into pieces of bounded size whose partial
+// products go to rows of a scratch array P and are summed in piece order
+// afterwards (MVReduce), so every CTA gets similar work and the sums stay
+// deterministic.
+struct MVItem {
+  int64_t v_off;   // element offset of (first row, first column of the piece)
+  int32_t stride;  // row stride of the group's V rows
+  int32_t nrows;   // <= 128
+  int32_t x_off;   // XT row of the piece's first column
+  int32_t ncols;   // multiple of 4
+  int32_t out;     // first output row: XT row (kind 0) or P row (kind 1)
+  int32_t kind;
+};
+static_assert(sizeof(MVItem) == 32, "MVItem layout");
+
+// t rows [t_row, t_row + nrows) = sum over pieces j (in order) of
+// P rows [p_row + j nrows, p_row + (j + 1) nrows).
+struct MVReduce {
+  int32_t t_row, nrows, p_row, npieces;
+};
+
+// A work item of the tensor-core product: a panel of m <= 64 rows and
+// ncols columns stored as BF16 (hi, lo) pairs in the UMMA canonical K-major
+// layout, 64 columns per chunk (the last chunk rounded up to 16 columns):
+// chunk c holds hi then lo, each ceil(m / 8) groups of 8 rows x kc columns
+// (kc * 16 bytes per group). Column j of the panel meets XT row
+// map + j (V items) or colmap[map + j] (near/U items). Row tiles of more
+// than 64 rows become several items.
+struct TcItem {
+  int64_t a_off;    // byte offset of chunk 0 in the tensor-core data
+  int32_t m, ncols;
+  int32_t map;      // XT row of column 0 (V) or colmap offset (near/U)
+  int32_t out;      // tile index (kind 0), XT row (kind 1) or P row (kind 2)
+  int32_t kind;     // 0: rows of y, 1: t rows of XT, 2: rows of P
+  int32_t row0;     // kind 0: first row of the item within its tile
+};
+static_assert(sizeof(TcItem) == 32, "TcItem layout");
+
 // Copy job of the packing pass: a row-major source slice -> rows of a tile panel.
 struct PackJob {
   int64_t src_off;   // element offset in the source array
@@ -131,6 +171,10 @@ struct Plan {
   std::vector<int32_t> warp_begin;  // nwarps + 1
   int nwarps = 0;
   int64_t v_len = 0;
+  // multi-right-hand-side V pass
+  std::vector<MVItem> mv_items;     // largest first
+  std::vector<MVReduce> mv_reduce;
+  int64_t p_rows = 0;               // rows of the partial-product scratch P
   // bytes
   int64_t dense_entries = 0, far_entries = 0;
 };
@@ -139,6 +183,16 @@ struct Plan {
 // row-major FP64 source factors (dense blocks: -1 when generated from a kernel).
 void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_t> &dense_src_off,
                const std::vector<int64_t> &u_src_off, Plan &p);
+
+// Tensor-core layout of a FP32 plan: V items (from the multi-RHS V items),
+// near/U items (row tiles, in pieces of at most 64 rows) and the column maps.
+struct TcPlan {
+  std::vector<TcItem> v_items, du_items;
+  std::vector<int64_t> v_src, du_src;  // element offset of each item's FP32 source rows
+  std::vector<int32_t> colmap;
+  int64_t bytes = 0;                       // tensor-core data size
+};
+void make_tc_plan(const Plan &p, TcPlan &tp);
 
 }  // namespace hm
 

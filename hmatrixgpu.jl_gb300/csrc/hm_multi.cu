@@ -150,30 +150,46 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
   }
 }
 
-// V pass: t[(t_off + k) * kRhs + r] = sum_j V[k, j] XT[(x_off + j) * kRhs + r];
-// CTA b works through the V units of warps [8b, 8b + 8) of the single-RHS
-// pass's byte-balanced split, 128 rows of a unit at a time.
+// V pass: for every multi-RHS V item (ticket order, largest first)
+//   out[(I.out + k) * kRhs + r] = sum_j V[k, j] XT[(I.x_off + j) * kRhs + r],
+// out = XT (t rows) or the partial rows P of a cut group.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) v_multi_kernel(const T *__restrict__ V,
-                                                           const VUnit *__restrict__ units,
-                                                           const int32_t *__restrict__ warp_begin,
-                                                           int nwarps, T *__restrict__ xt) {
+                                                           const MVItem *__restrict__ items,
+                                                           int32_t nitems, T *__restrict__ xt,
+                                                           T *__restrict__ P, int32_t *counter) {
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   T *buf = reinterpret_cast<T *>(dyn_smem);  // XT rows while streaming, slice sums after
-  const int w0 = blockIdx.x * (kThreads / 32);
-  if (w0 >= nwarps) return;
-  const int u0 = warp_begin[w0], u1 = warp_begin[min(w0 + kThreads / 32, nwarps)];
-  for (int u = u0; u < u1; u++) {
-    const VUnit U = units[u];
-    for (int k0 = 0; k0 < U.nrows; k0 += 128) {
-      const int rows = min(128, U.nrows - k0);
-      const T *src = xt + static_cast<int64_t>(U.x_off) * kRhs;
-      multi_panel<T>(
-          V + U.v_off + static_cast<int64_t>(k0) * U.stride, U.stride, rows, U.stride, buf, buf,
-          [&](int c0, int cn, T *xs) {
-            for (int e = threadIdx.x; e < cn * kRhs; e += kThreads) xs[e] = src[static_cast<int64_t>(c0) * kRhs + e];
-          },
-          [&](int row, int q, T s) { xt[static_cast<int64_t>(U.t_off + k0 + row) * kRhs + q] = s; });
+  __shared__ int32_t s_ticket[2];
+  for (int it = 0;; it++) {
+    if (threadIdx.x == 0) s_ticket[it & 1] = atomicAdd(counter, 1);
+    __syncthreads();
+    const int32_t u = s_ticket[it & 1];
+    if (u >= nitems) break;
+    const MVItem I = items[u];
+    const T *src = xt + static_cast<int64_t>(I.x_off) * kRhs;
+    T *out = I.kind == 0 ? xt : P;
+    multi_panel<T>(
+        V + I.v_off, I.stride, I.nrows, I.ncols, buf, buf,
+        [&](int c0, int cn, T *xs) {
+          for (int e = threadIdx.x; e < cn * kRhs; e += kThreads) xs[e] = src[static_cast<int64_t>(c0) * kRhs + e];
+        },
+        [&](int row, int q, T s) { out[static_cast<int64_t>(I.out + row) * kRhs + q] = s; });
+  }
+}
+
+// t rows of cut groups: pieces summed in order (one warp per row, lane = RHS).
+template <typename T>
+__global__ void reduce_multi_kernel(const MVReduce *__restrict__ red, int32_t nred, const T *__restrict__ P,
+                                    T *__restrict__ xt) {
+  const int lane = threadIdx.x & 31;
+  for (int32_t e = static_cast<int32_t>(blockIdx.x); e < nred; e += gridDim.x) {
+    const MVReduce R = red[e];
+    for (int row = threadIdx.x >> 5; row < R.nrows; row += blockDim.x >> 5) {
+      T s = T(0);
+      for (int j = 0; j < R.npieces; j++)
+        s += P[(static_cast<int64_t>(R.p_row) + static_cast<int64_t>(j) * R.nrows + row) * kRhs + lane];
+      xt[static_cast<int64_t>(R.t_row + row) * kRhs + lane] = s;
     }
   }
 }
@@ -262,8 +278,8 @@ static void multi_attrs() {
 }
 
 template <typename T>
-static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, T *xt, const T *X,
-                             int64_t ldx, int nr, T *Y, int64_t ldy, int grid_v, int grid_du,
+static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, T *xt, T *P, const T *X,
+                             int64_t ldx, int nr, T *Y, int64_t ldy, int grid_du,
                              cudaStream_t s, cudaEvent_t *ev, int *launches) {
   multi_attrs<T>();
   int gp = static_cast<int>((p.x_len + 63) / 64);
@@ -273,12 +289,16 @@ static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, 
   permute_multi_kernel<T><<<gp, kThreads, 0, s>>>(X, ldx, nr, p.smap0, p.n, p.x_len, xt, p.counter);
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
-  if (!p.warp_begin_empty) {
-    v_multi_kernel<T><<<grid_v, kThreads, multi_smem<T>(), s>>>(vdata, p.vunits, p.warp_begin, p.nwarps, xt);
+  if (p.nmv > 0) {
+    v_multi_kernel<T><<<grid_du, kThreads, multi_smem<T>(), s>>>(vdata, p.mv_items, p.nmv, xt, P, p.counter);
     nl++;
+    if (p.nmvr > 0) {
+      reduce_multi_kernel<T><<<p.nmvr < 4096 ? p.nmvr : 4096, kThreads, 0, s>>>(p.mv_reduce, p.nmvr, P, xt);
+      nl++;
+    }
   }
   if (ev) cudaEventRecord(ev[2], s);
-  DuMultiArgs<T> a{panels, p.tiles, p.tile_order, p.ntiles, p.segs, xt, p.tmap0, Y, ldy, nr, p.counter};
+  DuMultiArgs<T> a{panels, p.tiles, p.tile_order, p.ntiles, p.segs, xt, p.tmap0, Y, ldy, nr, p.counter + 1};
   du_multi_kernel<T><<<grid_du, kThreads, multi_smem<T>(), s>>>(a);
   nl++;
   if (ev) cudaEventRecord(ev[3], s);
@@ -287,19 +307,6 @@ static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, 
 }
 
 int rhs_per_pass() { return kRhs; }
-
-cudaError_t launch_permute_multi(bool f64, const DevPlan &p, const void *X, int64_t ldx, int nr,
-                                 void *xt, cudaStream_t s) {
-  int gp = static_cast<int>((p.x_len + 63) / 64);
-  if (gp > 2048) gp = 2048;
-  if (f64)
-    permute_multi_kernel<double><<<gp, kThreads, 0, s>>>(static_cast<const double *>(X), ldx, nr, p.smap0,
-                                                         p.n, p.x_len, static_cast<double *>(xt), p.counter);
-  else
-    permute_multi_kernel<float><<<gp, kThreads, 0, s>>>(static_cast<const float *>(X), ldx, nr, p.smap0,
-                                                        p.n, p.x_len, static_cast<float *>(xt), p.counter);
-  return cudaGetLastError();
-}
 
 int occupancy_du_multi(bool f64) {
   int n = 0;
@@ -314,16 +321,17 @@ int occupancy_du_multi(bool f64) {
 }
 
 cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,
-                                void *xt, const void *X, int64_t ldx, int nr, void *Y, int64_t ldy,
-                                int grid_v, int grid_du, cudaStream_t s, cudaEvent_t *ev,
+                                void *xt, void *P, const void *X, int64_t ldx, int nr, void *Y,
+                                int64_t ldy, int grid_du, cudaStream_t s, cudaEvent_t *ev,
                                 int *launches) {
   if (f64)
     return run_multi<double>(p, static_cast<const double *>(panels), static_cast<const double *>(vdata),
-                             static_cast<double *>(xt), static_cast<const double *>(X), ldx, nr,
-                             static_cast<double *>(Y), ldy, grid_v, grid_du, s, ev, launches);
+                             static_cast<double *>(xt), static_cast<double *>(P),
+                             static_cast<const double *>(X), ldx, nr, static_cast<double *>(Y), ldy,
+                             grid_du, s, ev, launches);
   return run_multi<float>(p, static_cast<const float *>(panels), static_cast<const float *>(vdata),
-                          static_cast<float *>(xt), static_cast<const float *>(X), ldx, nr,
-                          static_cast<float *>(Y), ldy, grid_v, grid_du, s, ev, launches);
+                          static_cast<float *>(xt), static_cast<float *>(P), static_cast<const float *>(X),
+                          ldx, nr, static_cast<float *>(Y), ldy, grid_du, s, ev, launches);
 }
 
 }  // namespace hm

@@ -24,6 +24,10 @@ namespace hm {
 static constexpr int kMaxTileRows = 128;
 static constexpr int64_t kVUnitBytes = 64 * 1024;
 static constexpr int32_t kUnitRows = 16;  // rows per near/U unit (2 per warp of 8)
+// multi-RHS V items: at most kMVRows rows (the tensor-core items' limit) and
+// about kMVEntries stored entries
+static constexpr int32_t kMVRows = 64;
+static constexpr int64_t kMVEntries = 64 * 1024;
 // Row strides are multiples of 4 elements (16 bytes in FP32, 32 in FP64): the
 // multi-RHS micro-kernel reads 4 columns per step.
 static constexpr int32_t kRowPad = 4;
@@ -234,6 +238,29 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     const int64_t row_bytes = static_cast<int64_t>(stride) * esize;
     const int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, kVUnitBytes / row_bytes));
     const int64_t t0 = p.t_off[a0];  // the group's t entries are contiguous
+    // multi-RHS items: 128-row blocks, wide ones cut into column pieces
+    for (int32_t k0 = 0; k0 < rows; k0 += kMVRows) {
+      const int32_t nr = std::min(kMVRows, rows - k0);
+      const int64_t pieces0 = std::max<int64_t>(1, (static_cast<int64_t>(nr) * stride + kMVEntries - 1) / kMVEntries);
+      const int32_t w = static_cast<int32_t>(round_up((stride + pieces0 - 1) / pieces0, 64));
+      const int32_t pieces = (stride + w - 1) / w;
+      if (pieces > 1) {
+        p.mv_reduce.push_back(MVReduce{static_cast<int32_t>(t0 + k0), nr, static_cast<int32_t>(p.p_rows), pieces});
+      }
+      for (int32_t j = 0; j < pieces; j++) {
+        MVItem it{};
+        it.v_off = gbase + static_cast<int64_t>(k0) * stride + static_cast<int64_t>(j) * w;
+        it.stride = stride;
+        it.nrows = nr;
+        it.x_off = bs.a_cs[a0] - ph + j * w;
+        it.ncols = std::min(w, stride - j * w);
+        it.kind = pieces > 1 ? 1 : 0;
+        it.out = pieces > 1 ? static_cast<int32_t>(p.p_rows + static_cast<int64_t>(j) * nr)
+                            : static_cast<int32_t>(t0 + k0);
+        p.mv_items.push_back(it);
+      }
+      if (pieces > 1) p.p_rows += static_cast<int64_t>(pieces) * nr;
+    }
     for (int32_t k0 = 0; k0 < rows; k0 += rows_per) {
       VUnit u{};
       u.v_off = gbase + static_cast<int64_t>(k0) * stride;
@@ -247,6 +274,9 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     }
   }
   p.v_len = round_up(std::max<int64_t>(voff, vec), vec);
+  std::stable_sort(p.mv_items.begin(), p.mv_items.end(), [](const MVItem &a, const MVItem &b) {
+    return static_cast<int64_t>(a.nrows) * a.ncols > static_cast<int64_t>(b.nrows) * b.ncols;
+  });
   p.nwarps = std::max(1, nwarps);
   p.warp_begin.assign(p.nwarps + 1, 0);
   {
@@ -269,6 +299,53 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   for (size_t a = 0; a < na; a++)
     p.far_entries += static_cast<int64_t>(bs.a_r[a]) *
                      ((bs.a_re[a] - bs.a_rs[a]) + (bs.a_ce[a] - bs.a_cs[a]));
+}
+
+void make_tc_plan(const Plan &p, TcPlan &tp) {
+  constexpr int32_t kTcRows = 64;  // rows per item: hi and lo stack to the 128 UMMA rows
+  tp = TcPlan();
+  // bytes of an item: hi and lo, ceil(m / 8) row groups x padded columns x 16 B
+  auto item_bytes = [](int32_t m, int32_t ncols) {
+    const int64_t npad = ncols > 0 ? round_up(ncols, 16) : 16;
+    return int64_t(32) * ((m + 7) / 8) * npad;
+  };
+  int64_t off = 0;
+  for (const MVItem &it : p.mv_items) {
+    TcItem t{};
+    t.a_off = off;
+    t.m = it.nrows;
+    t.ncols = it.ncols;
+    t.map = it.x_off;
+    t.out = it.out;
+    t.kind = it.kind == 0 ? 1 : 2;
+    const int64_t b = item_bytes(t.m, t.ncols);
+    off += b;
+    tp.v_items.push_back(t);
+    tp.v_src.push_back(it.v_off);
+  }
+  for (size_t ti = 0; ti < p.tiles.size(); ti++) {
+    const TileDesc &d = p.tiles[ti];
+    const int32_t map = static_cast<int32_t>(tp.colmap.size());
+    for (int32_t q = 0; q < d.nseg; q++) {
+      const Seg &sg = p.segs[d.seg0 + q];
+      for (int32_t j = 0; j < sg.ncols; j++) tp.colmap.push_back(sg.vec_off + j);
+    }
+    for (int32_t r0 = 0; r0 < std::max(d.m, 1); r0 += kTcRows) {
+      TcItem t{};
+      t.a_off = off;
+      t.m = std::min(kTcRows, d.m - r0);
+      t.ncols = d.ncols;
+      t.map = map;
+      t.out = static_cast<int32_t>(ti);
+      t.kind = 0;
+      t.row0 = r0;
+      const int64_t b = item_bytes(t.m, t.ncols);
+      off += b;
+      tp.du_items.push_back(t);
+      tp.du_src.push_back(d.data_off + static_cast<int64_t>(r0) * d.ld);
+    }
+  }
+  tp.bytes = std::max<int64_t>(off, 16);
 }
 
 }  // namespace hm

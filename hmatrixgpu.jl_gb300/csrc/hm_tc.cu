@@ -1,18 +1,34 @@
 // Mixed-precision multi-right-hand-side product on the 5th-generation tensor
-// cores (tcgen05, sm_103a): Y = H X for 32 right-hand sides per pass.
+// cores (tcgen05, sm_103a): Y = H X for up to 32 right-hand sides per pass.
 //
-// Every panel (<= 128 rows of a row tile, or of a V source group) meets the
-// XT rows of its columns as a GEMM D[128 x 32] += A[128 x K] B[32 x K]^T with
-// an FP32 accumulator in tensor memory. Operands are split on the fly into
-// BF16 pairs, a = a_hi + a_lo with a_hi = bf16(a), a_lo = bf16(a - a_hi)
-// (relative residual ~2^-17), and each 16-column step issues three UMMAs:
-// A_hi B_hi + A_hi B_lo + A_lo B_hi. Per 64-column chunk the CTA converts A
-// and B into canonical K-major no-swizzle layouts in shared memory (core
-// matrices of 8 rows x 16 bytes; K-adjacent cores 128 B apart, 8-row groups
-// 1024 B apart), double-buffered, while the previous chunk's UMMAs run; one
-// thread issues the UMMAs and commits them to an mbarrier per buffer. The
-// accumulator is read back with tcgen05.ld (warp w reads TMEM lanes
-// 32w..32w+31). All mbarrier waits are bounded and report into `status`.
+// Storage. Every panel of the product (a row tile of the near/U pass, or a
+// column piece of at most 128 V rows of a source group) is stored once more as
+// BF16 pairs a = hi + lo (hi = bf16(a), lo = bf16(a - hi); relative residual
+// about 2^-17; all four products of the hi/lo pairs are formed), already in
+// the UMMA canonical K-major layout, 64 columns per
+// chunk, so a chunk is two contiguous byte ranges copied as they are. The right-hand sides live in XTS, one 128-byte
+// row per entry of XT = [x permuted | t]: 32 BF16 hi values, then 32 lo values.
+//
+// Pipeline (one persistent CTA per SM; items from a ticket counter, in list
+// order, so concurrent CTAs work on neighbouring panels and share XTS rows in
+// L2; warp 0 takes the tickets and queues them for the other roles):
+//   warp 0      item tickets (lane 0), queued in shared memory for the others;
+//   warps 1, 3, 8-13  producers (chunk g to producer g mod 8) of an 8-stage
+//               ring of 64-column chunks: 16-byte cp.async copies of the chunk (hi rows to tile
+//               rows 0..63, lo rows to tile rows 64..127) and gathers of the
+//               XTS rows of its columns (whole 128-byte rows) into an N-major
+//               (MN-major) BF16 tile, then a wait, a proxy fence and an
+//               mbarrier arrive;
+//   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
+//               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 64 (hi and lo
+//               stacked along both M and N; items have at most 64 rows), into
+//               one of two 64-column TMEM accumulators (FP32); commits free the
+//               stage and, at the end of an item, hand the accumulator on;
+//   warps 4-7   epilogue: tcgen05.ld of TMEM lanes 32(w-4).., the sum of the
+//               four hi/lo quadrants, then y rows, t rows of XTS (split again)
+//               or partial rows P.
+// Every wait is bounded by the global timer; one that runs out records a code
+// in `status`, raises a CTA-wide abort flag and every role leaves its loop.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -22,28 +38,50 @@ namespace hm {
 
 namespace {
 
-constexpr int kTcThreads = 128;   // 4 warps: one per 32 TMEM lanes
-constexpr int kTcRhs = 32;        // N of the UMMA
-constexpr int kKc = 64;           // columns per chunk (4 UMMA K-steps of 16)
-constexpr int kABytes = 128 * kKc * 2;   // one BF16 A tile: 16 KB
-constexpr int kBBytes = kTcRhs * kKc * 2;  // one BF16 B tile: 4 KB
-constexpr uint32_t kSpin = 1u << 24;
+constexpr int kTcWarps = 14;   // roles: see the header comment
+constexpr int kBProducers = 8;  // warps 1, 3, 8..13
+constexpr int kTcThreads = kTcWarps * 32;
+constexpr int kTcRhs = 32;
+constexpr int kKc = 64;             // columns per chunk
+constexpr int kStages = 8;
+constexpr int kABytes = 128 * kKc * 2;    // A tile: 64 hi rows, then 64 lo rows: 16 KB
+constexpr int kBN = 2 * kTcRhs;           // B rows: 32 hi right-hand sides, then 32 lo
+constexpr int kBBytes = kBN * kKc * 2;    // one BF16 B tile: 8 KB
+constexpr uint32_t kTmemCols = 128;       // two 64-column accumulators
+constexpr int kQ = 16;                    // item queue slots
+constexpr int kConsumers = kBProducers + 1 + 4;  // warps that read each queued item
+// One producer per stage: a producer then never waits for a stage more than one
+// release ahead, which a parity wait on the stage's barrier could not tell
+// apart from the release before.
+static_assert(kBProducers == kStages, "one producer warp per stage");
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+
+// MN-major B with N = 64: the hi and lo halves of the 32 right-hand sides are
+// stacked along N, so one XTS row (128 bytes) is one K row of B. Core
+// matrices of 8 N values (16 B) x 8 columns; the 8 N groups are kBGroupN
+// bytes apart, the K groups of 8 columns kBGroupK bytes apart.
+constexpr uint32_t kBGroupN = 128;
+constexpr uint32_t kBGroupK = 8 * kBGroupN;
+constexpr uint32_t kBLbo = kBGroupK;  // leading byte offset: K direction
+constexpr uint32_t kBSbo = kBGroupN;  // stride byte offset: N direction
 
 __device__ __forceinline__ uint32_t su32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFF);
-  d |= static_cast<uint64_t>(128 >> 4) << 16;   // K-adjacent core matrices
-  d |= static_cast<uint64_t>(1024 >> 4) << 32;  // 8-row groups
-  d |= static_cast<uint64_t>(1) << 46;          // descriptor version for tcgen05
-  return d;                                     // no swizzle, base offset 0
+  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFF) << 16;
+  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32;
+  d |= static_cast<uint64_t>(1) << 46;  // descriptor version for tcgen05; no swizzle
+  return d;
 }
 
-// kind::f16 instruction descriptor: BF16 A and B (K-major), FP32 D, M = 128, N = 32.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((kTcRhs >> 3) << 17) | ((128u >> 4) << 24);
+// kind::f16 instruction descriptor: FP32 D, BF16 A (K-major) and B (MN-major),
+// N = 64, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) |
+                            ((static_cast<uint32_t>(kBN) >> 3) << 17) | ((128u >> 4) << 24);
 
 __device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
@@ -57,148 +95,20 @@ __device__ __forceinline__ void commit(uint64_t *bar) {
                : "memory");
 }
 
-__device__ __forceinline__ bool wait_parity(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpin; i++) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(su32(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
+__device__ __forceinline__ void arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
 }
 
-// Byte offset of element (row, k) in a canonical K-major BF16 tile of 64 columns.
-__device__ __forceinline__ int canon(int row, int k) {
-  return (row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\telect.sync _|p, 0xffffffff;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(pred));
+  return pred != 0;
 }
 
-__device__ __forceinline__ void split(float v, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
-  hi = __float2bfloat16_rn(v);
-  lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-}
-
-struct TcSmem {
-  unsigned char a_hi[2][kABytes], a_lo[2][kABytes];
-  unsigned char b_hi[2][kBBytes], b_lo[2][kBBytes];
-  float xrow[kKc][kTcRhs];  // the chunk's XT rows (FP32) before splitting
-  uint64_t bar[2];
-  uint32_t tmem;
-  int32_t ticket[2];
-  int32_t abort;  // a bounded wait ran out: stop taking work
-  int32_t cmap[kKc];
-};
-
-}  // namespace
-
-// One panel: rows [0, m) (m <= 128) of a row-major FP32 matrix A (stride lda,
-// rows zero-padded to a multiple of 4 columns), K = ncols_pad columns, times the
-// XT rows named by `col_row(c)` (-1 = zero row). Calls emit(row, q, value).
-template <typename ColRow, typename Emit>
-__device__ __forceinline__ void tc_panel(TcSmem &S, uint32_t (&phase)[2], uint32_t (&pending)[2],
-                                         const float *A, int64_t lda, int m, int ncols_pad,
-                                         const float *xt, ColRow col_row, Emit emit,
-                                         int32_t *status) {
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  int buf = 0;
-  bool first = true;
-  for (int c0 = 0; c0 < ncols_pad; c0 += kKc) {
-    const int cn = min(kKc, ncols_pad - c0);  // a multiple of 4
-    // the UMMAs that last read this buffer must be done before it is rewritten
-    if (pending[buf]) {
-      if (tid == 0 && !wait_parity(&S.bar[buf], phase[buf])) {
-        atomicCAS(status, 0, 11);
-        S.abort = 1;
-      }
-      __syncthreads();
-      phase[buf] ^= 1;
-      pending[buf] = 0;
-      if (S.abort) return;  // uniform: read after the barrier
-    }
-    // XT rows of the chunk's columns
-    for (int j = tid; j < kKc; j += kTcThreads) S.cmap[j] = j < cn ? col_row(c0 + j) : -1;
-    __syncthreads();
-    for (int e = tid; e < kKc * (kTcRhs / 4); e += kTcThreads) {
-      const int j = e / (kTcRhs / 4), q = (e % (kTcRhs / 4)) * 4;
-      const int r = S.cmap[j];
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r >= 0) v = *reinterpret_cast<const float4 *>(xt + static_cast<int64_t>(r) * kTcRhs + q);
-      *reinterpret_cast<float4 *>(&S.xrow[j][q]) = v;
-    }
-    // A: rows split into hi/lo, canonical layout; two rows per warp per step,
-    // 16 lanes x 4 columns per row
-    // (all 16 loads of a thread are issued before the first is used)
-    {
-      const int half = lane >> 4, c4 = (lane & 15) * 4, row0 = warp * 2 + half;
-      float4 v[16];
-#pragma unroll
-      for (int i = 0; i < 16; i++) {
-        const int row = row0 + 8 * i;
-        v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (row < m && c4 < cn) v[i] = __ldcs(reinterpret_cast<const float4 *>(A + static_cast<int64_t>(row) * lda + c0 + c4));
-      }
-#pragma unroll
-      for (int i = 0; i < 16; i++) {
-        __nv_bfloat16 h[4], l[4];
-        split(v[i].x, h[0], l[0]);
-        split(v[i].y, h[1], l[1]);
-        split(v[i].z, h[2], l[2]);
-        split(v[i].w, h[3], l[3]);
-        const int off = canon(row0 + 8 * i, c4);
-        *reinterpret_cast<uint2 *>(S.a_hi[buf] + off) = *reinterpret_cast<uint2 *>(h);
-        *reinterpret_cast<uint2 *>(S.a_lo[buf] + off) = *reinterpret_cast<uint2 *>(l);
-      }
-    }
-    __syncthreads();
-    // B: for right-hand side n and 8 consecutive columns k, one 16-byte store
-    for (int e = tid; e < kTcRhs * (kKc / 8); e += kTcThreads) {
-      const int n = e % kTcRhs, k8 = (e / kTcRhs) * 8;
-      __nv_bfloat16 h[8], l[8];
-#pragma unroll
-      for (int q = 0; q < 8; q++) split(S.xrow[k8 + q][n], h[q], l[q]);
-      const int off = canon(n, k8);
-      *reinterpret_cast<uint4 *>(S.b_hi[buf] + off) = *reinterpret_cast<uint4 *>(h);
-      *reinterpret_cast<uint4 *>(S.b_lo[buf] + off) = *reinterpret_cast<uint4 *>(l);
-    }
-    // generic-proxy writes -> visible to the tensor cores' async proxy
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (tid == 0) {
-      const uint32_t ah = su32(S.a_hi[buf]), al = su32(S.a_lo[buf]);
-      const uint32_t bh = su32(S.b_hi[buf]), bl = su32(S.b_lo[buf]);
-      bool overwrite = first;
-      for (int ks = 0; ks < cn / 16 + (cn % 16 ? 1 : 0); ks++) {
-        const uint32_t step = ks * 256;  // 16 columns = two K-adjacent core matrices
-        mma(S.tmem, sdesc(ah + step), sdesc(bh + step), overwrite ? 0u : 1u);
-        overwrite = false;
-        mma(S.tmem, sdesc(ah + step), sdesc(bl + step), 1u);
-        mma(S.tmem, sdesc(al + step), sdesc(bh + step), 1u);
-      }
-      commit(&S.bar[buf]);
-    }
-    first = false;  // uniform across the CTA: the accumulator now holds this panel's sums
-    pending[buf] = 1;
-    buf ^= 1;
-  }
-  // wait for the last UMMAs, then read the accumulator
-  for (int b = 0; b < 2; b++)
-    if (pending[b]) {
-      if (tid == 0 && !wait_parity(&S.bar[b], phase[b])) {
-        atomicCAS(status, 0, 12);
-        S.abort = 1;
-      }
-      __syncthreads();
-      phase[b] ^= 1;
-      pending[b] = 0;
-    }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  uint32_t r[kTcRhs];
-  const uint32_t taddr = S.tmem + (static_cast<uint32_t>(warp * 32) << 16);
+// 32 consecutive accumulator columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
       "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -208,152 +118,457 @@ __device__ __forceinline__ void tc_panel(TcSmem &S, uint32_t (&phase)[2], uint32
         "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
         "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-  const int row = warp * 32 + lane;
-  if (first == false && row < m)
-#pragma unroll
-    for (int q = 0; q < kTcRhs; q++) emit(row, q, __uint_as_float(r[q]));
-  if (first && row < m)  // no columns: the panel contributes zeros
-#pragma unroll
-    for (int q = 0; q < kTcRhs; q++) emit(row, q, 0.0f);
-  // the next panel's first UMMA overwrites the accumulator
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
 }
 
-__device__ __forceinline__ void tc_setup(TcSmem &S) {
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+struct TcSmem {
+  unsigned char a[kStages][kABytes];
+  unsigned char b[kStages][kBBytes];
+  float epi[64][kTcRhs + 1];  // lo-row sums handed from epilogue warps 6, 7 to 4, 5
+  uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], epi_ready, epi_free;
+  uint64_t qfull[kQ], qempty[kQ];
+  int32_t qitem[kQ];  // item queue: ticket order, -1 ends it
+  uint32_t tmem;
+  volatile int32_t abort;
+};
+
+// Waits for the phase of `bar` with parity `parity`; false when the abort flag
+// is up or the time limit ran out (then the flag goes up and `code` is recorded).
+__device__ __forceinline__ bool wait_bar(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
+                                         int code) {
+  const unsigned long long t0 = now_ns();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (S.abort) return false;
+    if (now_ns() - t0 > kWaitNs) {
+      atomicCAS(status, 0, code);
+      S.abort = 1;
+      return false;
+    }
+  }
+}
+
+// wait_bar by every lane of a warp, with one answer for the whole warp
+__device__ __forceinline__ bool wait_bar_warp(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
+                                              int code) {
+  return __all_sync(0xffffffffu, wait_bar(S, bar, parity, status, code));
+}
+
+// Item n of this CTA from the queue (-1: no more items, or an abort); every
+// consumer warp calls it once per n and releases the slot.
+__device__ __forceinline__ int next_item(TcSmem &S, int n, int32_t *status) {
+  const int q = n % kQ;
+  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((n / kQ) & 1), status, 30)) return -1;
+  const int it = S.qitem[q];
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) arrive(&S.qempty[q]);
+  return it;
+}
+
+__device__ __forceinline__ int64_t chunk_bytes(int G, int kc) { return static_cast<int64_t>(G) * kc * 16; }
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// hi/lo split of 8 values into two 16-byte words
+__device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo) {
+  float h[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) h[i] = __bfloat162float(__float2bfloat16_rn(v[i]));
+  hi = make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+  lo = make_uint4(pack2(v[0] - h[0], v[1] - h[1]), pack2(v[2] - h[2], v[3] - h[3]),
+                  pack2(v[4] - h[4], v[5] - h[5]), pack2(v[6] - h[6], v[7] - h[7]));
+}
+
+struct TcArgs {
+  const unsigned char *adata;  // tensor-core panels
+  const TcItem *items;
+  int32_t nitems;
+  int32_t *ticket;             // next item (zeroed by the permutation kernel)
+  const int32_t *colmap;
+  const uint16_t *xts;         // XTS rows (64 BF16 each)
+  uint16_t *xts_out;           // t rows (kind 1)
+  float *prow;                 // P rows (kind 2)
+  const TileDesc *tiles;
+  const int32_t *tmap0;
+  float *y;
+  int64_t ldy;
+  int32_t nr;
+  int32_t zero_row;
+  int32_t *status;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  TcSmem &S = *reinterpret_cast<TcSmem *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     S.abort = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.bar[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.bar[1])));
+    for (int s = 0; s < kStages; s++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.full[s])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.empty[s])));
+    }
+    for (int b = 0; b < 2; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.acc_full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(su32(&S.acc_empty[b])));
+    }
+    for (int q = 0; q < kQ; q++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.qfull[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&S.qempty[q])), "r"(kConsumers));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.epi_ready)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.epi_free)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if ((threadIdx.x >> 5) == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(su32(&S.tmem)));
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&S.tmem)),
+                 "r"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
 
-__device__ __forceinline__ void tc_teardown(TcSmem &S) {
+  if (warp == 0) {
+    // ---- A producer ---------------------------------------------------------
+    // ---- item tickets: lane 0 takes them and queues them for the others ----
+    if (lane == 0) {
+      for (int n = 0; !S.abort; n++) {
+        const int q = n % kQ;
+        if (!wait_bar(S, &S.qempty[q], static_cast<uint32_t>((n / kQ) & 1) ^ 1u, a.status, 29)) break;
+        int it = atomicAdd(a.ticket, 1);
+        if (it >= a.nitems) it = -1;
+        S.qitem[q] = it;
+        arrive(&S.qfull[q]);
+        if (it < 0) break;
+      }
+    }
+  } else if (warp == 1 || warp == 3 || warp >= 8) {
+    // ---- producers: chunk g (stage g % 8) goes to producer g % 8 --------------
+    // Column rows are looked up before the stage is free; then each of kKc / 4
+    // instructions copies 4 whole XTS rows (8 lanes x 16 bytes per row), the
+    // warp waits for its copies, fences them for the tensor cores' proxy and
+    // publishes the stage.
+    const int bw = warp == 1 ? 0 : warp == 3 ? 1 : warp - 6;  // 0..7
+    int64_t g = 0;
+    bool stop = false;
+    const int piece = lane & 7, sub = lane >> 3;
+    for (int n = 0; !stop; n++) {
+      const int it = next_item(S, n, a.status);
+      if (it < 0) break;
+      const TcItem I = a.items[it];
+      const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
+      for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
+        if ((g & (kBProducers - 1)) != bw) continue;
+        const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
+        int rows[kKc / 32];  // XTS rows of columns c0 + lane + 32 h
+#pragma unroll
+        for (int h = 0; h < kKc / 32; h++) {
+          const int c = c0 + lane + 32 * h;
+          rows[h] = a.zero_row;
+          if (c < I.ncols) rows[h] = I.kind == 0 ? __ldg(a.colmap + I.map + c) : I.map + c;
+        }
+        if (!wait_bar_warp(S, &S.empty[s], static_cast<uint32_t>((g / kStages) & 1) ^ 1u, a.status, 22)) {
+          stop = true;
+          break;
+        }
+        {  // A: the chunk's hi rows to tile rows 0.., its lo rows to tile rows 64..
+          const int G = (I.m + 7) >> 3;
+          const int units = G * kc;  // 16-byte units of each half
+          const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
+          const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
+          for (int u = lane; u < units; u += 32) {
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(hi + 16u * u), "l"(src + 16 * u) : "memory");
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(lo + 16u * u),
+                         "l"(src + 16 * (units + u))
+                         : "memory");
+          }
+        }
+        const uint32_t dst0 = su32(S.b[s]) + piece * kBGroupN;
+#pragma unroll
+        for (int i = 0; i < kKc / 4; i++) {
+          const int k = 4 * i + sub;
+          const int r = __shfl_sync(0xffffffffu, rows[i >> 3], k & 31);
+          if (k < kc) {
+            const uint16_t *src = a.xts + static_cast<int64_t>(r) * (2 * kTcRhs) + piece * 8;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst0 + (k >> 3) * kBGroupK + (k & 7) * 16),
+                         "l"(src)
+                         : "memory");
+          }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) arrive(&S.full[s]);
+      }
+    }
+  } else if (warp == 2) {
+    // ---- MMA issuer: the warp runs the loop, one elected lane issues --------
+    // Per 16 columns one UMMA: [A_hi; A_lo] (M = 128) x [B_hi B_lo] (N = 64)
+    // into the item's accumulator; the epilogue adds its four quadrants.
+    int64_t g = 0;
+    int n = 0;
+    bool stop = false;
+    for (; !stop; n++) {
+      const int it = next_item(S, n, a.status);
+      if (it < 0) break;
+      const TcItem I = a.items[it];
+      const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
+      const int ab = n & 1;
+      if (!wait_bar_warp(S, &S.acc_empty[ab], static_cast<uint32_t>((n >> 1) & 1) ^ 1u, a.status, 23)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t acc = S.tmem + ab * kBN;
+      for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
+        const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
+        if (!wait_bar_warp(S, &S.full[s], static_cast<uint32_t>((g / kStages) & 1), a.status, 24)) {
+          stop = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t asbo = static_cast<uint32_t>(kc) * 16;
+        const uint64_t da = sdesc(su32(S.a[s]), 128, asbo);
+        const uint64_t db = sdesc(su32(S.b[s]), kBGroupK, kBGroupN);
+        if (elect_one()) {
+          for (int ks = 0; ks < kc / 16; ks++) {
+            // the start address field counts 16-byte units
+            const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4, ob = static_cast<uint64_t>(ks * 2 * kBGroupK) >> 4;
+            mma(acc, da + oa, db + ob, (c0 | ks) ? 1u : 0u);
+          }
+          commit(&S.empty[s]);
+        }
+        __syncwarp();
+      }
+      if (stop) break;
+      if (elect_one()) commit(&S.acc_full[ab]);
+      __syncwarp();
+    }
+    // the last stage release must land before the CTA's shared memory goes away
+    if (!stop && g > 0)
+      wait_bar_warp(S, &S.empty[(g - 1) % kStages], static_cast<uint32_t>(((g - 1) / kStages) & 1), a.status, 26);
+  } else if (warp >= 4 && warp < 8) {
+    // ---- epilogue -----------------------------------------------------------
+    // Warp w reads TMEM lanes 32(w-4)..: warps 4, 5 hold the A_hi rows, warps
+    // 6, 7 the A_lo rows of the same panel rows. Warps 6, 7 hand their sums
+    // to 4, 5 through shared memory; 4, 5 add and write the results.
+    const int quarter = warp & 3, row = (quarter & 1) * 32 + lane;
+    const bool lo_part = quarter >= 2;
+    int n = 0;
+    for (;; n++) {
+      const int it = next_item(S, n, a.status);
+      if (it < 0) break;
+      const TcItem I = a.items[it];
+      const int ab = n & 1;
+      if (!wait_bar_warp(S, &S.acc_full[ab], static_cast<uint32_t>((n >> 1) & 1), a.status, 25)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      uint32_t r[kTcRhs], r2[kTcRhs];
+      const uint32_t taddr = S.tmem + ab * kBN + (static_cast<uint32_t>(quarter * 32) << 16);
+      tmem_ld32(taddr, r);
+      tmem_ld32(taddr + kTcRhs, r2);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) arrive(&S.acc_empty[ab]);
+      float v[kTcRhs];  // A_part B_hi + A_part B_lo
+#pragma unroll
+      for (int q = 0; q < kTcRhs; q++) v[q] = __uint_as_float(r[q]) + __uint_as_float(r2[q]);
+      if (lo_part) {
+        if (!wait_bar_warp(S, &S.epi_free, static_cast<uint32_t>(n & 1) ^ 1u, a.status, 27)) break;
+#pragma unroll
+        for (int q = 0; q < kTcRhs; q++) S.epi[row][q] = v[q];
+        __syncwarp();
+        if (lane == 0) arrive(&S.epi_ready);
+        continue;
+      }
+      if (!wait_bar_warp(S, &S.epi_ready, static_cast<uint32_t>(n & 1), a.status, 28)) break;
+#pragma unroll
+      for (int q = 0; q < kTcRhs; q++) v[q] += S.epi[row][q];
+      __syncwarp();
+      if (lane == 0) arrive(&S.epi_free);
+      if (row >= I.m) continue;
+      if (I.kind == 0) {
+        float *yr = a.y + a.tmap0[a.tiles[I.out].row0 + I.row0 + row];
+#pragma unroll
+        for (int q = 0; q < kTcRhs; q++)
+          if (q < a.nr) yr[q * a.ldy] = v[q];
+      } else if (I.kind == 1) {
+        uint4 *dst = reinterpret_cast<uint4 *>(a.xts_out + static_cast<int64_t>(I.out + row) * (2 * kTcRhs));
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          uint4 hi, lo;
+          split8(v + 8 * q, hi, lo);
+          dst[q] = hi;
+          dst[4 + q] = lo;
+        }
+      } else {
+        float4 *dst = reinterpret_cast<float4 *>(a.prow + static_cast<int64_t>(I.out + row) * kTcRhs);
+#pragma unroll
+        for (int q = 0; q < 8; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+    }
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if ((threadIdx.x >> 5) == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(S.tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(kTmemCols));
 }
 
-// V pass: t rows of every V unit (source-group rows), 128 at a time.
-__global__ void __launch_bounds__(kTcThreads) v_tc_kernel(const float *__restrict__ V,
-                                                          const VUnit *__restrict__ units,
-                                                          int32_t nunits, float *__restrict__ xt,
-                                                          int32_t *counter, int32_t *status) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
-  tc_setup(S);
-  uint32_t phase[2] = {0, 0}, pending[2] = {0, 0};
-  for (int it = 0;; it++) {
-    if (threadIdx.x == 0) S.ticket[it & 1] = atomicAdd(counter, 1);
-    __syncthreads();
-    const int u = S.ticket[it & 1];
-    if (u >= nunits) break;
-    const VUnit U = units[u];
-    for (int k0 = 0; k0 < U.nrows; k0 += 128) {
-      const int rows = min(128, U.nrows - k0);
-      tc_panel(
-          S, phase, pending, V + U.v_off + static_cast<int64_t>(k0) * U.stride, U.stride, rows,
-          U.stride, xt, [&](int c) { return U.x_off + c; },
-          [&](int row, int q, float v) { xt[static_cast<int64_t>(U.t_off + k0 + row) * kTcRhs + q] = v; },
-          status);
-      if (S.abort) break;
+// XTS x rows: row c holds the 32 right-hand sides X[smap[c] + r ldx] split into
+// BF16 hi (first 64 bytes) and lo (last 64 bytes); rows c >= n are zero.
+__global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, int nr,
+                                     const int32_t *__restrict__ smap0, int64_t n, int64_t x_len,
+                                     uint16_t *__restrict__ xts, int32_t *__restrict__ tickets) {
+  __shared__ float tile[64][kTcRhs + 1];
+  if (blockIdx.x == 0 && threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
+  for (int64_t c0 = blockIdx.x * 64ll; c0 < x_len; c0 += gridDim.x * 64ll) {
+    for (int e = threadIdx.x; e < 64 * kTcRhs; e += blockDim.x) {
+      const int r = e / 64, cc = e % 64;  // consecutive threads: consecutive c
+      const int64_t c = c0 + cc;
+      tile[cc][r] = (c < n && r < nr) ? X[smap0[c] + r * ldx] : 0.0f;
     }
-    if (S.abort) break;
-  }
-  tc_teardown(S);
-}
-
-// Near/U pass: one whole row tile per panel.
-struct DuTcArgs {
-  const float *panels;
-  const TileDesc *tiles;
-  const int32_t *order;
-  int32_t ntiles;
-  const Seg *segs;
-  const float *xt;
-  const int32_t *tmap0;
-  float *y;
-  int64_t ldy;
-  int nr;
-  int32_t *counter;
-  int32_t *status;
-};
-
-__global__ void __launch_bounds__(kTcThreads) du_tc_kernel(DuTcArgs a) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcSmem &S = *reinterpret_cast<TcSmem *>(smem_raw);
-  tc_setup(S);
-  uint32_t phase[2] = {0, 0}, pending[2] = {0, 0};
-  for (int it = 0;; it++) {
-    if (threadIdx.x == 0) S.ticket[it & 1] = atomicAdd(a.counter, 1);
     __syncthreads();
-    const int u = S.ticket[it & 1];
-    if (u >= a.ntiles) break;
-    const TileDesc d = a.tiles[a.order[u]];
-    const Seg *sg = a.segs + d.seg0;
-    tc_panel(
-        S, phase, pending, a.panels + d.data_off, d.ld, d.m, d.ld, a.xt,
-        [&](int c) {
-          if (c >= d.ncols) return -1;
-          int lo = 0, hi = d.nseg - 1;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (sg[mid].col0 <= c)
-              lo = mid;
-            else
-              hi = mid - 1;
-          }
-          return sg[lo].vec_off + (c - sg[lo].col0);
-        },
-        [&](int row, int q, float v) {
-          if (q < a.nr) a.y[a.tmap0[d.row0 + row] + q * a.ldy] = v;
-        },
-        a.status);
-    if (S.abort) break;
+    for (int e = threadIdx.x; e < 64 * 4; e += blockDim.x) {
+      const int cc = e >> 2, q = e & 3;
+      if (c0 + cc < x_len) {
+        float v[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) v[i] = tile[cc][8 * q + i];
+        uint4 hi, lo;
+        split8(v, hi, lo);
+        uint4 *dst = reinterpret_cast<uint4 *>(xts + (c0 + cc) * (2 * kTcRhs));
+        dst[q] = hi;
+        dst[4 + q] = lo;
+      }
+    }
+    __syncthreads();
   }
-  tc_teardown(S);
 }
+
+// t rows from partial rows, pieces summed in order; one warp per row, lane =
+// right-hand side.
+__global__ void reduce_split_kernel(const MVReduce *__restrict__ red, int32_t nred, const float *__restrict__ P,
+                                    uint16_t *__restrict__ xts) {
+  const int lane = threadIdx.x & 31;
+  for (int32_t e = static_cast<int32_t>(blockIdx.x); e < nred; e += gridDim.x) {
+    const MVReduce R = red[e];
+    for (int row = threadIdx.x >> 5; row < R.nrows; row += blockDim.x >> 5) {
+      float s = 0.0f;
+      for (int j = 0; j < R.npieces; j++)
+        s += P[(static_cast<int64_t>(R.p_row) + static_cast<int64_t>(j) * R.nrows + row) * kTcRhs + lane];
+      const __nv_bfloat16 hb = __float2bfloat16_rn(s);
+      const __nv_bfloat16 lb = __float2bfloat16_rn(s - __bfloat162float(hb));
+      uint16_t *dst = xts + static_cast<int64_t>(R.t_row + row) * (2 * kTcRhs);
+      dst[lane] = *reinterpret_cast<const uint16_t *>(&hb);
+      dst[kTcRhs + lane] = *reinterpret_cast<const uint16_t *>(&lb);
+    }
+  }
+}
+
+// Canonical BF16 (hi, lo) chunks of one item from its FP32 row-major source.
+__global__ void pack_tc_kernel(const TcPack *__restrict__ jobs, const float *__restrict__ src,
+                               unsigned char *__restrict__ adata) {
+  const TcPack J = jobs[blockIdx.x];
+  const int G = (J.m + 7) >> 3;
+  const int npad = J.ncols > 0 ? (J.ncols + 15) & ~15 : 16;
+  unsigned char *base = adata + J.a_off;
+  for (int c0 = 0; c0 < npad; c0 += kKc) {
+    const int kc = min(kKc, npad - c0);
+    const int64_t half = static_cast<int64_t>(G) * kc * 16;
+    const int units = G * 8 * (kc / 8);  // (row, 8 columns)
+    for (int u = threadIdx.x; u < units; u += blockDim.x) {
+      const int r = u / (kc / 8), k8 = (u % (kc / 8)) * 8;
+      float v[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int c = c0 + k8 + i;
+        v[i] = (r < J.m && c < J.ncols) ? src[J.src_off + static_cast<int64_t>(r) * J.ld + c] : 0.0f;
+      }
+      uint4 hi, lo;
+      split8(v, hi, lo);
+      const int64_t off = static_cast<int64_t>(r >> 3) * kc * 16 + (k8 >> 3) * 128 + (r & 7) * 16;
+      *reinterpret_cast<uint4 *>(base + off) = hi;
+      *reinterpret_cast<uint4 *>(base + half + off) = lo;
+    }
+    base += 2 * half;
+  }
+}
+
+}  // namespace
 
 size_t tc_smem_bytes() { return sizeof(TcSmem) + 1024; }
 
 static void tc_attrs() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(v_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_smem_bytes()));
-  cudaFuncSetAttribute(du_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_smem_bytes()));
+  cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_smem_bytes()));
   done = true;
 }
 
-int occupancy_tc() {
-  tc_attrs();
-  int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_tc_kernel, kTcThreads, tc_smem_bytes());
-  return n > 0 ? n : 1;
+cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s) {
+  for (int64_t j0 = 0; j0 < njobs; j0 += 65535) {
+    const int nb = static_cast<int>(njobs - j0 < 65535 ? njobs - j0 : 65535);
+    pack_tc_kernel<<<nb, 256, 0, s>>>(jobs + j0, src, static_cast<unsigned char *>(adata));
+  }
+  return cudaGetLastError();
 }
 
-// The V pass of this form takes its units from the ticket counter, so the
-// permutation re-arms it and the near/U pass uses the second counter slot.
-cudaError_t launch_matvec_tc(const DevPlan &p, const float *panels, const float *vdata, float *xt,
-                             int grid, cudaStream_t s, float *Y, int64_t ldy, int nr,
-                             cudaEvent_t ev_mid) {
+cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr,
+                             float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches) {
   tc_attrs();
+  int nl = 0;
+  int gp = static_cast<int>((p.x_len + 63) / 64);
+  if (gp > 2048) gp = 2048;
+  if (ev) cudaEventRecord(ev[0], s);
+  permute_split_kernel<<<gp, 256, 0, s>>>(X, ldx, nr, p.smap0, p.n, p.x_len, t.xts, p.counter + 2);
+  nl++;
+  if (ev) cudaEventRecord(ev[1], s);
+  TcArgs a{};
+  a.adata = static_cast<const unsigned char *>(t.adata);
+  a.colmap = t.colmap;
+  a.xts = t.xts;
+  a.xts_out = t.xts;
+  a.prow = t.prow;
+  a.tiles = p.tiles;
+  a.tmap0 = p.tmap0;
+  a.y = Y;
+  a.ldy = ldy;
+  a.nr = nr;
+  a.zero_row = static_cast<int32_t>(p.n);
+  a.status = p.status;
   const size_t smem = tc_smem_bytes();
-  if (!p.warp_begin_empty)
-    v_tc_kernel<<<grid, kTcThreads, smem, s>>>(vdata, p.vunits, p.nvunits, xt, p.counter, p.status);
-  if (ev_mid) cudaEventRecord(ev_mid, s);
-  DuTcArgs a{panels, p.tiles, p.tile_order, p.ntiles, p.segs, xt, p.tmap0, Y, ldy, nr,
-             p.counter + 1, p.status};
-  du_tc_kernel<<<grid, kTcThreads, smem, s>>>(a);
+  if (t.n_v > 0) {
+    a.items = t.v_items;
+    a.nitems = t.n_v;
+    a.ticket = p.counter + 2;
+    tc_kernel<<<t.ctas, kTcThreads, smem, s>>>(a);
+    nl++;
+    if (t.n_reduce > 0) {
+      reduce_split_kernel<<<t.n_reduce < 4096 ? t.n_reduce : 4096, 256, 0, s>>>(t.reduce, t.n_reduce, t.prow, t.xts);
+      nl++;
+    }
+  }
+  if (ev) cudaEventRecord(ev[2], s);
+  a.items = t.du_items;
+  a.nitems = t.n_du;
+  a.ticket = p.counter + 3;
+  tc_kernel<<<t.ctas, kTcThreads, smem, s>>>(a);
+  nl++;
+  if (ev) cudaEventRecord(ev[3], s);
+  if (launches) *launches = nl;
   return cudaGetLastError();
 }
 

@@ -31,6 +31,13 @@ def _cases():
     yield "sphere_yukawa", O.Kernel("yukawa", s.T, s.T), O.Tree(s.T, 16), O.Tree(s.T, 16), 1.0, 1e-5
     f = geometry.film(48, 40)
     yield "film_laplace", O.Kernel("laplace", f.T, f.T), O.Tree(f.T, 64), O.Tree(f.T, 64), 2.0, 1e-4
+    # leaves of up to 200 points: row tiles of more than 64 rows
+    b = geometry.cube(6000, seed=3)
+    yield "cube_bigleaf_laplace", O.Kernel("laplace", b.T, b.T), O.Tree(b.T, 200), O.Tree(b.T, 200), 1.5, 1e-5
+    # wide source groups: the multi-RHS V pass cuts them into column pieces
+    # whose partial products are summed afterwards
+    w = geometry.film(200, 160)
+    yield "film_wide_laplace", O.Kernel("laplace", w.T, w.T), O.Tree(w.T, 64), O.Tree(w.T, 64), 2.0, 1e-4
 
 
 CASES = {c[0]: c[1:] for c in _cases()}
