@@ -32,12 +32,15 @@ const HMGPU_MIXED = Int32(2)
 const KERNELS = Dict(:explicit => Int32(0), :laplace => Int32(1), :yukawa => Int32(2),
                      :log2d => Int32(3), :vector_r => Int32(4), :dipolar => Int32(5))
 
-struct Options
+struct Options            # hmgpu_options
     precision::Int32
     compensated::Int32
     keep_factors::Int32
     reserved::Int32
+    rank_model::Ptr{Cvoid} # const hmgpu_rank_model* (C_NULL: fixed ACA workspace)
 end
+Options(precision, compensated, keep_factors, reserved) =
+    Options(precision, compensated, keep_factors, reserved, C_NULL)
 
 struct KernelDesc
     kind::Int32
