@@ -8,9 +8,6 @@
 
 #include "hm_api.h"
 
-// From this many right-hand sides on, one multi-RHS pass (matrix read once,
-// compute bound) beats repeated single-RHS passes (matrix read per column).
-static constexpr int64_t kMultiRhsFrom = 3;
 
 namespace hm {
 
@@ -53,8 +50,6 @@ void HMatrix::dfree(void *p) {
   cudaFree(p);
 }
 
-int build_tc(HMatrix &H);
-
 template <typename V>
 static int upload(HMatrix &H, V **dst, const std::vector<V> &src) {
   int rc = H.dalloc(reinterpret_cast<void **>(dst), src.size() * sizeof(V));
@@ -64,11 +59,7 @@ static int upload(HMatrix &H, V **dst, const std::vector<V> &src) {
   return e == cudaSuccess ? HMGPU_OK : cuda_fail(e, "cudaMemcpy");
 }
 
-// Builds the product layout from the block set and the FP64 row-major factors
-// held on the device (d64: dense, u64/v64: low-rank; per-block offsets).
-int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
-                    const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
-                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen) {
+int setup_grids(HMatrix &H) {
   const bool f64 = H.opt.precision == HMGPU_F64;
   const bool comp = !f64 && (H.opt.compensated || H.opt.precision == HMGPU_MIXED);
   cudaDeviceProp prop;
@@ -77,44 +68,78 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   H.num_sms = prop.multiProcessorCount;
   H.grid_v = H.num_sms * occupancy_v(f64);
   H.grid_du = H.num_sms * occupancy_du(f64, comp);
-  const int vec = f64 ? 2 : 4;
-  make_plan(H.bs, vec, H.grid_v * (kThreads / 32), dense_src_off, u_src_off, H.plan);
+  return HMGPU_OK;
+}
+
+// Row units, V units and the static V split on the device (rebuilt by the autotuner).
+int upload_units(HMatrix &H) {
   const Plan &p = H.plan;
-  const size_t es = f64 ? 8 : 4;
+  H.dfree(H.dp.units);
+  H.dfree(H.dp.vunits);
+  H.dfree(H.dp.warp_begin);
   int rc;
-  if ((rc = H.dalloc(&H.panels, p.panel_len * es))) return rc;
-  if ((rc = H.dalloc(&H.vdata, p.v_len * es))) return rc;
-  if ((rc = H.dalloc(&H.xt, p.xt_len * es))) return rc;
-  cudaMemset(H.xt, 0, p.xt_len * es);
-  cudaMemset(H.vdata, 0, p.v_len * es);
-  if ((rc = upload(H, &H.dp.tiles, p.tiles))) return rc;
   if ((rc = upload(H, &H.dp.units, p.units))) return rc;
-  if ((rc = upload(H, &H.dp.tile_order, p.tile_order))) return rc;
-  if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
-  H.dp.nunits = static_cast<int32_t>(p.units.size());
-  H.dp.nvunits = static_cast<int32_t>(p.vunits.size());
   if ((rc = upload(H, &H.dp.vunits, p.vunits))) return rc;
   if ((rc = upload(H, &H.dp.warp_begin, p.warp_begin))) return rc;
-  std::vector<int32_t> t0(H.bs.m), s0(H.bs.n);
-  for (int64_t i = 0; i < H.bs.m; i++) t0[i] = static_cast<int32_t>(H.bs.tmap[i] - 1);
-  for (int64_t j = 0; j < H.bs.n; j++) s0[j] = static_cast<int32_t>(H.bs.smap[j] - 1);
-  if ((rc = upload(H, &H.dp.tmap0, t0))) return rc;
-  if ((rc = upload(H, &H.dp.smap0, s0))) return rc;
+  H.dp.nunits = static_cast<int32_t>(p.units.size());
+  H.dp.nvunits = static_cast<int32_t>(p.vunits.size());
+  H.dp.nwarps = p.nwarps;
+  H.dp.warp_begin_empty = p.vunits.empty();
+  return HMGPU_OK;
+}
+
+// Every table of H.plan, the index maps (tmap0: length m; smap0: the x region,
+// -1 for zero entries) and the ticket/status words; allocates XT.
+int upload_plan(HMatrix &H, const std::vector<int32_t> &tmap0, const std::vector<int32_t> &smap0,
+                int64_t zero_row) {
+  const Plan &p = H.plan;
+  const size_t es = H.opt.precision == HMGPU_F64 ? 8 : 4;
+  int rc;
+  if ((rc = H.dalloc(&H.xt, p.xt_len * es))) return rc;
+  cudaMemset(H.xt, 0, p.xt_len * es);
+  if ((rc = upload(H, &H.dp.tiles, p.tiles))) return rc;
+  if ((rc = upload(H, &H.dp.tile_order, p.tile_order))) return rc;
+  if ((rc = upload(H, &H.dp.segs, p.segs))) return rc;
+  if ((rc = upload_units(H))) return rc;
+  if ((rc = upload(H, &H.dp.tmap0, tmap0))) return rc;
+  if ((rc = upload(H, &H.dp.smap0, smap0))) return rc;
   if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.counter), 64))) return rc;
   cudaMemset(H.dp.counter, 0, 64);
   H.dp.status = H.dp.counter + 4;  // its own 16-byte slot of the same allocation
   H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
-  H.dp.nwarps = p.nwarps;
-  H.dp.warp_begin_empty = p.vunits.empty();
   if ((rc = upload(H, &H.dp.mv_items, p.mv_items))) return rc;
   if ((rc = upload(H, &H.dp.mv_reduce, p.mv_reduce))) return rc;
   H.dp.nmv = static_cast<int32_t>(p.mv_items.size());
   H.dp.nmvr = static_cast<int32_t>(p.mv_reduce.size());
   H.dp.p_rows = p.p_rows;
-  H.dp.m = H.bs.m;
-  H.dp.n = H.bs.n;
+  H.dp.m = static_cast<int64_t>(tmap0.size());
+  H.dp.n = static_cast<int64_t>(smap0.size());
+  H.dp.zero_row = zero_row;
   H.dp.x_len = p.x_len;
   H.dp.xt_len = p.xt_len;
+  return HMGPU_OK;
+}
+
+// Builds the product layout from the block set and the FP64 row-major factors
+// held on the device (d64: dense, u64/v64: low-rank; per-block offsets).
+int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
+                    const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
+                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen) {
+  const bool f64 = H.opt.precision == HMGPU_F64;
+  int rc;
+  if ((rc = setup_grids(H))) return rc;
+  const int vec = f64 ? 2 : 4;
+  make_plan(H.bs, vec, H.grid_v * (kThreads / 32), dense_src_off, u_src_off, H.plan);
+  const Plan &p = H.plan;
+  const size_t es = f64 ? 8 : 4;
+  if ((rc = H.dalloc(&H.panels, p.panel_len * es))) return rc;
+  if ((rc = H.dalloc(&H.vdata, p.v_len * es))) return rc;
+  cudaMemset(H.vdata, 0, p.v_len * es);
+  std::vector<int32_t> t0(H.bs.m), s0(H.bs.n);
+  for (int64_t i = 0; i < H.bs.m; i++) t0[i] = static_cast<int32_t>(H.bs.tmap[i] - 1);
+  for (int64_t j = 0; j < H.bs.n; j++) s0[j] = static_cast<int32_t>(H.bs.smap[j] - 1);
+  if ((rc = upload_plan(H, t0, s0, H.bs.n))) return rc;
+  cudaError_t e;
 
   // pack panels
   PackJob *djobs = nullptr;
@@ -391,7 +416,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
     *ev = H.prof_ev[H.prof_used++].data();
     return HMGPU_OK;
   };
-  if (nrhs >= kMultiRhsFrom) {
+  if (nrhs >= H.multi_from) {
     // several right-hand sides: one pass per rhs_per_pass() columns, the
     // matrix read once per pass (hm_multi.cu; hm_tc.cu for mixed precision)
     const int per = hm::rhs_per_pass();

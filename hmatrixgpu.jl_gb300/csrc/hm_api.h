@@ -33,6 +33,7 @@ struct HMatrix {
   // multi-right-hand-side scratch, allocated on first use
   void *xt_multi = nullptr, *p_multi = nullptr;
   int grid_du_multi = 0;
+  int multi_from = 3;  // right-hand sides from which one multi-RHS pass runs (autotuned)
   // tensor-core copy of the matrix (mixed precision)
   DevTc tc;
   int64_t tc_bytes = 0;
@@ -57,6 +58,11 @@ struct HMatrix {
 };
 
 int cuda_fail(cudaError_t e, const char *what);
+int setup_grids(HMatrix &H);
+int upload_units(HMatrix &H);
+int upload_plan(HMatrix &H, const std::vector<int32_t> &tmap0, const std::vector<int32_t> &smap0,
+                int64_t zero_row);
+int build_tc(HMatrix &H);
 // The 8 rank-predictor features of admissible block (x, y) at tolerance eps.
 void block_features(const Node &x, const Node &y, double eps, float *f);
 int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,

@@ -139,6 +139,13 @@ struct TcItem {
 };
 static_assert(sizeof(TcItem) == 32, "TcItem layout");
 
+// The V rows of one source group: rows [0, rows) of `stride` stored elements
+// at v_off, dotted with XT[x_off, x_off + stride), outputs at XT rows t_off...
+struct VGroup {
+  int64_t v_off;
+  int32_t stride, rows, x_off, t_off;
+};
+
 // Copy job of the packing pass: a row-major source slice -> rows of a tile panel.
 struct PackJob {
   int64_t src_off;   // element offset in the source array
@@ -162,12 +169,15 @@ struct Plan {
   std::vector<Seg> segs;
   int64_t panel_len = 0;
   std::vector<RowUnit> units;  // near/U pass work, largest first
+  int32_t unit_rows = 16;      // rows per unit (8 or 16)
   std::vector<int32_t> tile_order;  // tiles by decreasing columns
   std::vector<PackJob> pjobs;
   // V pass
   std::vector<int64_t> v_off, t_off;  // per low-rank block
   std::vector<int32_t> v_stride, v_phase;
+  std::vector<VGroup> vgroups;
   std::vector<VUnit> vunits;
+  int64_t vunit_bytes = 0;
   std::vector<int32_t> warp_begin;  // nwarps + 1
   int nwarps = 0;
   int64_t v_len = 0;
@@ -183,6 +193,19 @@ struct Plan {
 // row-major FP64 source factors (dense blocks: -1 when generated from a kernel).
 void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_t> &dense_src_off,
                const std::vector<int64_t> &u_src_off, Plan &p);
+
+// Near/U row units of `unit_rows` (<= 16) rows over p.tile_order, and the V
+// units of about `unit_bytes` with their static split over `nwarps` warps: both
+// only partition the stored layout, so they can be rebuilt at any time.
+void make_units(Plan &p, int32_t unit_rows);
+void make_vunits(Plan &p, int64_t unit_bytes, int nwarps);
+
+// Plan and block set of the block-diagonal batch of several H-matrices (see
+// hm_plan.cpp).
+int combine_plans(const std::vector<const Plan *> &plans, const std::vector<const BlockSet *> &sets,
+                  int nwarps, Plan &P, BlockSet &bs, std::vector<int32_t> &tmap0,
+                  std::vector<int32_t> &smap0, std::vector<int64_t> &panel_base,
+                  std::vector<int64_t> &v_base);
 
 // Tensor-core layout of a FP32 plan: V items (from the multi-RHS V items),
 // near/U items (row tiles, in pieces of at most 64 rows) and the column maps.

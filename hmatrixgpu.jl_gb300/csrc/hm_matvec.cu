@@ -97,7 +97,8 @@ struct RowAcc {
 };
 
 // ---------------------------------------------------------------------------
-// x permutation: XT[j] = x[smap[j]] for j < n, zero padding up to x_len.
+// x permutation: XT[j] = x[smap[j]] for j < n (zero where smap[j] < 0), zero
+// padding up to x_len.
 // Also re-arms the unit ticket of the near/U pass.
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -107,7 +108,7 @@ __global__ void permute_x_kernel(const T *__restrict__ x, const int32_t *__restr
   int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (j == 0) *counter = 0;
   for (; j < x_len; j += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    xt[j] = j < n ? x[smap0[j]] : T(0);
+    xt[j] = (j < n && smap0[j] >= 0) ? x[smap0[j]] : T(0);  // negative: padding between batch members
 }
 
 // ---------------------------------------------------------------------------

@@ -73,7 +73,7 @@ __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int n
     for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {
       const int r = e / 64, cc = e % 64;  // consecutive threads: consecutive c
       const int64_t c = c0 + cc;
-      tile[cc][r] = (c < n && r < nr) ? X[smap0[c] + r * ldx] : T(0);
+      tile[cc][r] = (c < n && r < nr && smap0[c] >= 0) ? X[smap0[c] + r * ldx] : T(0);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {

@@ -34,9 +34,59 @@ static constexpr int32_t kRowPad = 4;
 
 static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
+void make_units(Plan &p, int32_t unit_rows) {
+  p.units.clear();
+  p.unit_rows = unit_rows;
+  for (int32_t ti : p.tile_order) {
+    const TileDesc &d = p.tiles[ti];
+    const int32_t parts = (d.m + unit_rows - 1) / unit_rows;
+    for (int32_t q = 0; q < parts; q++) {
+      // near-equal row runs
+      int32_t i0 = static_cast<int32_t>(static_cast<int64_t>(d.m) * q / parts);
+      int32_t i1 = static_cast<int32_t>(static_cast<int64_t>(d.m) * (q + 1) / parts);
+      p.units.push_back(RowUnit{ti, i0, i1, 0});
+    }
+  }
+}
+
+void make_vunits(Plan &p, int64_t unit_bytes, int nwarps) {
+  const int esize = 16 / p.vec;
+  p.vunits.clear();
+  p.vunit_bytes = unit_bytes;
+  std::vector<int64_t> uweight;
+  for (const VGroup &g : p.vgroups) {
+    int32_t nv = g.stride / p.vec, lanes = 1;
+    while (lanes < nv && lanes < 32) lanes *= 2;
+    const int64_t row_bytes = static_cast<int64_t>(g.stride) * esize;
+    const int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, unit_bytes / row_bytes));
+    for (int32_t k0 = 0; k0 < g.rows; k0 += rows_per) {
+      VUnit u{};
+      u.v_off = g.v_off + static_cast<int64_t>(k0) * g.stride;
+      u.stride = g.stride;
+      u.nrows = std::min(rows_per, g.rows - k0);
+      u.x_off = g.x_off;
+      u.t_off = g.t_off + k0;
+      u.lanes = lanes;
+      p.vunits.push_back(u);
+      uweight.push_back(row_bytes * u.nrows + 256);
+    }
+  }
+  // static byte-balanced split of the V units over the resident warps
+  p.nwarps = std::max(1, nwarps);
+  p.warp_begin.assign(p.nwarps + 1, 0);
+  const int64_t total = std::accumulate(uweight.begin(), uweight.end(), int64_t(0));
+  int64_t acc = 0;
+  size_t u = 0;
+  for (int w = 0; w < p.nwarps; w++) {
+    p.warp_begin[w] = static_cast<int32_t>(u);
+    const int64_t goal = total * (w + 1) / p.nwarps;
+    while (u < uweight.size() && acc + uweight[u] / 2 <= goal) acc += uweight[u++];
+  }
+  p.warp_begin[p.nwarps] = static_cast<int32_t>(uweight.size());
+}
+
 void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_t> &dense_src_off,
                const std::vector<int64_t> &u_src_off, Plan &p) {
-  const int esize = 16 / vec;
   p = Plan();
   p.vec = vec;
   const int64_t m = bs.m, n = bs.n;
@@ -199,24 +249,13 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     return static_cast<int64_t>(p.tiles[a].ncols) > static_cast<int64_t>(p.tiles[b].ncols);
   });
   p.tile_order = order;
-  p.units.clear();
-  for (int32_t ti : order) {
-    const TileDesc &d = p.tiles[ti];
-    const int32_t parts = (d.m + kUnitRows - 1) / kUnitRows;
-    for (int32_t q = 0; q < parts; q++) {
-      // near-equal row runs
-      int32_t i0 = static_cast<int32_t>(static_cast<int64_t>(d.m) * q / parts);
-      int32_t i1 = static_cast<int32_t>(static_cast<int64_t>(d.m) * (q + 1) / parts);
-      p.units.push_back(RowUnit{ti, i0, i1, 0});
-    }
-  }
+  make_units(p, kUnitRows);
 
   // ---- V pass -----------------------------------------------------------------------
   p.v_off.assign(na, 0);
   p.v_stride.assign(na, 0);
   p.v_phase.assign(na, 0);
   int64_t voff = 0;
-  std::vector<int64_t> uweight;
   for (size_t gi = 0; gi + 1 < gstart.size(); gi++) {
     const int32_t a0 = gorder[gstart[gi]];
     const int32_t nb = bs.a_ce[a0] - bs.a_cs[a0];
@@ -233,11 +272,8 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
       rows += bs.a_r[a];
     }
     if (rows == 0) continue;
-    int32_t nv = stride / vec, lanes = 1;
-    while (lanes < nv && lanes < 32) lanes *= 2;
-    const int64_t row_bytes = static_cast<int64_t>(stride) * esize;
-    const int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, kVUnitBytes / row_bytes));
     const int64_t t0 = p.t_off[a0];  // the group's t entries are contiguous
+    p.vgroups.push_back(VGroup{gbase, stride, rows, bs.a_cs[a0] - ph, static_cast<int32_t>(t0)});
     // multi-RHS items: 128-row blocks, wide ones cut into column pieces
     for (int32_t k0 = 0; k0 < rows; k0 += kMVRows) {
       const int32_t nr = std::min(kMVRows, rows - k0);
@@ -261,35 +297,12 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
       }
       if (pieces > 1) p.p_rows += static_cast<int64_t>(pieces) * nr;
     }
-    for (int32_t k0 = 0; k0 < rows; k0 += rows_per) {
-      VUnit u{};
-      u.v_off = gbase + static_cast<int64_t>(k0) * stride;
-      u.stride = stride;
-      u.nrows = std::min(rows_per, rows - k0);
-      u.x_off = bs.a_cs[a0] - ph;
-      u.t_off = static_cast<int32_t>(t0 + k0);
-      u.lanes = lanes;
-      p.vunits.push_back(u);
-      uweight.push_back(row_bytes * u.nrows + 256);
-    }
   }
   p.v_len = round_up(std::max<int64_t>(voff, vec), vec);
   std::stable_sort(p.mv_items.begin(), p.mv_items.end(), [](const MVItem &a, const MVItem &b) {
     return static_cast<int64_t>(a.nrows) * a.ncols > static_cast<int64_t>(b.nrows) * b.ncols;
   });
-  p.nwarps = std::max(1, nwarps);
-  p.warp_begin.assign(p.nwarps + 1, 0);
-  {
-    int64_t total = std::accumulate(uweight.begin(), uweight.end(), int64_t(0));
-    int64_t acc = 0;
-    size_t u = 0;
-    for (int w = 0; w < p.nwarps; w++) {
-      p.warp_begin[w] = static_cast<int32_t>(u);
-      int64_t goal = total * (w + 1) / p.nwarps;
-      while (u < uweight.size() && acc + uweight[u] / 2 <= goal) acc += uweight[u++];
-    }
-    p.warp_begin[p.nwarps] = static_cast<int32_t>(uweight.size());
-  }
+  make_vunits(p, kVUnitBytes, nwarps);
 
   // ---- entry counts ------------------------------------------------------------------
   p.dense_entries = 0;
@@ -346,6 +359,137 @@ void make_tc_plan(const Plan &p, TcPlan &tp) {
     }
   }
   tp.bytes = std::max<int64_t>(off, 16);
+}
+
+// The plan and block set of diag(H_1, ..., H_k) from the members' (batch
+// members keep their own layouts; every index is shifted): XT = [x regions of
+// all members | t regions of all members], y and x concatenated in member
+// order. tmap0 / smap0: the device index maps (smap0 -1 on padding entries);
+// panel_base / v_base: where each member's panels and V rows go.
+int combine_plans(const std::vector<const Plan *> &plans, const std::vector<const BlockSet *> &sets,
+                  int nwarps, Plan &P, BlockSet &bs, std::vector<int32_t> &tmap0,
+                  std::vector<int32_t> &smap0, std::vector<int64_t> &panel_base,
+                  std::vector<int64_t> &v_base) {
+  P = Plan();
+  bs = BlockSet();
+  // ---- offsets of every member ------------------------------------------------------
+  const int32_t count = static_cast<int32_t>(plans.size());
+  std::vector<int64_t> row_base(count), col_base(count), x_base(count), t_base(count), p_base(count);
+  std::vector<int32_t> seg_base(count);
+  panel_base.assign(count, 0);
+  v_base.assign(count, 0);
+  int64_t rows = 0, cols = 0, X = 0, R = 0, pan = 0, vl = 0, pr = 0;
+  int32_t ns = 0;
+  for (int32_t k = 0; k < count; k++) {
+    const Plan &q = *plans[k];
+    row_base[k] = rows;
+    col_base[k] = cols;
+    x_base[k] = X;
+    t_base[k] = R;
+    panel_base[k] = pan;
+    v_base[k] = vl;
+    p_base[k] = pr;
+    seg_base[k] = ns;
+    rows += sets[k]->m;
+    cols += sets[k]->n;
+    X += q.x_len;
+    R += q.R;
+    pan += q.panel_len;
+    vl += q.v_len;
+    pr += q.p_rows;
+    ns += static_cast<int32_t>(q.segs.size());
+  }
+  if (rows >= (int64_t(1) << 31) || cols >= (int64_t(1) << 31) || X + R >= (int64_t(1) << 31))
+    return fail(HMGPU_ERR_INVALID, "batch too large for 32-bit row indices");
+  const int64_t T0 = X;
+
+  P.vec = plans[0]->vec;
+  P.x_len = X;
+  P.R = R;
+  P.xt_len = round_up(T0 + R, P.vec);
+  P.panel_len = std::max<int64_t>(pan, P.vec);
+  P.v_len = std::max<int64_t>(vl, P.vec);
+  P.p_rows = pr;
+  bs.m = rows;
+  bs.n = cols;
+  for (int32_t k = 0; k < count; k++) {
+    const Plan &q = *plans[k];
+    const BlockSet &mb = *sets[k];
+    const int64_t xl = q.x_len;
+    auto f = [&](int64_t v) { return v < xl ? x_base[k] + v : T0 + t_base[k] + (v - xl); };
+    for (TileDesc d : q.tiles) {
+      d.data_off += panel_base[k];
+      d.row0 += static_cast<int32_t>(row_base[k]);
+      d.seg0 += seg_base[k];
+      P.tiles.push_back(d);
+    }
+    for (Seg g : q.segs) {
+      g.vec_off = static_cast<int32_t>(f(g.vec_off));
+      P.segs.push_back(g);
+    }
+    for (VGroup g : q.vgroups) {
+      g.v_off += v_base[k];
+      g.x_off += static_cast<int32_t>(x_base[k]);
+      g.t_off = static_cast<int32_t>(f(g.t_off));
+      P.vgroups.push_back(g);
+    }
+    for (MVItem it : q.mv_items) {
+      it.v_off += v_base[k];
+      it.x_off += static_cast<int32_t>(x_base[k]);
+      it.out = static_cast<int32_t>(it.kind == 0 ? f(it.out) : it.out + p_base[k]);
+      P.mv_items.push_back(it);
+    }
+    for (MVReduce r : q.mv_reduce) {
+      r.t_row = static_cast<int32_t>(f(r.t_row));
+      r.p_row += static_cast<int32_t>(p_base[k]);
+      P.mv_reduce.push_back(r);
+    }
+    P.dense_entries += q.dense_entries;
+    P.far_entries += q.far_entries;
+    // block set (permuted index space, 1-based maps) for the queries
+    for (int64_t i = 0; i < mb.m; i++) bs.tmap.push_back(mb.tmap[i] + row_base[k]);
+    for (int64_t j = 0; j < mb.n; j++) bs.smap.push_back(mb.smap[j] + col_base[k]);
+    const int32_t rb = static_cast<int32_t>(row_base[k]), cb = static_cast<int32_t>(col_base[k]);
+    for (size_t b = 0; b < mb.d_rs.size(); b++) {
+      bs.d_rs.push_back(mb.d_rs[b] + rb);
+      bs.d_re.push_back(mb.d_re[b] + rb);
+      bs.d_cs.push_back(mb.d_cs[b] + cb);
+      bs.d_ce.push_back(mb.d_ce[b] + cb);
+    }
+    for (size_t b = 0; b < mb.a_rs.size(); b++) {
+      bs.a_rs.push_back(mb.a_rs[b] + rb);
+      bs.a_re.push_back(mb.a_re[b] + rb);
+      bs.a_cs.push_back(mb.a_cs[b] + cb);
+      bs.a_ce.push_back(mb.a_ce[b] + cb);
+      bs.a_r.push_back(mb.a_r[b]);
+    }
+    bs.aca_rank.insert(bs.aca_rank.end(), mb.aca_rank.begin(), mb.aca_rank.end());
+    bs.final_rank.insert(bs.final_rank.end(), mb.final_rank.begin(), mb.final_rank.end());
+  }
+  // work lists over the whole batch: tiles with more columns first, largest
+  // multi-RHS V items first, V units split over the resident warps
+  P.tile_order.resize(P.tiles.size());
+  std::iota(P.tile_order.begin(), P.tile_order.end(), 0);
+  std::stable_sort(P.tile_order.begin(), P.tile_order.end(),
+                   [&](int32_t a, int32_t b) { return P.tiles[a].ncols > P.tiles[b].ncols; });
+  make_units(P, plans[0]->unit_rows);
+  make_vunits(P, plans[0]->vunit_bytes, nwarps);
+  std::stable_sort(P.mv_items.begin(), P.mv_items.end(), [](const MVItem &a, const MVItem &b) {
+    return static_cast<int64_t>(a.nrows) * a.ncols > static_cast<int64_t>(b.nrows) * b.ncols;
+  });
+
+  // index maps: y of member k at rows row_base[k].., x at col_base[k]..
+  tmap0.assign(rows, 0);
+  smap0.assign(X, -1);
+  for (int32_t k = 0; k < count; k++) {
+    const BlockSet &mb = *sets[k];
+    for (int64_t i = 0; i < mb.m; i++)
+      tmap0[row_base[k] + i] = static_cast<int32_t>(mb.tmap[i] - 1 + row_base[k]);
+    for (int64_t j = 0; j < mb.n; j++)
+      smap0[x_base[k] + j] = static_cast<int32_t>(mb.smap[j] - 1 + col_base[k]);
+  }
+
+  return HMGPU_OK;
 }
 
 }  // namespace hm

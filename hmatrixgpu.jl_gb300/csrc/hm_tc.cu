@@ -438,7 +438,7 @@ __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, i
     for (int e = threadIdx.x; e < 64 * kTcRhs; e += blockDim.x) {
       const int r = e / 64, cc = e % 64;  // consecutive threads: consecutive c
       const int64_t c = c0 + cc;
-      tile[cc][r] = (c < n && r < nr) ? X[smap0[c] + r * ldx] : 0.0f;
+      tile[cc][r] = (c < n && r < nr && smap0[c] >= 0) ? X[smap0[c] + r * ldx] : 0.0f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * 4; e += blockDim.x) {
@@ -547,7 +547,7 @@ cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, i
   a.y = Y;
   a.ldy = ldy;
   a.nr = nr;
-  a.zero_row = static_cast<int32_t>(p.n);
+  a.zero_row = static_cast<int32_t>(p.zero_row);
   a.status = p.status;
   const size_t smem = tc_smem_bytes();
   if (t.n_v > 0) {

@@ -25,7 +25,7 @@ from ._lib import (F64, F32, MIXED, PRECISIONS, KERNEL_IDS, HMGPUError, Info, Ke
 from . import _build
 
 __all__ = ["ClusterTree", "BlockTree", "ACA_plus", "SVD_recompress", "HMatrix", "Kernel", "info",
-           "traverse", "mul_", "HMGPUError", "build", "RankModel", "block_features"]
+           "traverse", "mul_", "HMGPUError", "build", "RankModel", "block_features", "batch", "Graph"]
 
 
 def build(verbose=False):
@@ -407,6 +407,14 @@ class HMatrix:
         check(lib().hmgpu_hmatrix_aca_ranks(self._h, ptr(a, I64P), ptr(f, I64P)))
         return a, f
 
+    def autotune(self, cache_path=None):
+        """Times the product's free parameters on this H-matrix and keeps the
+        fastest (hmgpu_hmatrix_autotune); results are bitwise unchanged."""
+        r = (C.c_int32 * 4)()
+        path = None if cache_path is None else str(cache_path).encode()
+        check(lib().hmgpu_hmatrix_autotune(self._h, path, r))
+        return {"unit_rows": r[0], "vunit_kib": r[1], "multi_rhs_from": r[2], "from_cache": bool(r[3])}
+
     def status(self):
         """Device error word of the products so far (0 = clean; synchronises the
         device). Non-zero values name the bounded wait that ran out."""
@@ -447,6 +455,46 @@ class HMatrix:
 
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
+
+
+def batch(members):
+    """The block-diagonal H-matrix diag(H_1, ..., H_k) of several H-matrices
+    (hmgpu_hmatrix_batch): one product runs every member in the same kernel
+    launches; x and y are the members' vectors concatenated."""
+    hs = (C.c_void_p * len(members))(*[H._h for H in members])
+    h = C.c_void_p()
+    check(lib().hmgpu_hmatrix_batch(hs, len(members), C.byref(h)))
+    return HMatrix(None, None, None, _handle=h)
+
+
+class Graph:
+    """mul!(y, H, x) captured into a CUDA graph (hmgpu_graph_create) for torch
+    CUDA tensors x and y; launch() replays it on the current torch stream."""
+
+    def __init__(self, H, x, y):
+        import torch
+        nrhs = 1 if x.dim() == 1 else x.shape[1]
+        ldx = x.stride(1) if x.dim() == 2 else x.shape[0]
+        ldy = y.stride(1) if y.dim() == 2 else y.shape[0]
+        self.H, self.x, self.y = H, x, y  # the graph holds their device pointers
+        g = C.c_void_p()
+        with torch.cuda.device(x.device):
+            check(lib().hmgpu_graph_create(H._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                           nrhs, ldx, ldy, C.byref(g)))
+        self._g = g
+
+    def launch(self, stream=None):
+        import torch
+        if stream is None:
+            stream = torch.cuda.current_stream(self.x.device).cuda_stream
+        check(lib().hmgpu_graph_launch(self._g, C.c_void_p(stream)))
+        return self.y
+
+    def __del__(self):
+        g = getattr(self, "_g", None)
+        if g:
+            lib().hmgpu_graph_free(g)
+            self._g = None
 
 
 def mul_(y, H, x, stream=None):

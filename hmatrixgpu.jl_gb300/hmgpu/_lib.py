@@ -93,6 +93,11 @@ SIGNATURES = {
     "hmgpu_rank_model_params": (C.c_int, [VP, F32P, F32P, F32P, F32P]),
     "hmgpu_rank_model_free": (C.c_int, [VP]),
     "hmgpu_block_features": (C.c_int, [VP, VP, C.c_double, C.c_double, F32P, I64P]),
+    "hmgpu_hmatrix_batch": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
+    "hmgpu_graph_create": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64, C.POINTER(VP)]),
+    "hmgpu_graph_launch": (C.c_int, [VP, VP]),
+    "hmgpu_graph_free": (C.c_int, [VP]),
+    "hmgpu_hmatrix_autotune": (C.c_int, [VP, C.c_char_p, C.POINTER(C.c_int32)]),
 }
 
 

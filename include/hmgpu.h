@@ -253,6 +253,37 @@ int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const
 /* 8 -> 64 -> 64 -> 1 ReLU MLP in FP32 mapping block features to the rank    */
 /* plain ACA+ reaches, trained and evaluated by the library's own kernels.   */
 /* Used only to size and batch ACA work; results never depend on it.         */
+/* ---- batches, CUDA graphs, autotuning (no counterpart in the reference) -- */
+/* One H-matrix made of `count` members: the block-diagonal operator
+ * diag(H_1, ..., H_count), of size (sum m_k) x (sum n_k). Its products take
+ * x = [x_1; x_2; ...] (member k's entries at offset sum_{j<k} n_j) and write
+ * y = [y_1; y_2; ...], and run all members in the same kernel launches. The
+ * members must live on the current device and share precision and
+ * compensation; their device data is copied, so they stay usable and may be
+ * freed. Products of the batch equal the members' own products bit for bit. */
+int hmgpu_hmatrix_batch(hmgpu_hmatrix *const *members, int32_t count, hmgpu_hmatrix **out);
+
+/* hmgpu_matvec(H, x, y, nrhs, ldx, ldy) captured once into a CUDA graph and
+ * replayed by hmgpu_graph_launch on any stream (x and y are fixed device
+ * pointers; their contents may change between launches). Creation runs the
+ * product once, uncaptured, to allocate its scratch. H must outlive the
+ * graph, and replays of graphs of the same H must not overlap. */
+typedef struct hmgpu_graph hmgpu_graph;
+int hmgpu_graph_create(hmgpu_hmatrix *H, const void *x, void *y, int64_t nrhs, int64_t ldx,
+                       int64_t ldy, hmgpu_graph **out);
+int hmgpu_graph_launch(hmgpu_graph *G, void *stream);
+int hmgpu_graph_free(hmgpu_graph *G);
+
+/* Times the product's free parameters on H's own data (about a second of
+ * products) and keeps the fastest: rows per near/U unit (8 or 16), bytes per
+ * V unit (32, 64 or 128 KiB) and the number of right-hand sides from which one
+ * multi-RHS pass replaces repeated single-RHS products. None of them changes
+ * any result. With `cache_path` (a text file; NULL for none) the choice is
+ * looked up first and stored after, keyed by the H-matrix's structure and the
+ * device. result (optional, 4 values): unit rows, V unit KiB, multi-RHS
+ * threshold (1 << 30: never), 1 if it came from the cache. */
+int hmgpu_hmatrix_autotune(hmgpu_hmatrix *H, const char *cache_path, int32_t *result);
+
 /* ---------------------------------------------------------------------- */
 #define HMGPU_RANK_MODEL_PARAMS 4801
 #define HMGPU_RANK_FEATURES 8
