@@ -116,6 +116,64 @@ def set_grid(g):
         WORKLOAD = WORKLOAD.replace("film-2^20", f"film-{g}x{g}")
 
 
+def batch_measurement(dev, steps):
+    """32 independent H-matrices (unit-sphere surfaces, N log-uniform in
+    [8192, 131072], Yukawa exp(-r)/r, leaf 32, eta 1.5, tol 1e-5, FP32), one
+    product each: one product per member in turn, the block-diagonal batch
+    (one launch per kernel for all members) and the batch replayed from a CUDA
+    graph. Returns the per-product figures."""
+    import torch
+
+    import hmgpu
+    from tests import geometry
+    rng = np.random.default_rng(3)
+    sizes = np.exp(rng.uniform(np.log(8192), np.log(131072), 32)).astype(int)
+    t0 = time.time()
+    members = []
+    for i, N in enumerate(sizes):
+        P = geometry.sphere(int(N), seed=100 + i)
+        T = hmgpu.ClusterTree(P, max_points_per_leaf=32)
+        members.append(hmgpu.HMatrix(hmgpu.Kernel("yukawa", P), T, T, eta=1.5, eps=1e-5, precision="f32"))
+    B = hmgpu.batch(members)
+    build = time.time() - t0
+    m, n = B.shape
+    x = torch.randn(n, device=dev, generator=torch.Generator(dev).manual_seed(5))
+    y = torch.empty(m, device=dev)
+    offs = np.concatenate([[0], np.cumsum([H.shape[1] for H in members])])
+    xs = [x[offs[k]:offs[k + 1]] for k in range(len(members))]
+    ys = [y[offs[k]:offs[k + 1]] for k in range(len(members))]
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        s.record(stream)
+        for _ in range(reps):
+            fn()
+        e.record(stream)
+        torch.cuda.synchronize()
+        return s.elapsed_time(e) / reps
+
+    reps = max(20, min(steps, 200))
+    t_each = timed(lambda: [hmgpu.mul_(ys[k], members[k], xs[k]) for k in range(len(members))], reps)
+    y_each = y.clone()
+    t_batch = timed(lambda: hmgpu.mul_(y, B, x), reps)
+    same = bool(torch.equal(y, y_each))
+    G = hmgpu.Graph(B, x, y)
+    t_graph = timed(lambda: G.launch(), reps)
+    inf = B.info()
+    byts = 4 * (inf["dense_entries"] + inf["far_entries"]) + 4 * (2 * n + 2 * inf["total_rank"])
+    return {"workload": "32 sphere H-matrices, N log-uniform in [8192, 131072] (total %d), Yukawa, "
+                        "leaf 32, eta 1.5, tol 1e-5, FP32, 1 RHS each" % int(sizes.sum()),
+            "ms_members_one_by_one": t_each, "ms_batch": t_batch, "ms_batch_cuda_graph": t_graph,
+            "products_per_s_batch_graph": 32e3 / t_graph,
+            "speedup_batch_graph_vs_one_by_one": t_each / t_graph,
+            "batch_equals_members_bitwise": same, "algorithmic_gbs_batch_graph": byts / (t_graph * 1e-3) / 1e9,
+            "build_seconds": build}
+
+
 def cpu_sample(threads, target_s=15.0):
     """Times the oracle's restatement of the reference CPU mul! (src/mult.jl:6-32)
     on every SAMPLE_STRIDE-th block of the workload's matrix; returns products/s
@@ -184,6 +242,7 @@ def run_gpu(args):
     y = torch.empty(n, device=dev)
     stream = torch.cuda.current_stream(dev)
 
+    tune = H.autotune()  # unit sizes and the multi-RHS threshold, timed on this matrix
     for _ in range(max(args.warmup, 3)):
         hmgpu.mul_(y, H, x)
     torch.cuda.synchronize()
@@ -279,6 +338,7 @@ def run_gpu(args):
     du_bytes = (inf["dense_entries"] + u_entries) * es + es * (2 * n + R)
     du_ms = ph[2]
     achieved = du_bytes / (du_ms * 1e-3) / 1e9
+    batch32 = None if args.skip_batch else batch_measurement(dev, args.steps)
     cpu_v, cpu_d = cpu_sample(1, target_s=12.0)
     value = world * 1e3 / ms
     line = {
@@ -287,7 +347,7 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded film points, x ~ N(0,1))",
         "config": {"workload": WORKLOAD, "N": n, "leaf": LEAF, "eta": ETA, "tol": TOL,
-                   "precision": "f32", "nrhs": 1,
+                   "precision": "f32", "nrhs": 1, "autotuned": tune,
                    "l2": f"inputs larger than L2: {inf['matrix_bytes'] / 1e9:.1f} GB of factors streamed per step",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
         "hbm_gbs": alg_bytes / (ms * 1e-3) / 1e9,
@@ -310,6 +370,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": n * es},
         "gpu_launches": int(nl.value),
         "rhs32": rhs32,
+        "batch32": batch32,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -325,6 +386,7 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--grid", type=int, default=1024, help="film side (1024 = the headline workload)")
     ap.add_argument("--skip-rhs32", action="store_true", help="leave out the 32-RHS plain / mixed lines")
+    ap.add_argument("--skip-batch", action="store_true", help="leave out the 32-H-matrix batch lines")
     args = ap.parse_args()
     set_grid(args.grid)
     if args.impl == "reference":
