@@ -167,8 +167,10 @@ __global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ 
 // counter, tiles with the most columns first. The CTA gathers the tile's
 // vector entries (x for dense columns, t for rank columns) into shared memory
 // once per unit; then each warp streams one or two whole rows of the tile's
-// row-major panel with 16-byte loads against 16-byte shared-memory loads of
-// the entries, and reduces across lanes with a fixed butterfly.
+// row-major panel with 16-byte loads (up to 8 in flight per lane) against
+// 16-byte shared-memory loads of the entries, and reduces across lanes with a
+// fixed butterfly. Every lane adds its vectors in increasing column order in
+// every loop form, so a row's sum does not depend on the unit it is in.
 // ---------------------------------------------------------------------------
 template <typename T>
 struct DuArgs {
@@ -189,8 +191,11 @@ struct DuCols {
 };
 constexpr int kDuSegs = 512;
 
+// Six CTAs per SM (40 registers, a few spilled to L1) keep more rows, and so
+// more 16-byte loads, in flight than five CTAs without spills: the pass is
+// bound by memory latency, not by the instructions the spills add.
 template <typename T, bool COMP>
-__global__ void __launch_bounds__(kThreads) du_rows_kernel(DuArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, 6) du_rows_kernel(DuArgs<T> a) {
   using VT = typename Vec16<T>::type;
   constexpr int VEC = Vec16<T>::N;
   constexpr int CH = DuCols<T>::value;
@@ -238,6 +243,21 @@ __global__ void __launch_bounds__(kThreads) du_rows_kernel(DuArgs<T> a) {
       const VT *RB = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ib) * d.ld + c0);
       if (ha && hb) {
         int p = lane;
+        for (; p + 96 < nv; p += 128) {
+          const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
+          const VT x2 = ld_stream(RA + p + 64), x3 = ld_stream(RA + p + 96);
+          const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
+          const VT z2 = ld_stream(RB + p + 64), z3 = ld_stream(RB + p + 96);
+          const VT e0 = E[p], e1 = E[p + 32], e2 = E[p + 64], e3 = E[p + 96];
+          ra.add(x0, e0);
+          ra.add(x1, e1);
+          ra.add(x2, e2);
+          ra.add(x3, e3);
+          rb.add(z0, e0);
+          rb.add(z1, e1);
+          rb.add(z2, e2);
+          rb.add(z3, e3);
+        }
         for (; p + 32 < nv; p += 64) {
           const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
           const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
