@@ -139,18 +139,23 @@ struct TcSmem {
 
 // Waits for the phase of `bar` with parity `parity`; false when the abort flag
 // is up or the time limit ran out (then the flag goes up and `code` is recorded).
+__device__ __forceinline__ bool try_bar(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ bool wait_bar(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
                                          int code) {
+  if (try_bar(bar, parity)) return true;  // the common case reads no timer
   const unsigned long long t0 = now_ns();
   for (;;) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(su32(bar)), "r"(parity)
-        : "memory");
-    if (ok) return true;
+    if (try_bar(bar, parity)) return true;
     if (S.abort) return false;
     if (now_ns() - t0 > kWaitNs) {
       atomicCAS(status, 0, code);
@@ -334,25 +339,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
       if (!wait_bar_warp(S, &S.acc_empty[ab], static_cast<uint32_t>((n >> 1) & 1) ^ 1u, a.status, 23)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t acc = S.tmem + ab * kBN;
-      for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
-        const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
-        if (!wait_bar_warp(S, &S.full[s], static_cast<uint32_t>((g / kStages) & 1), a.status, 24)) {
+      // two chunks per turn where the item has them: one round of waits,
+      // descriptors and hand-offs per 128 columns
+      for (int c0 = 0; c0 < npad;) {
+        const int two = c0 + kKc < npad ? 2 : 1;
+        int s2[2], kc2[2];
+        bool ok = true;
+        for (int h = 0; h < two; h++) {
+          kc2[h] = min(kKc, npad - c0 - h * kKc);
+          s2[h] = static_cast<int>((g + h) % kStages);
+          ok = ok && wait_bar_warp(S, &S.full[s2[h]], static_cast<uint32_t>(((g + h) / kStages) & 1), a.status, 24);
+        }
+        if (!ok) {
           stop = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t asbo = static_cast<uint32_t>(kc) * 16;
-        const uint64_t da = sdesc(su32(S.a[s]), 128, asbo);
-        const uint64_t db = sdesc(su32(S.b[s]), kBGroupK, kBGroupN);
         if (elect_one()) {
-          for (int ks = 0; ks < kc / 16; ks++) {
-            // the start address field counts 16-byte units
-            const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4, ob = static_cast<uint64_t>(ks * 2 * kBGroupK) >> 4;
-            mma(acc, da + oa, db + ob, (c0 | ks) ? 1u : 0u);
+          for (int h = 0; h < two; h++) {
+            const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
+            const uint64_t db = sdesc(su32(S.b[s2[h]]), kBGroupK, kBGroupN);
+            for (int ks = 0; ks < kc2[h] / 16; ks++) {
+              // the start address field counts 16-byte units
+              const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4, ob = static_cast<uint64_t>(ks * 2 * kBGroupK) >> 4;
+              mma(acc, da + oa, db + ob, ((c0 + h * kKc) | ks) ? 1u : 0u);
+            }
+            commit(&S.empty[s2[h]]);
           }
-          commit(&S.empty[s]);
         }
         __syncwarp();
+        g += two;
+        c0 += two * kKc;
       }
       if (stop) break;
       if (elect_one()) commit(&S.acc_full[ab]);

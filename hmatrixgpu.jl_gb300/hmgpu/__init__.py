@@ -407,6 +407,17 @@ class HMatrix:
         check(lib().hmgpu_hmatrix_aca_ranks(self._h, ptr(a, I64P), ptr(f, I64P)))
         return a, f
 
+    def save(self, path):
+        """Writes the assembled H-matrix to `path` (hmgpu_hmatrix_save)."""
+        check(lib().hmgpu_hmatrix_save(self._h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path):
+        """An H-matrix saved by save(), on the current device, without assembly."""
+        h = C.c_void_p()
+        check(lib().hmgpu_hmatrix_load(str(path).encode(), C.byref(h)))
+        return cls(None, None, None, _handle=h)
+
     def autotune(self, cache_path=None):
         """Times the product's free parameters on this H-matrix and keeps the
         fastest (hmgpu_hmatrix_autotune); results are bitwise unchanged."""

@@ -284,6 +284,14 @@ int hmgpu_graph_free(hmgpu_graph *G);
  * threshold (1 << 30: never), 1 if it came from the cache. */
 int hmgpu_hmatrix_autotune(hmgpu_hmatrix *H, const char *cache_path, int32_t *result);
 
+/* An assembled H-matrix on disk (no counterpart in the reference; the
+ * reference's flattened HMatrix has no file form): the device layout, index
+ * maps and block set as they are, with a checksum, so that a load needs no
+ * assembly. load validates every table against the data sizes before anything
+ * reaches the device and places the matrix on the current device. */
+int hmgpu_hmatrix_save(const hmgpu_hmatrix *H, const char *path);
+int hmgpu_hmatrix_load(const char *path, hmgpu_hmatrix **out);
+
 /* ---------------------------------------------------------------------- */
 #define HMGPU_RANK_MODEL_PARAMS 4801
 #define HMGPU_RANK_FEATURES 8
