@@ -518,6 +518,28 @@ __global__ void gen_dense_kernel(KDev K, const int32_t *__restrict__ tmap0,
   }
 }
 
+// sparsify_hmatrix: block j's entries K[tmap[row0 + i], smap[col0 + c]] at
+// out[off + i n + c] (row by row, as the reference pushes them); a warp per block.
+struct SpJob {
+  int32_t row0, m, col0, n;
+  int64_t off;
+};
+
+__global__ void sparsify_kernel(KDev K, const int32_t *__restrict__ tmap0, const int32_t *__restrict__ smap0,
+                                const SpJob *__restrict__ jobs, int64_t njobs, double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t wi = w0; wi < njobs; wi += nw) {
+    const SpJob j = jobs[wi];
+    for (int i = 0; i < j.m; i++) {
+      const int64_t ti = tmap0[j.row0 + i];
+      double *dst = out + j.off + static_cast<int64_t>(i) * j.n;
+      for (int c = lane; c < j.n; c += 32) dst[c] = kentry(K, ti, smap0[j.col0 + c]);
+    }
+  }
+}
+
 struct KernelGen : DenseGenerator {
   KDev K;
   int generate(HMatrix &H, const PackJob *djobs, int64_t njobs) override {
@@ -655,29 +677,8 @@ static int upload_coords(const double *src, int64_t npts, DevBuf &dst) {
   return e == cudaSuccess ? HMGPU_OK : cuda_fail(e, "copying coordinates");
 }
 
-}  // namespace hm
-
-using namespace hm;
-
-// ---------------------------------------------------------------------------
-// HMatrix(K, X, Y; eta, eps, svd_recompress) on the device
-// ---------------------------------------------------------------------------
-extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel *kd,
-                                   const hmgpu_tree *Xh, const hmgpu_tree *Yh, double eta,
-                                   double eps, int svd_recompress, hmgpu_hmatrix **out) {
-  auto t0 = std::chrono::steady_clock::now();
-  if (!kd || !Xh || !Yh || !out) return fail(HMGPU_ERR_INVALID, "NULL argument");
-  *out = nullptr;
-  const Tree &X = Xh->t;
-  const Tree &Y = Yh->t;
-  hmgpu_options o{HMGPU_F32, 0, 0, 0};
-  if (opt) o = *opt;
-  if (o.precision != HMGPU_F64 && o.precision != HMGPU_F32 && o.precision != HMGPU_MIXED)
-    return fail(HMGPU_ERR_INVALID, "unknown precision mode");
-  if (!(eps >= 0.0)) return fail(HMGPU_ERR_INVALID, "eps must be >= 0");
-  const int64_t m = static_cast<int64_t>(X.index_map.size()), n = static_cast<int64_t>(Y.index_map.size());
-  if (m >= (int64_t(1) << 31) || n >= (int64_t(1) << 31)) return fail(HMGPU_ERR_INVALID, "too many rows or columns");
-  // size(K) must match the trees (the reference indexes K through the trees' maps)
+// size(K) must match the trees (the reference indexes K through the trees' maps).
+static int check_kernel(const hmgpu_kernel *kd, int64_t m, int64_t n) {
   int64_t km = 0, kn = 0;
   switch (kd->kind) {
     case HMGPU_KERNEL_EXPLICIT:
@@ -708,6 +709,49 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
                                        std::to_string(n) + ")");
   if (kd->kind != HMGPU_KERNEL_EXPLICIT && (!kd->X || !kd->Y))
     return fail(HMGPU_ERR_INVALID, "kernel points are NULL");
+  return HMGPU_OK;
+}
+
+// The kernel's points (or explicit matrix) on the device.
+static int upload_kernel(const hmgpu_kernel *kd, int64_t n, DevBuf &dX, DevBuf &dY, DevBuf &dA, KDev &K) {
+  K = KDev{kd->kind, nullptr, nullptr, nullptr, kd->lda};
+  int rc;
+  if (kd->kind == HMGPU_KERNEL_EXPLICIT) {
+    if ((rc = dA.alloc(static_cast<size_t>(kd->lda) * n * sizeof(double)))) return rc;
+    cudaError_t e = cudaMemcpy(dA.p, kd->A, kd->lda * n * sizeof(double), cudaMemcpyDefault);
+    if (e != cudaSuccess) return cuda_fail(e, "copying the explicit matrix");
+    K.A = dA.as<double>();
+  } else {
+    if ((rc = upload_coords(kd->X, kd->nX, dX)) || (rc = upload_coords(kd->Y, kd->nY, dY))) return rc;
+    K.X = dX.as<double>();
+    K.Y = dY.as<double>();
+  }
+  return HMGPU_OK;
+}
+
+}  // namespace hm
+
+using namespace hm;
+
+// ---------------------------------------------------------------------------
+// HMatrix(K, X, Y; eta, eps, svd_recompress) on the device
+// ---------------------------------------------------------------------------
+extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel *kd,
+                                   const hmgpu_tree *Xh, const hmgpu_tree *Yh, double eta,
+                                   double eps, int svd_recompress, hmgpu_hmatrix **out) {
+  auto t0 = std::chrono::steady_clock::now();
+  if (!kd || !Xh || !Yh || !out) return fail(HMGPU_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  const Tree &X = Xh->t;
+  const Tree &Y = Yh->t;
+  hmgpu_options o{HMGPU_F32, 0, 0, 0};
+  if (opt) o = *opt;
+  if (o.precision != HMGPU_F64 && o.precision != HMGPU_F32 && o.precision != HMGPU_MIXED)
+    return fail(HMGPU_ERR_INVALID, "unknown precision mode");
+  if (!(eps >= 0.0)) return fail(HMGPU_ERR_INVALID, "eps must be >= 0");
+  const int64_t m = static_cast<int64_t>(X.index_map.size()), n = static_cast<int64_t>(Y.index_map.size());
+  if (m >= (int64_t(1) << 31) || n >= (int64_t(1) << 31)) return fail(HMGPU_ERR_INVALID, "too many rows or columns");
+  if (int rc = check_kernel(kd, m, n)) return rc;
 
   auto Hp = std::make_unique<HMatrix>();
   HMatrix &H = *Hp;
@@ -727,18 +771,9 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
 
   // device copies of the geometry and the maps
   DevBuf dX, dY, dA, dt, ds;
-  KDev K{kd->kind, nullptr, nullptr, nullptr, kd->lda};
+  KDev K;
   int rc;
-  if (kd->kind == HMGPU_KERNEL_EXPLICIT) {
-    if ((rc = dA.alloc(static_cast<size_t>(kd->lda) * n * sizeof(double)))) return rc;
-    cudaError_t e = cudaMemcpy(dA.p, kd->A, kd->lda * n * sizeof(double), cudaMemcpyDefault);
-    if (e != cudaSuccess) return cuda_fail(e, "copying the explicit matrix");
-    K.A = dA.as<double>();
-  } else {
-    if ((rc = upload_coords(kd->X, kd->nX, dX)) || (rc = upload_coords(kd->Y, kd->nY, dY))) return rc;
-    K.X = dX.as<double>();
-    K.Y = dY.as<double>();
-  }
+  if ((rc = upload_kernel(kd, n, dX, dY, dA, K))) return rc;
   {
     std::vector<int32_t> t0v(m), s0v(n);
     for (int64_t i = 0; i < m; i++) t0v[i] = static_cast<int32_t>(X.index_map[i] - 1);
@@ -1002,5 +1037,88 @@ extern "C" int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const doubl
   for (int64_t c = 0; c < r.r; c++)
     for (int64_t q = 0; q < n; q++) V_out[c + q * r.r] = vo[c * n + q];
   *r_out = r.r;
+  return HMGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sparsify_hmatrix(K, X, Y; eta) (src/hmatrix.jl:234-274)
+// ---------------------------------------------------------------------------
+extern "C" int hmgpu_sparsify(const hmgpu_kernel *kd, const hmgpu_tree *Xh, const hmgpu_tree *Yh, double eta,
+                              int64_t *I, int64_t *J, double *V, int64_t *nnz) {
+  if (!kd || !Xh || !Yh) return fail(HMGPU_ERR_INVALID, "NULL argument");
+  const Tree &X = Xh->t;
+  const Tree &Y = Yh->t;
+  const int64_t m = static_cast<int64_t>(X.index_map.size()), n = static_cast<int64_t>(Y.index_map.size());
+  if (m >= (int64_t(1) << 31) || n >= (int64_t(1) << 31)) return fail(HMGPU_ERR_INVALID, "too many rows or columns");
+  if (int rc = check_kernel(kd, m, n)) return rc;
+  Blocks blk;
+  try {
+    build_blocks(X, Y, eta, true, blk);  // BlockTree + merge_dense_matrices! + traverse (:236-239)
+  } catch (const std::bad_alloc &) {
+    return fail(HMGPU_ERR_NOMEM, "host allocation failed");
+  }
+  const size_t nd = blk.dense.size() / 2;
+  int64_t count = 0;
+  for (size_t b = 0; b < nd; b++) {
+    const Node &x = X.nodes[blk.dense[2 * b]], &y = Y.nodes[blk.dense[2 * b + 1]];
+    count += (x.end - x.start) * (y.end - y.start);
+  }
+  if (nnz) *nnz = count;
+  if (!I && !J && !V) return HMGPU_OK;
+  if (!I || !J || !V) return fail(HMGPU_ERR_INVALID, "I, J and V must all be given, or all be NULL to count");
+  // indices on the host (1-based original indices, :251-263)
+  int64_t k = 0;
+  for (size_t b = 0; b < nd; b++) {
+    const Node &x = X.nodes[blk.dense[2 * b]], &y = Y.nodes[blk.dense[2 * b + 1]];
+    for (int64_t i = x.start; i < x.end; i++)
+      for (int64_t j = y.start; j < y.end; j++, k++) {
+        I[k] = X.index_map[i - 1];
+        J[k] = Y.index_map[j - 1];
+      }
+  }
+  // values on the device, in pieces of at most kPiece entries
+  constexpr int64_t kPiece = int64_t(32) << 20;
+  DevBuf dX, dY, dA, dt, ds, dout, djobs;
+  KDev K;
+  int rc;
+  if ((rc = upload_kernel(kd, n, dX, dY, dA, K))) return rc;
+  {
+    std::vector<int32_t> t0v(m), s0v(n);
+    for (int64_t i = 0; i < m; i++) t0v[i] = static_cast<int32_t>(X.index_map[i] - 1);
+    for (int64_t j = 0; j < n; j++) s0v[j] = static_cast<int32_t>(Y.index_map[j] - 1);
+    if ((rc = dt.alloc(m * 4)) || (rc = ds.alloc(n * 4))) return rc;
+    cudaMemcpy(dt.p, t0v.data(), m * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(ds.p, s0v.data(), n * 4, cudaMemcpyHostToDevice);
+  }
+  int64_t largest = 0;
+  for (size_t b = 0; b < nd; b++) {
+    const Node &x = X.nodes[blk.dense[2 * b]], &y = Y.nodes[blk.dense[2 * b + 1]];
+    largest = std::max<int64_t>(largest, (x.end - x.start) * (y.end - y.start));
+  }
+  const int64_t piece = std::max(kPiece, largest);
+  if ((rc = dout.alloc(static_cast<size_t>(std::min(piece, std::max<int64_t>(count, 1))) * sizeof(double)))) return rc;
+  int64_t base = 0;
+  for (size_t b0 = 0; b0 < nd;) {
+    std::vector<SpJob> jobs;
+    int64_t used = 0;
+    size_t b = b0;
+    for (; b < nd; b++) {
+      const Node &x = X.nodes[blk.dense[2 * b]], &y = Y.nodes[blk.dense[2 * b + 1]];
+      const int64_t e = (x.end - x.start) * (y.end - y.start);
+      if (!jobs.empty() && used + e > piece) break;
+      jobs.push_back(SpJob{static_cast<int32_t>(x.start - 1), static_cast<int32_t>(x.end - x.start),
+                           static_cast<int32_t>(y.start - 1), static_cast<int32_t>(y.end - y.start), used});
+      used += e;
+    }
+    if ((rc = djobs.alloc(jobs.size() * sizeof(SpJob)))) return rc;
+    cudaMemcpy(djobs.p, jobs.data(), jobs.size() * sizeof(SpJob), cudaMemcpyHostToDevice);
+    const int grid = static_cast<int>(std::min<int64_t>((static_cast<int64_t>(jobs.size()) + 7) / 8, 65535));
+    sparsify_kernel<<<grid, 256>>>(K, dt.as<int32_t>(), ds.as<int32_t>(), djobs.as<SpJob>(),
+                                   static_cast<int64_t>(jobs.size()), dout.as<double>());
+    cudaError_t e = cudaMemcpy(V + base, dout.p, used * sizeof(double), cudaMemcpyDefault);
+    if (e != cudaSuccess) return cuda_fail(e, "sparsify entries");
+    base += used;
+    b0 = b;
+  }
   return HMGPU_OK;
 }

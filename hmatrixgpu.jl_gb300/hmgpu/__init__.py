@@ -25,7 +25,8 @@ from ._lib import (F64, F32, MIXED, PRECISIONS, KERNEL_IDS, HMGPUError, Info, Ke
 from . import _build
 
 __all__ = ["ClusterTree", "BlockTree", "ACA_plus", "SVD_recompress", "HMatrix", "Kernel", "info",
-           "traverse", "mul_", "HMGPUError", "build", "RankModel", "block_features", "batch", "Graph"]
+           "traverse", "mul_", "HMGPUError", "build", "RankModel", "block_features", "batch", "Graph",
+           "sparsify_hmatrix"]
 
 
 def build(verbose=False):
@@ -466,6 +467,28 @@ class HMatrix:
 
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
+
+
+def sparsify_hmatrix(K, X, Y, eta=1.5, triplets=False):
+    """sparsify_hmatrix(K, X, Y; eta) (src/hmatrix.jl:234-274): the dense leaves
+    of the merged block tree as a sparse matrix (scipy CSC, size(K)); with
+    triplets=True the 1-based (I, J, V) arrays in the reference's order. The
+    entries are generated on the device."""
+    if not isinstance(K, Kernel):
+        K = Kernel("explicit", A=K)
+    d = K.desc()
+    nnz = C.c_int64()
+    check(lib().hmgpu_sparsify(C.byref(d), X._h, Y._h, float(eta), None, None, None, C.byref(nnz)))
+    n = nnz.value
+    I = np.empty(n, np.int64)
+    J = np.empty(n, np.int64)
+    V = np.empty(n)
+    check(lib().hmgpu_sparsify(C.byref(d), X._h, Y._h, float(eta), ptr(I, I64P), ptr(J, I64P), ptr(V),
+                               C.byref(nnz)))
+    if triplets:
+        return I, J, V
+    import scipy.sparse as sp
+    return sp.csc_matrix((V, (I - 1, J - 1)), shape=K.size())
 
 
 def batch(members):

@@ -93,6 +93,7 @@ SIGNATURES = {
     "hmgpu_rank_model_params": (C.c_int, [VP, F32P, F32P, F32P, F32P]),
     "hmgpu_rank_model_free": (C.c_int, [VP]),
     "hmgpu_block_features": (C.c_int, [VP, VP, C.c_double, C.c_double, F32P, I64P]),
+    "hmgpu_sparsify": (C.c_int, [C.POINTER(KernelDesc), VP, VP, C.c_double, I64P, I64P, F64P, I64P]),
     "hmgpu_hmatrix_batch": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
     "hmgpu_graph_create": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64, C.POINTER(VP)]),
     "hmgpu_graph_launch": (C.c_int, [VP, VP]),

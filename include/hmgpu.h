@@ -253,6 +253,16 @@ int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const
 /* 8 -> 64 -> 64 -> 1 ReLU MLP in FP32 mapping block features to the rank    */
 /* plain ACA+ reaches, trained and evaluated by the library's own kernels.   */
 /* Used only to size and batch ACA work; results never depend on it.         */
+/* sparsify_hmatrix(K, X, Y; eta) (src/hmatrix.jl:234-274): the entries of every
+ * dense leaf of BlockTree(X, Y; eta) after merge_dense_matrices!, leaves in
+ * traversal order and each block row by row, as 1-based triplets (I, J, V) in
+ * original index order, exactly the arrays the reference gives sparse(). The
+ * values come from the device entry generator. With I, J and V all NULL only
+ * *nnz is set; otherwise all three must hold *nnz entries (I and J in host
+ * memory, V in host or device memory). */
+int hmgpu_sparsify(const hmgpu_kernel *K, const hmgpu_tree *X, const hmgpu_tree *Y, double eta,
+                   int64_t *I, int64_t *J, double *V, int64_t *nnz);
+
 /* ---- batches, CUDA graphs, autotuning (no counterpart in the reference) -- */
 /* One H-matrix made of `count` members: the block-diagonal operator
  * diag(H_1, ..., H_count), of size (sum m_k) x (sum n_k). Its products take

@@ -303,6 +303,28 @@ int or_block_tree(const or_tree *X, const or_tree *Y, double eta, int merge, or_
   return 0;
 }
 
+int64_t or_sparsify(const or_kernel *K, const or_tree *X, const or_tree *Y, double eta, int64_t *I,
+                    int64_t *J, double *V) {
+  or_blocks *b = NULL;
+  or_block_tree(X, Y, eta, 1, &b); /* BlockTree + merge_dense_matrices! (:236-237), traverse (:239) */
+  int64_t cnt = 0;
+  for (int64_t p = 0; p < b->nd; p++) { /* :250-264 */
+    const or_node *a = &X->nodes[b->dense[2 * p]], *c = &Y->nodes[b->dense[2 * p + 1]];
+    for (int64_t i = a->start; i < a->end; i++) {
+      const int64_t row = X->index_map[i - 1];
+      for (int64_t j = c->start; j < c->end; j++, cnt++) {
+        if (!I) continue;
+        const int64_t col = Y->index_map[j - 1];
+        I[cnt] = row;
+        J[cnt] = col;
+        V[cnt] = or_kernel_entry(K, row, col);
+      }
+    }
+  }
+  or_blocks_free(b);
+  return cnt;
+}
+
 int64_t or_blocks_num_dense(const or_blocks *b) { return b->nd; }
 int64_t or_blocks_num_approx(const or_blocks *b) { return b->na; }
 int64_t or_blocks_num_nodes(const or_blocks *b) { return b->nnodes; }

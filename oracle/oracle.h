@@ -81,6 +81,12 @@ typedef struct {
 double or_kernel_entry(const or_kernel *K, int64_t i, int64_t j);
 /* Dense product y = K * x over the whole matrix (reference test check). */
 void or_kernel_matvec(const or_kernel *K, const double *x, double *y);
+/* sparsify_hmatrix(K, X, Y; eta), src/hmatrix.jl:234-274: the entries of every
+ * dense leaf of the merged block tree, leaves in traversal order, each block row
+ * by row, as 1-based (I, J, V) triplets (the arrays the reference hands to
+ * sparse()). Returns the number of entries; fills I, J, V when non-NULL. */
+int64_t or_sparsify(const or_kernel *K, const or_tree *X, const or_tree *Y, double eta, int64_t *I,
+                    int64_t *J, double *V);
 
 /* ---- ACA+ and recompression: src/aca.jl:9-143 ---------------------------- */
 /* ACA+ on the sub-block K[rows, cols] (1-based original indices). U is m x cap

@@ -58,6 +58,8 @@ def lib():
         L.or_kernel_entry.argtypes = [C.POINTER(_Kernel), C.c_int64, C.c_int64]
         L.or_kernel_entry.restype = C.c_double
         L.or_kernel_matvec.argtypes = [C.POINTER(_Kernel), F64P, F64P]
+        L.or_sparsify.argtypes = [C.POINTER(_Kernel), C.c_void_p, C.c_void_p, C.c_double, I64P, I64P, F64P]
+        L.or_sparsify.restype = C.c_int64
         L.or_aca_plus.argtypes = [C.POINTER(_Kernel), I64P, C.c_int64, I64P, C.c_int64, C.c_double,
                                   C.c_int64, C.c_int64, F64P, F64P, I64P]
         L.or_svd_recompress.argtypes = [C.c_int64, C.c_int64, C.c_int64, F64P, F64P, C.c_double,
@@ -185,6 +187,19 @@ class Blocks:
                                  _p(self.node_adm, I8P), _p(self.node_dense, I8P),
                                  _p(self.node_left, I64P), _p(self.node_right, I64P))
         L.or_blocks_free(h)
+
+
+def sparsify(K, X, Y, eta=1.5):
+    """sparsify_hmatrix (src/hmatrix.jl:234-274) as its (I, J, V) triplets:
+    1-based original indices and K entries of every dense leaf, in the order
+    the reference pushes them."""
+    L = lib()
+    n = L.or_sparsify(C.byref(K._k), X._h, Y._h, float(eta), None, None, None)
+    I = np.empty(n, np.int64)
+    J = np.empty(n, np.int64)
+    V = np.empty(n)
+    L.or_sparsify(C.byref(K._k), X._h, Y._h, float(eta), _p(I, I64P), _p(J, I64P), _p(V))
+    return I, J, V
 
 
 def aca_plus(K, rows, cols, eps, max_iter=0):

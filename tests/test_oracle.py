@@ -172,3 +172,29 @@ def test_mul_cpu_threads_match():
     assert np.max(np.abs(y1 - y4)) <= 1e-13 * np.max(np.abs(y1))
     yd = K.matvec(x)
     assert np.linalg.norm(y1 - yd) / np.linalg.norm(yd) < 1e-5
+
+
+def _dense_multiply(H, x):
+    # test/test_hmatrix.jl:79-100: the dense blocks of the flattened HMatrix alone
+    y = np.zeros(H.m)
+    for rs, re, cs, ce, off in H.dense_block_indices:
+        m, n = re - rs + 1, ce - cs + 1
+        D = H.dense_blocks[off:off + m * n].reshape(m, n)
+        y[H.target_index_map[rs - 1:re] - 1] += D @ x[H.source_index_map[cs - 1:ce] - 1]
+    return y
+
+
+def test_sparsify_against_dense_part(circle_h):
+    """test/test_hmatrix.jl:102-108: sparsify_hmatrix(K, X, X; eta=1.5) * x equals
+    the product with the HMatrix's dense blocks (atol 1e-12)."""
+    K, T, H = circle_h
+    I, J, V = O.sparsify(K, T, T, eta=1.5)
+    assert len(I) == len(J) == len(V) > 0
+    assert (I >= 1).all() and (I <= H.m).all() and (J >= 1).all() and (J <= H.n).all()
+    x = np.random.default_rng(10).random(H.n)
+    c = np.zeros(H.m)
+    np.add.at(c, I - 1, V * x[J - 1])
+    assert np.max(np.abs(_dense_multiply(H, x) - c)) < 1e-12
+    # every entry is K[I, J]
+    for k in range(0, len(I), 997):
+        assert V[k] == K.entry(I[k], J[k])
