@@ -117,8 +117,10 @@ __global__ void permute_x_kernel(const T *__restrict__ x, const int32_t *__restr
 // row and 32/lanes rows run side by side. Row storage is phase-aligned with
 // XT, so element p of the row pairs with XT[x_off + p].
 // ---------------------------------------------------------------------------
+// Six CTAs per SM (40 registers) and four loads in flight per lane: the pass
+// is bound by memory latency, like the near/U pass.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ V,
+__global__ void __launch_bounds__(kThreads, 6) v_pass_kernel(const T *__restrict__ V,
                                                           const VUnit *__restrict__ units,
                                                           const int32_t *__restrict__ warp_begin,
                                                           T *__restrict__ xt) {
@@ -138,6 +140,23 @@ __global__ void __launch_bounds__(kThreads) v_pass_kernel(const T *__restrict__ 
       if (k < U.nrows) {
         const VT *row = reinterpret_cast<const VT *>(V + U.v_off + static_cast<int64_t>(k) * U.stride);
         int p = sub;
+        for (; p + 3 * g < nv; p += 4 * g) {  // four 16-byte loads of V in flight per lane
+          VT a0 = ld_stream(row + p), a1 = ld_stream(row + p + g);
+          VT a2 = ld_stream(row + p + 2 * g), a3 = ld_stream(row + p + 3 * g);
+          VT b0 = __ldg(X + p), b1 = __ldg(X + p + g), b2 = __ldg(X + p + 2 * g), b3 = __ldg(X + p + 3 * g);
+          const T *ea0 = reinterpret_cast<const T *>(&a0), *eb0 = reinterpret_cast<const T *>(&b0);
+          const T *ea1 = reinterpret_cast<const T *>(&a1), *eb1 = reinterpret_cast<const T *>(&b1);
+          const T *ea2 = reinterpret_cast<const T *>(&a2), *eb2 = reinterpret_cast<const T *>(&b2);
+          const T *ea3 = reinterpret_cast<const T *>(&a3), *eb3 = reinterpret_cast<const T *>(&b3);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea0[q], eb0[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea1[q], eb1[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea2[q], eb2[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea3[q], eb3[q], acc);
+        }
         for (; p + g < nv; p += 2 * g) {
           VT a0 = ld_stream(row + p), a1 = ld_stream(row + p + g);
           VT b0 = __ldg(X + p), b1 = __ldg(X + p + g);

@@ -55,10 +55,10 @@ void make_vunits(Plan &p, int64_t unit_bytes, int nwarps) {
   p.vunit_bytes = unit_bytes;
   std::vector<int64_t> uweight;
   for (const VGroup &g : p.vgroups) {
-    // lanes per row: a power of two leaving each lane at least two 16-byte
+    // lanes per row: a power of two leaving each lane at least four 16-byte
     // vectors of the row, so that loads overlap (at most a warp per row)
     int32_t nv = g.stride / p.vec, lanes = 1;
-    while (lanes * 2 < nv && lanes < 32) lanes *= 2;
+    while (lanes * 4 < nv && lanes < 32) lanes *= 2;
     const int64_t row_bytes = static_cast<int64_t>(g.stride) * esize;
     const int32_t rows_per = static_cast<int32_t>(std::max<int64_t>(1, unit_bytes / row_bytes));
     for (int32_t k0 = 0; k0 < g.rows; k0 += rows_per) {
