@@ -19,6 +19,7 @@ stream and returns without synchronising, as the reference's device mul! does.
 module HMatrixGB
 
 using LinearAlgebra
+import SparseArrays
 import LinearAlgebra: mul!
 import Base: *
 
@@ -209,10 +210,88 @@ function *(H::HMatrix{T}, x::AbstractVecOrMat{T}) where {T}
     return mul!(y, H, x)
 end
 
+# ---------------------------------------------------------------------------
+# sparsify_hmatrix (src/hmatrix.jl:234-274), batches, files, tuning
+# ---------------------------------------------------------------------------
+# A handle of either storage precision, typed from hmgpu_info.precision.
+function _wrap_auto(h)
+    info_buf = zeros(UInt8, 256)
+    check(ccall((:hmgpu_hmatrix_info, libhmgpu), Cint, (Ptr{Cvoid}, Ptr{UInt8}), h, info_buf))
+    p = reinterpret(Int32, info_buf[121:124])[1]
+    return _wrap(p == HMGPU_F64 ? Float64 : Float32, h)
+end
+
+"""
+    sparsify_hmatrix(kind::Symbol, Xpts, Ypts, X::ClusterTree, Y::ClusterTree; eta=1.5)
+
+sparsify_hmatrix(K, X, Y; eta) (src/hmatrix.jl:234-274) for the named kernel
+over `Xpts`/`Ypts`: the near field as a `SparseMatrixCSC`, entries generated on
+the GPU.
+"""
+function sparsify_hmatrix(kind::Symbol, Xpts::AbstractMatrix, Ypts::AbstractMatrix, X::ClusterTree,
+                          Y::ClusterTree; eta=1.5)
+    xp, yp = Matrix{Float64}(Xpts), Matrix{Float64}(Ypts)
+    k = Ref(KernelDesc(KERNELS[kind], 0, pointer(xp), size(xp, 2), pointer(yp), size(yp, 2), C_NULL, 0))
+    nnz = Ref{Int64}(0)
+    GC.@preserve xp yp begin
+        check(ccall((:hmgpu_sparsify, libhmgpu), Cint,
+                    (Ref{KernelDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Float64, Ptr{Int64}, Ptr{Int64},
+                     Ptr{Float64}, Ref{Int64}), k, X.handle, Y.handle, eta, C_NULL, C_NULL, C_NULL, nnz))
+        I, J, V = Vector{Int64}(undef, nnz[]), Vector{Int64}(undef, nnz[]), Vector{Float64}(undef, nnz[])
+        check(ccall((:hmgpu_sparsify, libhmgpu), Cint,
+                    (Ref{KernelDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Float64, Ptr{Int64}, Ptr{Int64},
+                     Ptr{Float64}, Ref{Int64}), k, X.handle, Y.handle, eta, I, J, V, nnz))
+    end
+    m = kind == :dipolar ? 3 * size(xp, 2) : size(xp, 2)
+    n = kind in (:vector_r, :dipolar) ? 3 * size(yp, 2) : size(yp, 2)
+    return SparseArrays.sparse(I, J, V, m, n)
+end
+
+"""
+    batch(Hs) -> HMatrix
+
+diag(H_1, ..., H_k) as one H-matrix: x and y are the members' vectors
+concatenated, and one product runs every member in the same kernel launches.
+"""
+function batch(Hs::AbstractVector{<:HMatrix})
+    hs = Ptr{Cvoid}[H.handle for H in Hs]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hmgpu_hmatrix_batch, libhmgpu), Cint, (Ptr{Ptr{Cvoid}}, Int32, Ref{Ptr{Cvoid}}),
+                hs, length(hs), h))
+    return _wrap_auto(h[])
+end
+
+"""save(H, path): the assembled H-matrix on disk; load(path) reads it back without assembly."""
+save(H::HMatrix, path::AbstractString) =
+    check(ccall((:hmgpu_hmatrix_save, libhmgpu), Cint, (Ptr{Cvoid}, Cstring), H.handle, path))
+
+function load(path::AbstractString)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hmgpu_hmatrix_load, libhmgpu), Cint, (Cstring, Ref{Ptr{Cvoid}}), path, h))
+    return _wrap_auto(h[])
+end
+
+"""autotune!(H; cache=nothing): times and keeps the product's work-partition
+parameters (results are unchanged); `cache` names a file for the choices."""
+function autotune!(H::HMatrix; cache::Union{Nothing,AbstractString}=nothing)
+    r = zeros(Int32, 4)
+    check(ccall((:hmgpu_hmatrix_autotune, libhmgpu), Cint, (Ptr{Cvoid}, Cstring, Ptr{Int32}),
+                H.handle, cache === nothing ? C_NULL : cache, r))
+    return (unit_rows=r[1], vunit_kib=r[2], multi_rhs_from=r[3], from_cache=r[4] != 0)
+end
+
+"""status(H): the device error word of the products so far (0 = clean)."""
+function status(H::HMatrix)
+    st = Ref{Cint}(0)
+    rc = ccall((:hmgpu_hmatrix_status, libhmgpu), Cint, (Ptr{Cvoid}, Ref{Cint}), H.handle, st)
+    rc in (0, -5) || check(rc)
+    return Int(st[])
+end
+
 # CUDA.jl hooks, resolved at run time so that this file loads without CUDA.jl.
 _devptr(a) = reinterpret(Ptr{Cvoid}, UInt(Base.unsafe_convert(Main.CUDA.CuPtr{eltype(a)}, a)))
 _stream() = reinterpret(Ptr{Cvoid}, Main.CUDA.stream().handle)
 
-export ClusterTree, HMatrix, info
+export ClusterTree, HMatrix, info, sparsify_hmatrix, batch, save, load, autotune!, status
 
 end # module

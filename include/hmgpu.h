@@ -195,7 +195,7 @@ typedef struct {
   int64_t device_bytes;          /* bytes held on the device                        */
   int64_t n_tiles;               /* row tiles of the near/U pass                    */
   int32_t precision;
-  int32_t hi_only_blocks;        /* HMGPU_MIXED: blocks stored hi-only BF16         */
+  int32_t hi_only_blocks;        /* 0: mixed precision keeps hi and lo for every block */
   double build_seconds;          /* wall time of the last import/build              */
   int64_t aca_batches;           /* device ACA batches of the build                 */
   int64_t aca_reruns;            /* blocks rerun after outgrowing their workspace   */
