@@ -35,8 +35,8 @@ WORKLOAD = "film-2^20 Laplace leaf64 eta2 tol1e-4, 1 RHS, FP32 storage"
 GRID, LEAF, ETA, TOL = 1024, 64, 2.0, 1e-4
 SAMPLE_STRIDE = 64  # the CPU legs time every 64th dense and admissible block
 # DRAM traffic / algorithmic bytes of the near/U kernel, from an ncu capture on
-# film 256 x 256 (431.6 MB of dram__bytes_read + write for 425.2 MB algorithmic)
-TRAFFIC_RATIO = 431.6 / 425.2
+# film 512 x 512 (1981.2 MB of dram__bytes_read + write for 1952.3 MB algorithmic)
+TRAFFIC_RATIO = 1981.2 / 1952.3
 
 
 def peaks():
@@ -380,9 +380,9 @@ def run_gpu(args):
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": src, "algorithmic_bytes_per_launch": du_bytes,
                      "traffic": du_bytes * TRAFFIC_RATIO,
-                     "traffic_source": "ncu dram__bytes_read+write of du_rows_kernel on film 256x256 "
-                                       "(431.6 MB for 425.2 MB algorithmic), scaled by algorithmic bytes "
-                                       "(profiles/du_rows_kernel_film256.md)"},
+                     "traffic_source": "ncu dram__bytes_read+write of du_rows_kernel on film 512x512 "
+                                       "(1981.2 MB for 1952.3 MB algorithmic), scaled by algorithmic bytes "
+                                       "(profiles/du_rows_v_pass_film512.md)"},
         "cpu_baseline": {"value": cpu_v, "unit": "matvec/s", "cores": 1, "kind": "port",
                          "sample": cpu_d["sample"]},
         "e2e": {"value": job_rate(world, e2e_s), "unit": "matvec/s", "h2d_bytes_per_step": n * es,
