@@ -103,6 +103,17 @@ int upload_plan(HMatrix &H, const std::vector<int32_t> &tmap0, const std::vector
   if ((rc = upload_units(H))) return rc;
   if ((rc = upload(H, &H.dp.tmap0, tmap0))) return rc;
   if ((rc = upload(H, &H.dp.smap0, smap0))) return rc;
+  {
+    int64_t n_src = 0;
+    for (int32_t v : smap0) n_src = std::max<int64_t>(n_src, static_cast<int64_t>(v) + 1);
+    std::vector<int32_t> sinv0(n_src, -1);
+    for (size_t c = 0; c < smap0.size(); c++)
+      if (smap0[c] >= 0) sinv0[smap0[c]] = static_cast<int32_t>(c);
+    for (int32_t v : sinv0)
+      if (v < 0) return fail(HMGPU_ERR_INVALID, "source map is not a permutation");
+    if ((rc = upload(H, &H.dp.sinv0, sinv0))) return rc;
+    H.dp.n_src = n_src;
+  }
   if ((rc = H.dalloc(reinterpret_cast<void **>(&H.dp.counter), 64))) return rc;
   cudaMemset(H.dp.counter, 0, 64);
   H.dp.status = H.dp.counter + 4;  // its own 16-byte slot of the same allocation

@@ -27,6 +27,8 @@ struct DevPlan {
   int32_t *tmap0 = nullptr;  // 0-based target map, length m
   int32_t *smap0 = nullptr;  // 0-based source map, length n (-1: a zero entry)
   int64_t zero_row = 0;      // an XT row that is always zero
+  int32_t *sinv0 = nullptr;  // XT row of each 0-based source index (inverse of smap0)
+  int64_t n_src = 0;
   int32_t *counter = nullptr;  // ticket counters of the passes (16 slots)
   int32_t *status = nullptr;   // device error word (0 = ok), see hmgpu_hmatrix_status
   int64_t m = 0, n = 0, x_len = 0, xt_len = 0;

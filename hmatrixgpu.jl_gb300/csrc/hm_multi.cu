@@ -62,23 +62,26 @@ __device__ __forceinline__ void lds8(const T *p, T (&v)[8]) {
   }
 }
 
-// XT rows: XT[c * kRhs + r] = X[smap[c] + r * ldx] for c < n and r < nr, else 0.
+// XT rows from X in its own order: X[j + r ldx] goes to XT[sinv[j] kRhs + r]
+// (0 for r >= nr). Reads of X are coalesced along j and every XT row is written
+// whole; the x-region rows that no source index maps to stay zero from the
+// allocation. Also re-arms both ticket counters.
 template <typename T>
 __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int nr,
-                                     const int32_t *__restrict__ smap0, int64_t n, int64_t x_len,
+                                     const int32_t *__restrict__ sinv0, int64_t n_src,
                                      T *__restrict__ xt, int32_t *__restrict__ counter) {
   __shared__ T tile[64][kRhs + 1];
   if (blockIdx.x == 0 && threadIdx.x < 2) counter[threadIdx.x] = 0;  // both ticket slots
-  for (int64_t c0 = blockIdx.x * 64ll; c0 < x_len; c0 += gridDim.x * 64ll) {
+  for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
     for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {
-      const int r = e / 64, cc = e % 64;  // consecutive threads: consecutive c
-      const int64_t c = c0 + cc;
-      tile[cc][r] = (c < n && r < nr && smap0[c] >= 0) ? X[smap0[c] + r * ldx] : T(0);
+      const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
+      const int64_t j = j0 + jj;
+      tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] : T(0);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {
-      const int cc = e / kRhs, r = e % kRhs;
-      if (c0 + cc < x_len) xt[(c0 + cc) * kRhs + r] = tile[cc][r];
+      const int jj = e / kRhs, r = e % kRhs;
+      if (j0 + jj < n_src) xt[static_cast<int64_t>(sinv0[j0 + jj]) * kRhs + r] = tile[jj][r];
     }
     __syncthreads();
   }
@@ -282,11 +285,11 @@ static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, 
                              int64_t ldx, int nr, T *Y, int64_t ldy, int grid_du,
                              cudaStream_t s, cudaEvent_t *ev, int *launches) {
   multi_attrs<T>();
-  int gp = static_cast<int>((p.x_len + 63) / 64);
+  int gp = static_cast<int>((p.n_src + 63) / 64);
   if (gp > 2048) gp = 2048;
   int nl = 0;
   if (ev) cudaEventRecord(ev[0], s);
-  permute_multi_kernel<T><<<gp, kThreads, 0, s>>>(X, ldx, nr, p.smap0, p.n, p.x_len, xt, p.counter);
+  permute_multi_kernel<T><<<gp, kThreads, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xt, p.counter);
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
   if (p.nmv > 0) {

@@ -444,29 +444,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(kTmemCols));
 }
 
-// XTS x rows: row c holds the 32 right-hand sides X[smap[c] + r ldx] split into
-// BF16 hi (first 64 bytes) and lo (last 64 bytes); rows c >= n are zero.
+// XTS x rows from X in its own order: the 32 right-hand sides X[j + r ldx]
+// (0 for r >= nr) of source index j, split into BF16 hi (first 64 bytes) and lo
+// (last 64 bytes), go to row sinv[j]. Reads of X are coalesced along j and
+// every row is written whole; x-region rows that no source index maps to stay
+// zero from the allocation. Also re-arms the two item tickets.
 __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, int nr,
-                                     const int32_t *__restrict__ smap0, int64_t n, int64_t x_len,
+                                     const int32_t *__restrict__ sinv0, int64_t n_src,
                                      uint16_t *__restrict__ xts, int32_t *__restrict__ tickets) {
   __shared__ float tile[64][kTcRhs + 1];
   if (blockIdx.x == 0 && threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
-  for (int64_t c0 = blockIdx.x * 64ll; c0 < x_len; c0 += gridDim.x * 64ll) {
+  for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
     for (int e = threadIdx.x; e < 64 * kTcRhs; e += blockDim.x) {
-      const int r = e / 64, cc = e % 64;  // consecutive threads: consecutive c
-      const int64_t c = c0 + cc;
-      tile[cc][r] = (c < n && r < nr && smap0[c] >= 0) ? X[smap0[c] + r * ldx] : 0.0f;
+      const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
+      const int64_t j = j0 + jj;
+      tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] : 0.0f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * 4; e += blockDim.x) {
-      const int cc = e >> 2, q = e & 3;
-      if (c0 + cc < x_len) {
+      const int jj = e >> 2, q = e & 3;
+      if (j0 + jj < n_src) {
         float v[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++) v[i] = tile[cc][8 * q + i];
+        for (int i = 0; i < 8; i++) v[i] = tile[jj][8 * q + i];
         uint4 hi, lo;
         split8(v, hi, lo);
-        uint4 *dst = reinterpret_cast<uint4 *>(xts + (c0 + cc) * (2 * kTcRhs));
+        uint4 *dst = reinterpret_cast<uint4 *>(xts + static_cast<int64_t>(sinv0[j0 + jj]) * (2 * kTcRhs));
         dst[q] = hi;
         dst[4 + q] = lo;
       }
@@ -547,10 +550,10 @@ cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, i
                              float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches) {
   tc_attrs();
   int nl = 0;
-  int gp = static_cast<int>((p.x_len + 63) / 64);
+  int gp = static_cast<int>((p.n_src + 63) / 64);
   if (gp > 2048) gp = 2048;
   if (ev) cudaEventRecord(ev[0], s);
-  permute_split_kernel<<<gp, 256, 0, s>>>(X, ldx, nr, p.smap0, p.n, p.x_len, t.xts, p.counter + 2);
+  permute_split_kernel<<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, t.xts, p.counter + 2);
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
   TcArgs a{};
