@@ -28,6 +28,10 @@ struct Tree {
 };
 
 int build_tree(const double *coords, int64_t npts, int64_t leaf, int64_t dims, Tree &t);
+// The same tree built on the current GPU (hm_tree_dev.cu), bit-identical.
+int build_tree_device(const double *coords, int64_t npts, int64_t leaf, int64_t dims, Tree &t);
+// Pre-order renumbering and dims expansion shared by both builds.
+void finish_tree(Tree &t, std::vector<int64_t> &perm, int64_t dims);
 
 // ---- block tree (src/block.jl) ---------------------------------------------------
 struct BNode {

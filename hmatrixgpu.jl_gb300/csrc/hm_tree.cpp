@@ -130,6 +130,16 @@ int build_tree(const double *coords, int64_t npts, int64_t leaf, int64_t dims, T
     }
     t.nodes[w.slot] = nd;
   }
+  finish_tree(t, perm, dims);
+  return HMGPU_OK;
+}
+
+// Nodes (children created in consecutive slots when their parent is processed,
+// root in slot 0) renumbered into pre-order, and the dims expansion of the
+// ranges and the index map (src/tree.jl:59-64, :123-137). perm: the final
+// point order, 1-based.
+void finish_tree(Tree &t, std::vector<int64_t> &perm, int64_t dims) {
+  const int64_t npts = static_cast<int64_t>(perm.size());
   // Renumber into pre-order (parent, left subtree, right subtree).
   {
     std::vector<int64_t> newid(t.nodes.size(), -1), order;
@@ -164,7 +174,6 @@ int build_tree(const double *coords, int64_t npts, int64_t leaf, int64_t dims, T
   } else {
     t.index_map.swap(perm);
   }
-  return HMGPU_OK;
 }
 
 // ---------------------------------------------------------------------------

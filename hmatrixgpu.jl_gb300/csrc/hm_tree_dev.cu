@@ -1,0 +1,432 @@
+// Cluster tree built on the GPU, bit-identical to the host build (hm_tree.cpp).
+//
+// The reference builds the tree recursively on the host (src/tree.jl:70-116,
+// build_tree_node): bounding box and centroid of the node's points in their
+// current order, split along the longest box edge at the centroid with a stable
+// partition (`sortperm` of the predicate `x[axis] < center[axis]`, left part
+// first), leaf iff the node holds at most max_points_per_leaf points.
+//
+// Here the tree grows level by level, one CTA per node of the level:
+//   pass 1  bounding box (any order: only min/max) and the centroid sums; a sum
+//           is one floating-point chain in the points' current order, exactly
+//           as `sum(x; dims=2)` over the node's columns in src/tree.jl:83,
+//           kept sequential by one lane per axis while the other warps stage
+//           the next chunk of coordinates in shared memory;
+//   pass 2  count of the points left of the centroid;
+//   pass 3  stable scatter of the point indices and their coordinates into the
+//           other buffer (left part in order, then the right part in order).
+// The coordinates travel with the indices (structure of arrays, ping-pong
+// buffers), so every pass reads contiguous memory. Leaves copy their index
+// range into the final permutation. Nodes get slots in the order their parents
+// finish; the shared host step renumbers them into pre-order, so the slot order
+// does not matter.
+//
+// All arithmetic goes through the _rn intrinsics (no contraction); the norm is
+// LinearAlgebra.generic_norm2 of a 3-vector as in the host build.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hm_api.h"
+#include "hm_internal.h"
+
+namespace hm {
+namespace {
+
+constexpr int kTreeThreads = 512;
+constexpr int kWarps = kTreeThreads / 32;
+constexpr int kChunk = 512;   // coordinates per axis staged per step of pass 1
+constexpr int kItems = 4;     // points per thread per step of pass 3
+
+struct DNode {
+  int32_t start, cnt;   // 0-based first point and number of points
+  int32_t left, right;  // child slots, -1 for none
+  double center[3];
+  double radius;
+  int32_t leaf, pad;
+};
+
+struct Level {
+  const double *cx, *cy, *cz;  // coordinates of the current order
+  const int32_t *cperm;        // current order (0-based point indices)
+  double *nx, *ny, *nz;        // next order, written by splitting nodes
+  int32_t *nperm;
+  int32_t *final_perm;         // order of the finished tree
+  DNode *nodes;
+  int32_t first, next_base, cap;
+  int32_t leaf;
+  int32_t *ctl;  // [0] next-level slots taken, [1] error code, [2] size of the failed node
+};
+
+__device__ __forceinline__ double nan_min(double a, double b) {
+  return (isnan(a) || isnan(b)) ? __longlong_as_double(0x7ff8000000000000ll) : (b < a ? b : a);
+}
+__device__ __forceinline__ double nan_max(double a, double b) {
+  return (isnan(a) || isnan(b)) ? __longlong_as_double(0x7ff8000000000000ll) : (b > a ? b : a);
+}
+
+// Base.isless ordering used by argmax: NaN above all numbers.
+__device__ __forceinline__ bool isless_gt(double a, double b) {
+  if (isnan(a)) return !isnan(b);
+  if (isnan(b)) return false;
+  return a > b;
+}
+
+// LinearAlgebra.generic_norm2 of a 3-vector, as the host build computes it.
+__device__ double norm3_dev(double a, double b, double c) {
+  const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+  if (isnan(a) || isnan(b) || isnan(c)) return qnan;
+  double mx = fabs(a);
+  if (fabs(b) > mx) mx = fabs(b);
+  if (fabs(c) > mx) mx = fabs(c);
+  if (mx == 0.0 || isinf(mx)) return mx;
+  const double m2 = __dmul_rn(mx, mx);
+  if (isfinite(__dmul_rn(__dmul_rn(3.0, mx), mx)) && m2 != 0.0) {
+    double s = __dmul_rn(a, a);
+    s = __dadd_rn(s, __dmul_rn(b, b));
+    s = __dadd_rn(s, __dmul_rn(c, c));
+    return __dsqrt_rn(s);
+  }
+  const double qa = __ddiv_rn(fabs(a), mx), qb = __ddiv_rn(fabs(b), mx), qc = __ddiv_rn(fabs(c), mx);
+  double s = __dmul_rn(qa, qa);
+  s = __dadd_rn(s, __dmul_rn(qb, qb));
+  s = __dadd_rn(s, __dmul_rn(qc, qc));
+  return __dmul_rn(mx, __dsqrt_rn(s));
+}
+
+__global__ void tree_init_kernel(const double *__restrict__ coords, int32_t npts, double *x, double *y,
+                                 double *z, int32_t *perm) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = coords[3 * i];
+    y[i] = coords[3 * i + 1];
+    z[i] = coords[3 * i + 2];
+    perm[i] = static_cast<int32_t>(i);
+  }
+}
+
+// Exclusive block scan of one int per thread; returns the prefix and sets *total.
+__device__ int block_exclusive_scan(int v, int *warp_tot, int *total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < kWarps ? warp_tot[lane] : 0;
+    int s = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int u = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += u;
+    }
+    if (lane < kWarps) warp_tot[lane] = s - t;  // exclusive warp offsets
+    if (lane == kWarps - 1) warp_tot[kWarps] = s;
+  }
+  __syncthreads();
+  const int r = warp_tot[w] + inc - v;
+  *total = warp_tot[kWarps];
+  __syncthreads();  // warp_tot is reused by the next call
+  return r;
+}
+
+__global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
+  __shared__ double stage[2][3][kChunk];
+  __shared__ double red_lo[kWarps][3], red_hi[kWarps][3], sums[3];
+  __shared__ double s_center;
+  __shared__ int s_axis, s_split, s_nl;
+  __shared__ int warp_tot[kWarps + 1];
+
+  const int slot = L.first + blockIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int32_t start = L.nodes[slot].start, cnt = L.nodes[slot].cnt;
+  const double *src[3] = {L.cx + start, L.cy + start, L.cz + start};
+
+  // ---- pass 1: bounding box and the three sequential sums -----------------
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  double lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+  double acc = 0.0;  // lanes 0..2 of warp 0: the sum of axis `lane`
+  const int nch = (cnt + kChunk - 1) / kChunk;
+  for (int k = 0; k <= nch; k++) {
+    if (warp != 0) {
+      if (k < nch) {
+        const int base = k * kChunk, len = min(kChunk, cnt - base);
+        double(*buf)[kChunk] = stage[k & 1];
+        for (int i = tid - 32; i < len; i += kTreeThreads - 32) {
+#pragma unroll
+          for (int a = 0; a < 3; a++) {
+            const double v = src[a][base + i];
+            buf[a][i] = v;
+            lo[a] = nan_min(lo[a], v);
+            hi[a] = nan_max(hi[a], v);
+          }
+        }
+      }
+    } else if (lane < 3 && k > 0) {
+      const int base = (k - 1) * kChunk, len = min(kChunk, cnt - base);
+      const double *row = stage[(k - 1) & 1][lane];
+      int i = 0;
+      for (; i + 8 <= len; i += 8) {
+        double v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = row[i + j];
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc = __dadd_rn(acc, v[j]);
+      }
+      for (; i < len; i++) acc = __dadd_rn(acc, row[i]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[a] = nan_min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+      hi[a] = nan_max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+    }
+  }
+  if (lane == 0)
+    for (int a = 0; a < 3; a++) {
+      red_lo[warp][a] = lo[a];
+      red_hi[warp][a] = hi[a];
+    }
+  if (warp == 0 && lane < 3) sums[lane] = acc;
+  __syncthreads();
+  if (tid == 0) {
+    double blo[3], bhi[3], len[3];
+    DNode nd;
+    for (int a = 0; a < 3; a++) {
+      blo[a] = red_lo[1][a];
+      bhi[a] = red_hi[1][a];
+      for (int w = 2; w < kWarps; w++) {
+        blo[a] = nan_min(blo[a], red_lo[w][a]);
+        bhi[a] = nan_max(bhi[a], red_hi[w][a]);
+      }
+      len[a] = __dsub_rn(bhi[a], blo[a]);
+      nd.center[a] = __ddiv_rn(sums[a], static_cast<double>(cnt));
+    }
+    int axis = 0;
+    for (int a = 1; a < 3; a++)
+      if (isless_gt(len[a], len[axis])) axis = a;
+    const double r1 = norm3_dev(__dsub_rn(nd.center[0], bhi[0]), __dsub_rn(nd.center[1], bhi[1]),
+                                __dsub_rn(nd.center[2], bhi[2]));
+    const double r2 = norm3_dev(__dsub_rn(nd.center[0], blo[0]), __dsub_rn(nd.center[1], blo[1]),
+                                __dsub_rn(nd.center[2], blo[2]));
+    nd.radius = (isnan(r1) || isnan(r2)) ? __longlong_as_double(0x7ff8000000000000ll) : (r2 > r1 ? r2 : r1);
+    nd.start = start;
+    nd.cnt = cnt;
+    nd.left = nd.right = -1;
+    nd.leaf = cnt <= L.leaf;
+    nd.pad = 0;
+    L.nodes[slot] = nd;
+    s_center = nd.center[axis];
+    s_axis = axis;
+    s_split = !nd.leaf;
+  }
+  __syncthreads();
+
+  if (!s_split) {  // a leaf: its order is final
+    for (int i = tid; i < cnt; i += kTreeThreads) L.final_perm[start + i] = L.cperm[start + i];
+    return;
+  }
+  const double c = s_center;
+  const double *key = s_axis == 0 ? src[0] : (s_axis == 1 ? src[1] : src[2]);
+
+  // ---- pass 2: size of the left part ---------------------------------------
+  int nleft = 0;
+  for (int i = tid; i < cnt; i += kTreeThreads) nleft += key[i] < c ? 1 : 0;
+  int nl = 0;
+  block_exclusive_scan(nleft, warp_tot, &nl);
+  if (nl == 0 || nl == cnt) {  // a coincident cluster: the host reports it
+    if (tid == 0) {
+      atomicCAS(L.ctl + 1, 0, HMGPU_ERR_TREE);
+      atomicMax(L.ctl + 2, cnt);
+    }
+    return;
+  }
+
+  // ---- pass 3: stable scatter ------------------------------------------------
+  double *dst[3] = {L.nx + start, L.ny + start, L.nz + start};
+  const int32_t *pin = L.cperm + start;
+  int32_t *pout = L.nperm + start;
+  int left_before = 0;  // left points in earlier steps
+  for (int base = 0; base < cnt; base += kTreeThreads * kItems) {
+    const int i0 = base + tid * kItems;
+    bool f[kItems];
+    int nf = 0;
+#pragma unroll
+    for (int j = 0; j < kItems; j++) {
+      f[j] = i0 + j < cnt && key[i0 + j] < c;
+      nf += f[j] ? 1 : 0;
+    }
+    int step_total = 0;
+    int lb = left_before + block_exclusive_scan(nf, warp_tot, &step_total);
+#pragma unroll
+    for (int j = 0; j < kItems; j++) {
+      const int i = i0 + j;
+      if (i >= cnt) break;
+      const int d = f[j] ? lb : nl + (i - lb);
+      lb += f[j] ? 1 : 0;
+      pout[d] = pin[i];
+#pragma unroll
+      for (int a = 0; a < 3; a++) dst[a][d] = src[a][i];
+    }
+    left_before += step_total;
+  }
+  if (tid == 0) {
+    const int s = atomicAdd(L.ctl, 2);
+    const int l = L.next_base + s;
+    if (l + 1 >= L.cap) {
+      atomicCAS(L.ctl + 1, 0, 1);  // out of node slots
+      return;
+    }
+    DNode ch{};
+    ch.left = ch.right = -1;
+    ch.start = start;
+    ch.cnt = nl;
+    L.nodes[l] = ch;
+    ch.start = start + nl;
+    ch.cnt = cnt - nl;
+    L.nodes[l + 1] = ch;
+    L.nodes[slot].left = l;
+    L.nodes[slot].right = l + 1;
+  }
+}
+
+struct Buf {
+  void *p = nullptr;
+  ~Buf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes ? bytes : 16); }
+  template <typename V>
+  V *as() const {
+    return static_cast<V *>(p);
+  }
+};
+
+}  // namespace
+
+int build_tree_device(const double *coords, int64_t npts, int64_t leaf, int64_t dims, Tree &t) {
+  if (dims <= 0) return fail(HMGPU_ERR_INVALID, "Parameter `dims` must be a positive integer.");
+  if (npts <= 0) return fail(HMGPU_ERR_INVALID, "cluster tree needs at least one point");
+  if (leaf <= 0) return fail(HMGPU_ERR_INVALID, "max_points_per_leaf must be positive");
+  if (!coords) return fail(HMGPU_ERR_INVALID, "coords is NULL");
+  if (npts >= (int64_t{1} << 30))
+    return fail(HMGPU_ERR_INVALID, "the device tree build takes fewer than 2^30 points");
+  const int32_t n = static_cast<int32_t>(npts);
+  const int32_t cap = 2 * n - 1 + 2;  // a binary tree over n points has at most 2n - 1 nodes
+  Buf dcoords, dxyz, dperm, dfinal, dnodes, dctl;
+  cudaError_t e = cudaSuccess;
+  if ((e = dcoords.alloc(sizeof(double) * 3 * npts)) != cudaSuccess ||
+      (e = dxyz.alloc(sizeof(double) * 6 * npts)) != cudaSuccess ||
+      (e = dperm.alloc(sizeof(int32_t) * 2 * npts)) != cudaSuccess ||
+      (e = dfinal.alloc(sizeof(int32_t) * npts)) != cudaSuccess ||
+      (e = dnodes.alloc(sizeof(DNode) * static_cast<size_t>(cap))) != cudaSuccess ||
+      (e = dctl.alloc(sizeof(int32_t) * 4)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(HMGPU_ERR_NOMEM, "device memory for the tree build");
+  }
+  e = cudaMemcpy(dcoords.p, coords, sizeof(double) * 3 * npts, cudaMemcpyDefault);
+  if (e != cudaSuccess) return cuda_fail(e, "copying coordinates");
+  double *xyz = dxyz.as<double>();
+  int32_t *perm = dperm.as<int32_t>();
+  tree_init_kernel<<<std::min<int64_t>((npts + 255) / 256, 4096), 256>>>(dcoords.as<double>(), n, xyz,
+                                                                          xyz + npts, xyz + 2 * npts, perm);
+  DNode root{};
+  root.start = 0;
+  root.cnt = n;
+  root.left = root.right = -1;
+  cudaMemcpy(dnodes.p, &root, sizeof root, cudaMemcpyHostToDevice);
+  cudaMemset(dctl.p, 0, sizeof(int32_t) * 4);
+
+  int32_t first = 0, count = 1, cur = 0;
+  const int32_t lf = static_cast<int32_t>(std::min<int64_t>(leaf, INT32_MAX));
+  while (count > 0) {
+    Level L;
+    const double *c = xyz + static_cast<size_t>(cur) * 3 * npts;
+    double *nb = xyz + static_cast<size_t>(cur ^ 1) * 3 * npts;
+    L.cx = c;
+    L.cy = c + npts;
+    L.cz = c + 2 * npts;
+    L.cperm = perm + static_cast<size_t>(cur) * npts;
+    L.nx = nb;
+    L.ny = nb + npts;
+    L.nz = nb + 2 * npts;
+    L.nperm = perm + static_cast<size_t>(cur ^ 1) * npts;
+    L.final_perm = dfinal.as<int32_t>();
+    L.nodes = dnodes.as<DNode>();
+    L.first = first;
+    L.next_base = first + count;
+    L.cap = cap;
+    L.leaf = lf;
+    L.ctl = dctl.as<int32_t>();
+    tree_level_kernel<<<count, kTreeThreads>>>(L);
+    int32_t ctl[4];
+    e = cudaMemcpy(ctl, dctl.p, sizeof ctl, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "tree level kernel");
+    if (ctl[1] == HMGPU_ERR_TREE)
+      return fail(HMGPU_ERR_TREE, "cluster of " + std::to_string(ctl[2]) +
+                                      " points cannot be bisected (coincident points exceed the leaf size)");
+    if (ctl[1] != 0) return fail(HMGPU_ERR_CUDA, "tree build ran out of node slots");
+    first += count;
+    count = ctl[0];
+    cudaMemset(dctl.p, 0, sizeof(int32_t));
+    cur ^= 1;
+  }
+  const int32_t nnodes = first;
+  std::vector<DNode> hn(nnodes);
+  std::vector<int32_t> hp(npts);
+  e = cudaMemcpy(hn.data(), dnodes.p, sizeof(DNode) * nnodes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hp.data(), dfinal.p, sizeof(int32_t) * npts, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "reading the tree back");
+  t.npts = npts;
+  t.dims = dims;
+  t.index_map.clear();
+  t.nodes.resize(nnodes);
+  for (int32_t k = 0; k < nnodes; k++) {
+    const DNode &d = hn[k];
+    Node &q = t.nodes[k];
+    q.start = int64_t{d.start} + 1;
+    q.end = q.start + d.cnt;
+    q.left = d.left;
+    q.right = d.right;
+    std::memcpy(q.center, d.center, sizeof q.center);
+    q.radius = d.radius;
+    q.leaf = d.leaf != 0;
+  }
+  std::vector<int64_t> p64(npts);
+  for (int64_t i = 0; i < npts; i++) p64[i] = int64_t{hp[i]} + 1;
+  finish_tree(t, p64, dims);
+  return HMGPU_OK;
+}
+
+}  // namespace hm
+
+extern "C" int hmgpu_tree_build_device(const double *coords, int64_t npts, int64_t leaf, int64_t dims,
+                                       hmgpu_tree **out) {
+  if (!out) return hm::fail(HMGPU_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  auto *h = new (std::nothrow) hmgpu_tree;
+  if (!h) return hm::fail(HMGPU_ERR_NOMEM, "host allocation failed");
+  int rc;
+  try {
+    rc = hm::build_tree_device(coords, npts, leaf, dims, h->t);
+  } catch (const std::bad_alloc &) {
+    rc = hm::fail(HMGPU_ERR_NOMEM, "host allocation failed");
+  }
+  if (rc != HMGPU_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return HMGPU_OK;
+}

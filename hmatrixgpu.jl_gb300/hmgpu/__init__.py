@@ -59,16 +59,22 @@ class ClusterNode:
 
 
 class ClusterTree:
-    """ClusterTree(coordinates; max_points_per_leaf=32, dims=1) (src/tree.jl:45-67)."""
+    """ClusterTree(coordinates; max_points_per_leaf=32, dims=1) (src/tree.jl:45-67).
 
-    def __init__(self, coordinates, max_points_per_leaf=32, dims=1):
+    gpu=True builds the same tree (bit for bit) on the current CUDA device."""
+
+    def __init__(self, coordinates, max_points_per_leaf=32, dims=1, gpu=False):
         if dims <= 0:
             raise ValueError("Parameter `dims` must be a positive integer.")
         self.coordinates = _coords(coordinates)
         L = lib()
         h = C.c_void_p()
-        check(L.hmgpu_tree_build(ptr(self.coordinates), self.coordinates.shape[1],
-                                 int(max_points_per_leaf), int(dims), C.byref(h)))
+        if gpu:
+            check(L.hmgpu_tree_build_device(self.coordinates.ctypes.data, self.coordinates.shape[1],
+                                            int(max_points_per_leaf), int(dims), C.byref(h)))
+        else:
+            check(L.hmgpu_tree_build(ptr(self.coordinates), self.coordinates.shape[1],
+                                     int(max_points_per_leaf), int(dims), C.byref(h)))
         self._h = h
         self.dims = dims
         self.max_points_per_leaf = max_points_per_leaf

@@ -27,9 +27,10 @@ def sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
-# Per-file flags: the assembly kernels must not contract a*b+c into an FMA, so
-# that matrix entries and ACA residuals round exactly as the reference's do.
-PER_FILE = {"hm_build.cu": ["--fmad=false"]}
+# Per-file flags: the assembly and tree kernels must not contract a*b+c into an
+# FMA, so that matrix entries, ACA residuals and cluster centres round exactly
+# as the reference's do.
+PER_FILE = {"hm_build.cu": ["--fmad=false"], "hm_tree_dev.cu": ["--fmad=false"]}
 
 
 def _compile(src, extra):

@@ -55,6 +55,7 @@ SIGNATURES = {
     "hmgpu_last_error": (C.c_char_p, []),
     "hmgpu_abi_version": (C.c_int, []),
     "hmgpu_tree_build": (C.c_int, [F64P, C.c_int64, C.c_int64, C.c_int64, C.POINTER(VP)]),
+    "hmgpu_tree_build_device": (C.c_int, [VP, C.c_int64, C.c_int64, C.c_int64, C.POINTER(VP)]),
     "hmgpu_tree_info": (C.c_int, [VP, I64P, I64P, I64P, I64P, I64P]),
     "hmgpu_tree_export": (C.c_int, [VP, I64P, I64P, I64P, I8P, I64P, I64P, F64P, F64P]),
     "hmgpu_tree_free": (C.c_int, [VP]),

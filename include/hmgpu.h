@@ -69,6 +69,13 @@ typedef struct hmgpu_tree hmgpu_tree;
 /* coords: 3 x npts column-major (Julia's coordinates[:, i]). */
 int hmgpu_tree_build(const double *coords, int64_t npts, int64_t max_points_per_leaf,
                      int64_t dims, hmgpu_tree **out);
+/* The same tree built on the current GPU, bit-identical to hmgpu_tree_build
+ * (same permutation, ranges, centers and radii; same errors). Replaces the
+ * same reference call; coords may be host or device memory; npts < 2^30.
+ * Level by level, one CTA per node; the centroid sums keep the reference's
+ * sequential order. */
+int hmgpu_tree_build_device(const double *coords, int64_t npts, int64_t max_points_per_leaf,
+                            int64_t dims, hmgpu_tree **out);
 /* nnodes, index-map length (dims*npts), and info(): depth, max/min points. */
 int hmgpu_tree_info(const hmgpu_tree *t, int64_t *nnodes, int64_t *index_len, int64_t *depth,
                     int64_t *max_points, int64_t *min_points);
