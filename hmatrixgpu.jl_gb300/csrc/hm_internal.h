@@ -47,6 +47,8 @@ struct Blocks {
 };
 
 void build_blocks(const Tree &X, const Tree &Y, double eta, bool merge, Blocks &b);
+// The same block tree built on the current GPU (hm_tree_dev.cu), bit-identical.
+int build_blocks_device(const Tree &X, const Tree &Y, double eta, bool merge, Blocks &b);
 
 // ---- the assembled block structure ------------------------------------------------
 // Block ranges are 0-based and half-open in permuted index space.

@@ -1,4 +1,5 @@
-// Cluster tree built on the GPU, bit-identical to the host build (hm_tree.cpp).
+// Cluster tree and block tree built on the GPU, bit-identical to the host
+// builds (hm_tree.cpp).
 //
 // The reference builds the tree recursively on the host (src/tree.jl:70-116,
 // build_tree_node): bounding box and centroid of the node's points in their
@@ -29,6 +30,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <memory>
 #include <vector>
 
 #include "hm_api.h"
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
   __shared__ double stage[2][3][kChunk];
   __shared__ double red_lo[kWarps][3], red_hi[kWarps][3], sums[3];
   __shared__ double s_center;
-  __shared__ int s_axis, s_split, s_nl;
+  __shared__ int s_axis, s_split;
   __shared__ int warp_tot[kWarps + 1];
 
   const int slot = L.first + blockIdx.x;
@@ -301,6 +303,130 @@ __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// block tree (src/block.jl:58-155) level by level
+// ---------------------------------------------------------------------------
+// The host build numbers block-tree nodes in creation order of a pre-order walk:
+// the children of the j-th internal node (counted in pre-order) get the numbers
+// 1 + 2j and 2 + 2j. Here the tree grows breadth first; a bottom-up sweep then
+// counts the internal nodes of every subtree (and applies the dense merge and
+// the traverse counts), and a top-down sweep gives every node its pre-order
+// internal rank, its number and its place in the traverse lists.
+
+struct CNodes {  // a cluster tree, pre-order, structure of arrays
+  const double *center;  // 3 per node
+  const double *radius;
+  const int32_t *left, *right;
+  const int8_t *leaf;
+};
+
+struct BLevel {  // one breadth-first level of the block tree
+  int32_t *x, *y;     // target and source cluster nodes
+  int32_t *child;     // first child in the next level, -1 for none
+  int8_t *kind;       // 0 split, 1 admissible, 2 dense leaf
+  int8_t *dn;         // dense after the merge
+  int8_t *reached;    // visited by traverse (no emitting ancestor)
+  int32_t *nint;      // internal nodes in the subtree
+  int32_t *na, *nd;   // traverse emissions in the subtree (approx, dense)
+  int32_t *rank;      // pre-order rank among internal nodes (internal nodes only)
+  int32_t *id;        // number in the host numbering
+  int32_t *offa, *offd;
+};
+
+__global__ void bt_level_kernel(int32_t n, BLevel cur, BLevel nxt, CNodes X, CNodes Y, double eta,
+                                int32_t *counter) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t xi = cur.x[i], yi = cur.y[i];
+    const double *cx = X.center + 3 * static_cast<int64_t>(xi), *cy = Y.center + 3 * static_cast<int64_t>(yi);
+    const double rx = X.radius[xi], ry = Y.radius[yi];
+    const double dist = norm3_dev(__dsub_rn(cx[0], cy[0]), __dsub_rn(cx[1], cy[1]), __dsub_rn(cx[2], cy[2]));
+    int8_t kind;
+    int32_t child = -1;
+    if (dist > __dmul_rn(eta, __dadd_rn(rx, ry))) {
+      kind = 1;
+    } else if (X.leaf[xi] && Y.leaf[yi]) {
+      kind = 2;
+    } else {
+      kind = 0;
+      const bool split_y = (!Y.leaf[yi] && ry > rx) || X.leaf[xi];
+      child = atomicAdd(counter, 2);
+      if (split_y) {
+        nxt.x[child] = xi;
+        nxt.y[child] = Y.left[yi];
+        nxt.x[child + 1] = xi;
+        nxt.y[child + 1] = Y.right[yi];
+      } else {
+        nxt.x[child] = X.left[xi];
+        nxt.y[child] = yi;
+        nxt.x[child + 1] = X.right[xi];
+        nxt.y[child + 1] = yi;
+      }
+    }
+    cur.kind[i] = kind;
+    cur.child[i] = child;
+  }
+}
+
+// Bottom-up: merge_dense_matrices! (src/block.jl:98-112) and the subtree counts.
+__global__ void bt_up_kernel(int32_t n, BLevel cur, BLevel nxt, int merge) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int8_t kind = cur.kind[i];
+    int8_t dn = kind == 2;
+    int32_t nint = 0, na = kind == 1, nd = dn;
+    if (kind == 0) {
+      const int32_t l = cur.child[i];
+      dn = merge && nxt.dn[l] && nxt.dn[l + 1];
+      nint = 1 + nxt.nint[l] + nxt.nint[l + 1];
+      na = dn ? 0 : nxt.na[l] + nxt.na[l + 1];
+      nd = dn ? 1 : nxt.nd[l] + nxt.nd[l + 1];
+    }
+    cur.dn[i] = dn;
+    cur.nint[i] = nint;
+    cur.na[i] = na;
+    cur.nd[i] = nd;
+  }
+}
+
+// Top-down: numbers, node records in the host numbering, traverse lists
+// (src/block.jl:127-155: admissible and dense nodes in pre-order, no descent
+// below them).
+__global__ void bt_down_kernel(int32_t n, BLevel cur, BLevel nxt, int32_t *ox, int32_t *oy, int32_t *ol,
+                               int32_t *orr, int8_t *oadm, int8_t *odense, int32_t *approx,
+                               int32_t *dense) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int8_t kind = cur.kind[i], dn = cur.dn[i], reached = cur.reached[i];
+    const int32_t id = cur.id[i], x = cur.x[i], y = cur.y[i];
+    ox[id] = x;
+    oy[id] = y;
+    oadm[id] = kind == 1;
+    odense[id] = dn;
+    ol[id] = orr[id] = -1;
+    if (reached && kind == 1) {
+      approx[2 * cur.offa[i]] = x;
+      approx[2 * cur.offa[i] + 1] = y;
+    }
+    if (reached && dn) {
+      dense[2 * cur.offd[i]] = x;
+      dense[2 * cur.offd[i] + 1] = y;
+    }
+    if (kind == 0) {
+      const int32_t l = cur.child[i], j = cur.rank[i];
+      ol[id] = 1 + 2 * j;
+      orr[id] = 2 + 2 * j;
+      nxt.id[l] = 1 + 2 * j;
+      nxt.id[l + 1] = 2 + 2 * j;
+      nxt.rank[l] = j + 1;
+      nxt.rank[l + 1] = j + 1 + nxt.nint[l];
+      const int8_t go = reached && !dn;
+      nxt.reached[l] = nxt.reached[l + 1] = go;
+      nxt.offa[l] = cur.offa[i];
+      nxt.offa[l + 1] = cur.offa[i] + nxt.na[l];
+      nxt.offd[l] = cur.offd[i];
+      nxt.offd[l + 1] = cur.offd[i] + nxt.nd[l];
+    }
+  }
+}
+
 struct Buf {
   void *p = nullptr;
   ~Buf() {
@@ -409,6 +535,165 @@ int build_tree_device(const double *coords, int64_t npts, int64_t leaf, int64_t 
   return HMGPU_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// block tree, host orchestration
+// ---------------------------------------------------------------------------
+namespace {
+
+struct LevelStore {
+  Buf mem;
+  BLevel v{};
+  int32_t n = 0;
+  cudaError_t alloc(int32_t count) {
+    n = count;
+    const size_t c = static_cast<size_t>(std::max<int32_t>(count, 1));
+    const size_t bytes = c * (11 * sizeof(int32_t) + 3 * sizeof(int8_t)) + 64;
+    cudaError_t e = mem.alloc(bytes);
+    if (e != cudaSuccess) return e;
+    char *p = mem.as<char>();
+    auto i32 = [&]() {
+      int32_t *q = reinterpret_cast<int32_t *>(p);
+      p += c * sizeof(int32_t);
+      return q;
+    };
+    v.x = i32();
+    v.y = i32();
+    v.child = i32();
+    v.nint = i32();
+    v.na = i32();
+    v.nd = i32();
+    v.rank = i32();
+    v.id = i32();
+    v.offa = i32();
+    v.offd = i32();
+    i32();  // spare, keeps the byte arrays after 4-byte data
+    v.kind = reinterpret_cast<int8_t *>(p);
+    v.dn = v.kind + c;
+    v.reached = v.dn + c;
+    return cudaSuccess;
+  }
+};
+
+struct TreeDev {
+  Buf mem;
+  CNodes c{};
+  cudaError_t upload(const Tree &t) {
+    const size_t nn = t.nodes.size();
+    std::vector<double> ctr(3 * nn), rad(nn);
+    std::vector<int32_t> lr(2 * nn);
+    std::vector<int8_t> lf(nn);
+    for (size_t k = 0; k < nn; k++) {
+      const Node &q = t.nodes[k];
+      std::memcpy(&ctr[3 * k], q.center, sizeof q.center);
+      rad[k] = q.radius;
+      lr[k] = static_cast<int32_t>(q.left);
+      lr[nn + k] = static_cast<int32_t>(q.right);
+      lf[k] = q.leaf ? 1 : 0;
+    }
+    cudaError_t e = mem.alloc(nn * (4 * sizeof(double) + 2 * sizeof(int32_t) + 1));
+    if (e != cudaSuccess) return e;
+    char *p = mem.as<char>();
+    double *dc = reinterpret_cast<double *>(p), *dr = dc + 3 * nn;
+    int32_t *dl = reinterpret_cast<int32_t *>(dr + nn);
+    int8_t *df = reinterpret_cast<int8_t *>(dl + 2 * nn);
+    if ((e = cudaMemcpy(dc, ctr.data(), 3 * nn * sizeof(double), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(dr, rad.data(), nn * sizeof(double), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(dl, lr.data(), 2 * nn * sizeof(int32_t), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(df, lf.data(), nn, cudaMemcpyHostToDevice)))
+      return e;
+    c.center = dc;
+    c.radius = dr;
+    c.left = dl;
+    c.right = dl + nn;
+    c.leaf = df;
+    return cudaSuccess;
+  }
+};
+
+int grid_for(int32_t n) { return static_cast<int>(std::min<int64_t>((int64_t{n} + 255) / 256, 152 * 16)); }
+
+}  // namespace
+
+int build_blocks_device(const Tree &X, const Tree &Y, double eta, bool merge, Blocks &b) {
+  if (X.nodes.empty() || Y.nodes.empty()) return fail(HMGPU_ERR_INVALID, "empty cluster tree");
+  if (X.nodes.size() >= (size_t{1} << 30) || Y.nodes.size() >= (size_t{1} << 30))
+    return fail(HMGPU_ERR_INVALID, "cluster tree too large for the device block build");
+  TreeDev dx, dy;
+  cudaError_t e;
+  if ((e = dx.upload(X)) != cudaSuccess || (e = dy.upload(Y)) != cudaSuccess)
+    return cuda_fail(e, "uploading cluster trees");
+  Buf dctr;
+  if ((e = dctr.alloc(sizeof(int32_t))) != cudaSuccess) return cuda_fail(e, "block tree counter");
+  int32_t *counter = dctr.as<int32_t>();
+
+  std::vector<std::unique_ptr<LevelStore>> lv;
+  lv.emplace_back(new LevelStore);
+  if ((e = lv[0]->alloc(1)) != cudaSuccess) return cuda_fail(e, "block tree level");
+  {
+    const int32_t zero = 0;
+    const int8_t one = 1;
+    cudaMemcpy(lv[0]->v.x, &zero, 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(lv[0]->v.y, &zero, 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(lv[0]->v.rank, &zero, 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(lv[0]->v.id, &zero, 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(lv[0]->v.offa, &zero, 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(lv[0]->v.offd, &zero, 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(lv[0]->v.reached, &one, 1, cudaMemcpyHostToDevice);
+  }
+  int64_t total = 1;
+  for (;;) {
+    LevelStore &c = *lv.back();
+    const int64_t cap = 2 * int64_t{c.n};
+    if (total + cap >= (int64_t{1} << 31)) return fail(HMGPU_ERR_INVALID, "block tree too large for the device build");
+    std::unique_ptr<LevelStore> nx(new LevelStore);
+    if ((e = nx->alloc(static_cast<int32_t>(cap))) != cudaSuccess) return cuda_fail(e, "block tree level");
+    cudaMemset(counter, 0, sizeof(int32_t));
+    bt_level_kernel<<<grid_for(c.n), 256>>>(c.n, c.v, nx->v, dx.c, dy.c, eta, counter);
+    int32_t got = 0;
+    if ((e = cudaMemcpy(&got, counter, sizeof got, cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return cuda_fail(e, "block tree level kernel");
+    if (got == 0) break;
+    nx->n = got;
+    total += got;
+    lv.push_back(std::move(nx));
+  }
+  const int nl = static_cast<int>(lv.size());
+  BLevel none{};
+  for (int l = nl - 1; l >= 0; l--)
+    bt_up_kernel<<<grid_for(lv[l]->n), 256>>>(lv[l]->n, lv[l]->v, l + 1 < nl ? lv[l + 1]->v : none,
+                                               merge ? 1 : 0);
+  int32_t na = 0, nd = 0;
+  cudaMemcpy(&na, lv[0]->v.na, 4, cudaMemcpyDeviceToHost);
+  cudaMemcpy(&nd, lv[0]->v.nd, 4, cudaMemcpyDeviceToHost);
+  Buf out;
+  const size_t T = static_cast<size_t>(total);
+  if ((e = out.alloc(T * (4 * sizeof(int32_t) + 2) + 2 * sizeof(int32_t) * (size_t(na) + nd) + 64)) != cudaSuccess)
+    return cuda_fail(e, "block tree output");
+  int32_t *ox = out.as<int32_t>(), *oy = ox + T, *ol = oy + T, *orr = ol + T;
+  int32_t *oa = orr + T, *od = oa + 2 * size_t(na);
+  int8_t *oadm = reinterpret_cast<int8_t *>(od + 2 * size_t(nd)), *oden = oadm + T;
+  for (int l = 0; l < nl; l++)
+    bt_down_kernel<<<grid_for(lv[l]->n), 256>>>(lv[l]->n, lv[l]->v, l + 1 < nl ? lv[l + 1]->v : none, ox, oy,
+                                                 ol, orr, oadm, oden, oa, od);
+  std::vector<int32_t> hx(T), hy(T), hl(T), hr(T);
+  std::vector<int8_t> hadm(T), hden(T);
+  b.approx.resize(2 * size_t(na));
+  b.dense.resize(2 * size_t(nd));
+  if ((e = cudaMemcpy(hx.data(), ox, 4 * T, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(hy.data(), oy, 4 * T, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(hl.data(), ol, 4 * T, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(hr.data(), orr, 4 * T, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(hadm.data(), oadm, T, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(hden.data(), oden, T, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(b.approx.data(), oa, 8 * size_t(na), cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(b.dense.data(), od, 8 * size_t(nd), cudaMemcpyDeviceToHost)))
+    return cuda_fail(e, "reading the block tree back");
+  b.nodes.resize(T);
+  for (size_t k = 0; k < T; k++)
+    b.nodes[k] = BNode{hx[k], hy[k], hl[k], hr[k], hadm[k] != 0, hden[k] != 0};
+  return HMGPU_OK;
+}
 }  // namespace hm
 
 extern "C" int hmgpu_tree_build_device(const double *coords, int64_t npts, int64_t leaf, int64_t dims,
@@ -420,6 +705,26 @@ extern "C" int hmgpu_tree_build_device(const double *coords, int64_t npts, int64
   int rc;
   try {
     rc = hm::build_tree_device(coords, npts, leaf, dims, h->t);
+  } catch (const std::bad_alloc &) {
+    rc = hm::fail(HMGPU_ERR_NOMEM, "host allocation failed");
+  }
+  if (rc != HMGPU_OK) {
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_blocks_build_device(const hmgpu_tree *X, const hmgpu_tree *Y, double eta, int merge,
+                                         hmgpu_blocks **out) {
+  if (!X || !Y || !out) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  auto *h = new (std::nothrow) hmgpu_blocks;
+  if (!h) return hm::fail(HMGPU_ERR_NOMEM, "host allocation failed");
+  int rc;
+  try {
+    rc = hm::build_blocks_device(X->t, Y->t, eta, merge != 0, h->b);
   } catch (const std::bad_alloc &) {
     rc = hm::fail(HMGPU_ERR_NOMEM, "host allocation failed");
   }

@@ -130,13 +130,15 @@ class BlockTreeNode:
 
 class BlockTree:
     """BlockTree(X, Y; eta=1.5) (src/block.jl:31-44). `merge=True` also applies
-    merge_dense_matrices! (src/block.jl:98-112) as HMatrix does."""
+    merge_dense_matrices! (src/block.jl:98-112) as HMatrix does. gpu=True
+    builds the same tree (bit for bit) on the current CUDA device."""
 
-    def __init__(self, X, Y, eta=1.5, merge=False):
+    def __init__(self, X, Y, eta=1.5, merge=False, gpu=False):
         self.X, self.Y, self.eta = X, Y, eta
         L = lib()
         h = C.c_void_p()
-        check(L.hmgpu_blocks_build(X._h, Y._h, float(eta), int(bool(merge)), C.byref(h)))
+        build = L.hmgpu_blocks_build_device if gpu else L.hmgpu_blocks_build
+        check(build(X._h, Y._h, float(eta), int(bool(merge)), C.byref(h)))
         try:
             v = [C.c_int64() for _ in range(3)]
             check(L.hmgpu_blocks_counts(h, *[C.byref(x) for x in v]))

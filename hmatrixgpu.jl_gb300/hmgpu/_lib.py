@@ -60,6 +60,7 @@ SIGNATURES = {
     "hmgpu_tree_export": (C.c_int, [VP, I64P, I64P, I64P, I8P, I64P, I64P, F64P, F64P]),
     "hmgpu_tree_free": (C.c_int, [VP]),
     "hmgpu_blocks_build": (C.c_int, [VP, VP, C.c_double, C.c_int, C.POINTER(VP)]),
+    "hmgpu_blocks_build_device": (C.c_int, [VP, VP, C.c_double, C.c_int, C.POINTER(VP)]),
     "hmgpu_blocks_counts": (C.c_int, [VP, I64P, I64P, I64P]),
     "hmgpu_blocks_export": (C.c_int, [VP, I64P, I64P]),
     "hmgpu_blocks_export_nodes": (C.c_int, [VP, I64P, I64P, I8P, I8P, I64P, I64P]),

@@ -62,7 +62,7 @@ int hmgpu_abi_version(void);
 /* ---------------------------------------------------------------------- */
 /* Cluster tree: replaces ClusterTree(coords; max_points_per_leaf, dims)     */
 /* (src/tree.jl:45-137) and info(::ClusterTree) (src/tree.jl:153-187).      */
-/* Host-side, bit-exact with the reference's bisection.                     */
+/* Host or GPU build, both bit-exact with the reference's bisection.        */
 /* ---------------------------------------------------------------------- */
 typedef struct hmgpu_tree hmgpu_tree;
 
@@ -96,6 +96,12 @@ typedef struct hmgpu_blocks hmgpu_blocks;
 
 int hmgpu_blocks_build(const hmgpu_tree *X, const hmgpu_tree *Y, double eta, int merge,
                        hmgpu_blocks **out);
+/* The same block tree built on the current GPU, bit-identical to
+ * hmgpu_blocks_build: node numbers, flags, children and both traverse lists.
+ * Breadth first, then a bottom-up sweep (merge, subtree counts) and a top-down
+ * sweep that reproduces the host's pre-order numbering. */
+int hmgpu_blocks_build_device(const hmgpu_tree *X, const hmgpu_tree *Y, double eta, int merge,
+                              hmgpu_blocks **out);
 int hmgpu_blocks_counts(const hmgpu_blocks *b, int64_t *ndense, int64_t *napprox,
                         int64_t *nnodes);
 /* (target node, source node) pairs of traverse()'s direct_list / approx_list. */

@@ -1,8 +1,10 @@
-"""Cluster tree built on the GPU (hmgpu_tree_build_device) against the host
-build (hmgpu_tree_build), which follows ClusterTree (src/tree.jl:45-137).
+"""Cluster and block trees built on the GPU (hmgpu_tree_build_device,
+hmgpu_blocks_build_device) against the host builds, which follow ClusterTree
+(src/tree.jl:45-137) and BlockTree + merge + traverse (src/block.jl:31-155).
 
 The two builds must agree bit for bit: index map, ranges, children in
-pre-order, leaf flags, centers and radii; and they must fail alike."""
+pre-order, leaf flags, centers and radii; block-tree node numbers, flags,
+children and both traverse lists; and they must fail alike."""
 import ctypes as C
 import time
 
@@ -120,3 +122,46 @@ def test_device_tree_hmatrix_identical(gpu):
     Hd = hmgpu.HMatrix(K, Td, Td, eta=1.5, eps=1e-6, precision="f64")
     x = torch.randn(P.shape[1], device=gpu, dtype=torch.float64)
     assert torch.equal(Hh * x, Hd * x)
+
+
+def _same_blocks(a, b):
+    for name in ("_target", "_source", "_adm", "_dense", "_left", "_right", "_dense_pairs", "_approx_pairs"):
+        np.testing.assert_array_equal(getattr(a, name), getattr(b, name), err_msg=name)
+
+
+BLOCK_CASES = [
+    ("sphere_square", lambda: geometry.sphere(3000, seed=1), None, 32, 1.5),
+    ("cube_eta1", lambda: geometry.cube(8000, seed=2), None, 16, 1.0),
+    ("cube_eta3", lambda: geometry.cube(8000, seed=2), None, 16, 3.0),
+    ("film_lattice", lambda: geometry.film(128, 128, jitter=0.0, seed=3), None, 64, 2.0),
+    ("rect_cube_sphere", lambda: geometry.cube(5000, seed=4), lambda: geometry.sphere(3000, seed=5), 24, 1.5),
+    ("rect_small_big", lambda: geometry.cube(100, seed=6), lambda: geometry.cube(9000, seed=7), 8, 1.0),
+    ("single_leaf", lambda: geometry.cube(20, seed=8), None, 32, 1.5),
+    ("eta0", lambda: geometry.sphere(1500, seed=9), None, 16, 0.0),
+]
+
+
+@pytest.mark.parametrize("merge", [False, True])
+@pytest.mark.parametrize("name,px,py,leaf,eta", BLOCK_CASES, ids=[c[0] for c in BLOCK_CASES])
+def test_device_blocks_match_host(gpu, name, px, py, leaf, eta, merge):
+    X = hmgpu.ClusterTree(px(), max_points_per_leaf=leaf)
+    Y = X if py is None else hmgpu.ClusterTree(py(), max_points_per_leaf=leaf)
+    host = hmgpu.BlockTree(X, Y, eta=eta, merge=merge)
+    dev = hmgpu.BlockTree(X, Y, eta=eta, merge=merge, gpu=True)
+    _same_blocks(host, dev)
+
+
+def test_device_blocks_full_size(gpu):
+    """Block tree of the 2^20-point film (eta 2, merged, as the H-matrix build
+    uses it), timed beside the host build."""
+    P = geometry.film(1024, 1024, seed=1)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=64, gpu=True)
+    hmgpu.BlockTree(T, T, eta=2.0, merge=True, gpu=True)  # first use of the kernels
+    t0 = time.perf_counter()
+    dev = hmgpu.BlockTree(T, T, eta=2.0, merge=True, gpu=True)
+    t1 = time.perf_counter()
+    host = hmgpu.BlockTree(T, T, eta=2.0, merge=True)
+    t2 = time.perf_counter()
+    _same_blocks(host, dev)
+    print(f"\nblock tree of 2^20 points ({len(dev._target)} nodes): device {1e3 * (t1 - t0):.1f} ms, "
+          f"host {1e3 * (t2 - t1):.1f} ms")
