@@ -138,6 +138,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
                     const std::vector<int64_t> &v_src_off, DenseGenerator *gen) {
   const bool f64 = H.opt.precision == HMGPU_F64;
   int rc;
+  PhaseClock clk;
   if ((rc = setup_grids(H))) return rc;
   const int vec = f64 ? 2 : 4;
   make_plan(H.bs, vec, H.grid_v * (kThreads / 32), dense_src_off, u_src_off, H.plan);
@@ -150,6 +151,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   for (int64_t i = 0; i < H.bs.m; i++) t0[i] = static_cast<int32_t>(H.bs.tmap[i] - 1);
   for (int64_t j = 0; j < H.bs.n; j++) s0[j] = static_cast<int32_t>(H.bs.smap[j] - 1);
   if ((rc = upload_plan(H, t0, s0, H.bs.n))) return rc;
+  H.build_phase[4] = clk.lap();
   cudaError_t e;
 
   // pack panels
@@ -183,7 +185,12 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   H.dfree(djobs);
   H.dfree(dvj);
   H.device_bytes -= static_cast<int64_t>(p.pjobs.size() * sizeof(PackJob) + vj.size() * sizeof(VPackJob));
-  if (H.opt.precision == HMGPU_MIXED) return build_tc(H);
+  H.build_phase[5] = clk.lap();
+  if (H.opt.precision == HMGPU_MIXED) {
+    rc = build_tc(H);
+    H.build_phase[6] = clk.lap();
+    return rc;
+  }
   return HMGPU_OK;
 }
 
@@ -500,6 +507,13 @@ extern "C" int hmgpu_matvec_host(hmgpu_hmatrix *h, const void *x, void *y, int64
 // ---------------------------------------------------------------------------
 // queries
 // ---------------------------------------------------------------------------
+extern "C" int hmgpu_hmatrix_build_profile(const hmgpu_hmatrix *h, double *seconds, int32_t n) {
+  if (!h || (!seconds && n > 0)) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
+  const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);
+  for (int32_t i = 0; i < n && i < HMGPU_BUILD_PHASES; i++) seconds[i] = H.build_phase[i];
+  return HMGPU_OK;
+}
+
 extern "C" int hmgpu_hmatrix_info(const hmgpu_hmatrix *h, hmgpu_info *info) {
   if (!h || !info) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
   const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);

@@ -1,5 +1,6 @@
 // The H-matrix object behind the opaque hmgpu_hmatrix handle.
 #pragma once
+#include <chrono>
 #include <cuda_runtime.h>
 
 #include <array>
@@ -46,6 +47,7 @@ struct HMatrix {
   size_t prof_used = 0;
   int64_t prof_launches = 0;
   double build_seconds = 0.0;
+  double build_phase[HMGPU_BUILD_PHASES] = {};  // see hmgpu_hmatrix_build_profile
   int64_t aca_batches = 0, aca_reruns = 0, aca_ws_bytes = 0;
   int64_t device_bytes = 0;
   std::vector<void *> dev_allocs;
@@ -58,6 +60,17 @@ struct HMatrix {
 };
 
 int cuda_fail(cudaError_t e, const char *what);
+
+// Seconds since the previous call (the first call starts the clock).
+struct PhaseClock {
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  double lap() {
+    auto n = std::chrono::steady_clock::now();
+    double d = std::chrono::duration<double>(n - t).count();
+    t = n;
+    return d;
+  }
+};
 int setup_grids(HMatrix &H);
 int upload_units(HMatrix &H);
 int upload_plan(HMatrix &H, const std::vector<int32_t> &tmap0, const std::vector<int32_t> &smap0,

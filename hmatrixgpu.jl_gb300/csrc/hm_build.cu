@@ -556,6 +556,23 @@ struct KernelGen : DenseGenerator {
   }
 };
 
+// Gather of the kept blocks' factors from the per-batch buffers into one
+// store: one warp per copy.
+struct CopyJob {
+  const double *src;
+  double *dst;
+  int64_t n;
+};
+
+__global__ void __launch_bounds__(256) gather_kernel(const CopyJob *__restrict__ jobs, int64_t njobs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < njobs; w += warps) {
+    const CopyJob j = jobs[w];
+    for (int64_t i = lane; i < j.n; i += 32) j.dst[i] = j.src[i];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host orchestration
 // ---------------------------------------------------------------------------
@@ -757,6 +774,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   HMatrix &H = *Hp;
   H.opt = o;
   cudaGetDevice(&H.device);
+  PhaseClock clk;
   Blocks blk;
   try {
     build_blocks(X, Y, eta, true, blk);  // src/hmatrix.jl:74-78
@@ -768,6 +786,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   bs.n = n;
   bs.tmap = X.index_map;
   bs.smap = Y.index_map;
+  H.build_phase[0] = clk.lap();
 
   // device copies of the geometry and the maps
   DevBuf dX, dY, dA, dt, ds;
@@ -836,6 +855,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   C.budget = static_cast<int64_t>(std::min<size_t>(free_b / 4, size_t(16) << 30) / sizeof(double));
   C.grid = persistent_grid();
 
+  H.build_phase[1] = clk.lap();
   std::vector<AcaRes> res(na);
   std::vector<char> kept(na, 0);
   std::vector<std::unique_ptr<DevBuf>> ubufs, vbufs;
@@ -877,6 +897,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   H.aca_batches = C.batches;
   H.aca_reruns = static_cast<int64_t>(again.size());
   H.aca_ws_bytes = C.ws_bytes;
+  H.build_phase[2] = clk.lap();
 
   // block lists in the reference's order (src/hmatrix.jl:180-213)
   for (size_t d = 0; d < blk.dense.size() / 2; d++) {
@@ -917,20 +938,31 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
       (rc = H.dalloc(reinterpret_cast<void **>(&v64), vlen * 8)))
     return rc;
   {
+    std::vector<CopyJob> cj;
+    cj.reserve(2 * usrc.size());
     size_t q = 0;
     for (size_t a = 0; a < na; a++) {
       if (!kept[a]) continue;
       const int64_t r = res[a].r;
-      const int64_t ub = static_cast<int64_t>(jobs[a].m) * r * 8, vb = static_cast<int64_t>(jobs[a].n) * r * 8;
-      if (ub) cudaMemcpyAsync(u64 + usrc[q], ubufs[buf_of[a]]->as<double>() + loc_u[a], ub, cudaMemcpyDeviceToDevice);
-      if (vb) cudaMemcpyAsync(v64 + vsrc[q], vbufs[buf_of[a]]->as<double>() + loc_v[a], vb, cudaMemcpyDeviceToDevice);
+      const int64_t un = static_cast<int64_t>(jobs[a].m) * r, vn = static_cast<int64_t>(jobs[a].n) * r;
+      if (un) cj.push_back(CopyJob{ubufs[buf_of[a]]->as<double>() + loc_u[a], u64 + usrc[q], un});
+      if (vn) cj.push_back(CopyJob{vbufs[buf_of[a]]->as<double>() + loc_v[a], v64 + vsrc[q], vn});
       q++;
     }
-    cudaError_t e = cudaDeviceSynchronize();
+    DevBuf dcj;
+    if ((rc = dcj.alloc(cj.size() * sizeof(CopyJob)))) return rc;
+    cudaError_t e = cudaMemcpy(dcj.p, cj.data(), cj.size() * sizeof(CopyJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !cj.empty()) {
+      const int grid = static_cast<int>(std::min<int64_t>((static_cast<int64_t>(cj.size()) + 7) / 8, 152 * 16));
+      gather_kernel<<<grid, 256>>>(dcj.as<CopyJob>(), static_cast<int64_t>(cj.size()));
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "gathering factors");
   }
   ubufs.clear();
   vbufs.clear();
+  H.build_phase[3] = clk.lap();
   std::vector<int64_t> dsrc(bs.d_rs.size(), -1);
   KernelGen gen;
   gen.K = K;

@@ -385,6 +385,14 @@ class HMatrix:
                 "build_seconds": i.build_seconds, "aca_batches": i.aca_batches,
                 "aca_reruns": i.aca_reruns, "aca_workspace_bytes": i.aca_workspace_bytes}
 
+    BUILD_PHASES = ("block_tree", "setup", "aca", "gather", "plan", "pack", "tensor_core")
+
+    def build_profile(self):
+        """Seconds per phase of the last build (hmgpu_hmatrix_build_profile)."""
+        v = (C.c_double * len(self.BUILD_PHASES))()
+        check(lib().hmgpu_hmatrix_build_profile(self._h, v, len(self.BUILD_PHASES)))
+        return dict(zip(self.BUILD_PHASES, list(v)))
+
     def blocks(self):
         """(dense (nD, 4), approx (nA, 5)) block tables: 1-based inclusive ranges, rank last."""
         i = self._info

@@ -75,6 +75,7 @@ SIGNATURES = {
     "hmgpu_matvec_host": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64]),
     "hmgpu_matvec_noalloc": (C.c_int, [VP, VP, VP, VP]),
     "hmgpu_hmatrix_info": (C.c_int, [VP, C.POINTER(Info)]),
+    "hmgpu_hmatrix_build_profile": (C.c_int, [VP, C.POINTER(C.c_double), C.c_int32]),
     "hmgpu_hmatrix_status": (C.c_int, [VP, C.POINTER(C.c_int)]),
     "hmgpu_hmatrix_set_profiling": (C.c_int, [VP, C.c_int]),
     "hmgpu_hmatrix_phase_times": (C.c_int, [VP, F64P, I64P, I64P]),

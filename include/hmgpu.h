@@ -217,6 +217,16 @@ typedef struct {
 /* info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures. */
 int hmgpu_hmatrix_info(const hmgpu_hmatrix *H, hmgpu_info *info);
 
+/* Wall time of the phases of the last build (no counterpart in the reference;
+ * the reference's only timing hook is an @time around assembly), in seconds:
+ *   [0] block tree, [1] device copies of geometry and maps and the ACA job
+ *   list, [2] ACA + recompression, [3] block lists and the gather of the
+ *   factors, [4] product plan (host) and its upload, [5] packing of the
+ *   factors and generation of the dense blocks, [6] tensor-core copy (mixed
+ *   precision). Imports fill [4..6] only. Writes min(n, HMGPU_BUILD_PHASES). */
+#define HMGPU_BUILD_PHASES 7
+int hmgpu_hmatrix_build_profile(const hmgpu_hmatrix *H, double *seconds, int32_t n);
+
 /* Device status of the products run so far (no counterpart in the reference):
  * synchronises the device; *status = 0 if every bounded wait inside the
  * kernels completed, else the code of the first one that expired (then
