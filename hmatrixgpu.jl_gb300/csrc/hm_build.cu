@@ -3,8 +3,9 @@
 // build_matrices (src/hmatrix.jl:170-217), ACA_plus (src/aca.jl:36-106) and
 // SVD_recompress (src/aca.jl:123-143).
 //
-// One warp owns one admissible block at a time; warps take blocks from a
-// ticket counter, largest first.  The ACA follows the reference's pivot and
+// A warp owns one admissible block at a time, or a whole CTA for the large
+// blocks; teams take blocks from ticket counters, largest first. The Jacobi
+// SVD of the small k x k core runs one block per thread.  The ACA follows the reference's pivot and
 // stopping rules exactly; matrix entries and residual updates use explicitly
 // rounded FP64 operations in the reference's order, so for kernels built from
 // +,-,*,/ and sqrt the pivots match the oracle bit for bit.  The only reduction
@@ -107,47 +108,142 @@ __device__ double kentry(const KDev &K, int64_t i, int64_t j) {
 }
 
 // ---------------------------------------------------------------------------
-// warp helpers
+// teams: one block of the matrix is worked on by a warp (NT = 32) or, for the
+// large blocks, by a whole CTA (NT = kBuildThreads)
 // ---------------------------------------------------------------------------
+constexpr int kBuildThreads = 256;  // threads per CTA of the assembly kernels
+constexpr int kBuildWarps = kBuildThreads / 32;
+constexpr int64_t kTeamMinMN = 4096;  // blocks with m + n at least this get a CTA
+constexpr int kCols = 8;             // columns per pass of the QR and Q applications
+
+struct TeamScratch {  // shared memory of the CTA teams
+  double v[kCols][kBuildWarps];
+  int64_t key[kBuildWarps];
+  int idx[kBuildWarps];
+  int ticket;
+};
+
+template <int NT>
+__device__ __forceinline__ int trank() {
+  return NT == 32 ? static_cast<int>(threadIdx.x & 31) : static_cast<int>(threadIdx.x);
+}
+template <int NT>
+__device__ __forceinline__ void tsync() {
+  if (NT == 32)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
+// Team sums of NV values per thread: each value is reduced across the warp by
+// the butterfly above and then across the CTA's warps in warp order.
+template <int NT, int NV>
+__device__ __forceinline__ void tsum(double (&v)[NV], TeamScratch *sc) {
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = warp_sum(v[q]);
+  if (NT == 32) return;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();  // earlier readers of the scratch are done
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) sc->v[q][w] = v[q];
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; q++) {
+    double s = sc->v[q][0];
+    for (int u = 1; u < NT / 32; u++) s += sc->v[q][u];
+    v[q] = s;
+  }
+}
+template <int NT>
+__device__ __forceinline__ double tsum1(double x, TeamScratch *sc) {
+  double v[1] = {x};
+  tsum<NT, 1>(v, sc);
+  return v[0];
+}
+
 // Order of argmax_not_in_list (src/aca.jl:9-17): sortperm(rev=true) is stable,
 // so the largest |value| wins, NaN above all numbers, ties to the lowest index.
-__device__ __forceinline__ bool am_better(double va, int ia, double vb, int ib) {
+// Compared as integers: the bits of |value| order the numbers, every NaN maps
+// to one key above +Inf. This is a total order, so any reduction tree gives the
+// same winner.
+__device__ __forceinline__ int64_t am_key(double v) {
+  const int64_t b = __double_as_longlong(v) & 0x7fffffffffffffffll;
+  return b > 0x7ff0000000000000ll ? 0x7ff8000000000000ll : b;
+}
+__device__ __forceinline__ bool am_better(int64_t ka, int ia, int64_t kb, int ib) {
   if (ib < 0) return ia >= 0;
   if (ia < 0) return false;
-  const bool an = isnan(va), bn = isnan(vb);
-  if (an != bn) return an;
-  if (!an && va != vb) return va > vb;
+  if (ka != kb) return ka > kb;
   return ia < ib;
 }
 
-__device__ int warp_argmax_unused(const double *r, const uint8_t *used, int len) {
-  const int lane = threadIdx.x & 31;
-  double bv = 0.0;
+template <int NT>
+__device__ int team_argmax_unused(const double *r, const uint8_t *used, int len, TeamScratch *sc) {
+  int64_t bk = 0;
   int bi = -1;
-  for (int j = lane; j < len; j += 32) {
+  for (int j = trank<NT>(); j < len; j += NT) {
     if (used[j]) continue;
-    double v = fabs(r[j]);
-    if (am_better(v, j, bv, bi)) {
-      bv = v;
+    const int64_t kj = am_key(r[j]);
+    if (am_better(kj, j, bk, bi)) {
+      bk = kj;
       bi = j;
     }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    double ov = __shfl_xor_sync(0xffffffffu, bv, o);
-    int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-    if (am_better(ov, oi, bv, bi)) {
-      bv = ov;
+    const int64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (am_better(ok, oi, bk, bi)) {
+      bk = ok;
       bi = oi;
     }
   }
+  if (NT == 32) return bi;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) {
+    sc->key[w] = bk;
+    sc->idx[w] = bi;
+  }
+  __syncthreads();
+  bk = sc->key[0];
+  bi = sc->idx[0];
+  for (int u = 1; u < NT / 32; u++)
+    if (am_better(sc->key[u], sc->idx[u], bk, bi)) {
+      bk = sc->key[u];
+      bi = sc->idx[u];
+    }
   return bi;
+}
+
+// Jobs of one kernel: jobs [0, nbig) by whole CTAs, then [nbig, njobs) by
+// single warps; both from ticket counters tk[0] and tk[1], largest first.
+template <typename Big, typename Small>
+__device__ void run_teams(int nbig, int njobs, int32_t *tk, TeamScratch *sc, Big big, Small small) {
+  for (;;) {
+    if (threadIdx.x == 0) sc->ticket = atomicAdd(tk, 1);
+    __syncthreads();
+    const int j = sc->ticket;
+    __syncthreads();
+    if (j >= nbig) break;
+    big(j);
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int j = 0;
+    if (lane == 0) j = nbig + atomicAdd(tk + 1, 1);
+    j = __shfl_sync(0xffffffffu, j, 0);
+    if (j >= njobs) return;
+    small(j);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -195,308 +291,379 @@ __device__ inline WS ws_view(double *base, int m, int n, int kcap) {
   return w;
 }
 
+inline bool team_job(const AcaJob &j) { return int64_t{j.m} + j.n >= kTeamMinMN; }
+
 // ---------------------------------------------------------------------------
-// ACA+ (src/aca.jl:36-106), one warp per block
+// ACA+ (src/aca.jl:36-106), one team per block
 // ---------------------------------------------------------------------------
-__device__ void aca_warp(const KDev &K, const int32_t *tmap0, const int32_t *smap0,
-                         const AcaJob &jb, double eps, double *wsbase, AcaRes *res) {
-  const int lane = threadIdx.x & 31;
+// Residual entries K[i, j] - sum_q U[i, q] V[q, j], one term at a time
+// (:43-58); E entries per thread at once so that their dependency chains
+// interleave. `col` selects a column (fixed j, entries over i) or a row.
+template <int NT, int E, bool COL>
+__device__ __forceinline__ void residual(const KDev &K, const int32_t *trow, const int32_t *scol, const WS &w,
+                                         int m, int n, int k, int fixed, double *out) {
+  const int len = COL ? m : n;
+  const int64_t fixed_ix = COL ? scol[fixed] : trow[fixed];
+  for (int p0 = trank<NT>(); p0 < len; p0 += E * NT) {
+    double v[E];
+    int pp[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      pp[e] = min(p0 + e * NT, len - 1);
+      v[e] = COL ? kentry(K, trow[pp[e]], fixed_ix) : kentry(K, fixed_ix, scol[pp[e]]);
+    }
+    for (int q = 0; q < k; q++) {
+      if (COL) {
+        const double vq = w.V[static_cast<int64_t>(q) * n + fixed];
+        const double *uq = w.U + static_cast<int64_t>(q) * m;
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = dsub(v[e], dmul(uq[pp[e]], vq));
+      } else {
+        const double uq = w.U[fixed + static_cast<int64_t>(q) * m];
+        const double *vq = w.V + static_cast<int64_t>(q) * n;
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = dsub(v[e], dmul(uq, vq[pp[e]]));
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++)
+      if (p0 + e * NT < len) out[p0 + e * NT] = v[e];
+  }
+}
+
+template <int NT, bool COL>
+__device__ void residual_any(const KDev &K, const int32_t *trow, const int32_t *scol, const WS &w, int m, int n,
+                             int k, int fixed) {
+  const int len = COL ? m : n;
+  double *out = COL ? w.rcol : w.rrow;
+  if (len >= 4 * NT)
+    residual<NT, 4, COL>(K, trow, scol, w, m, n, k, fixed, out);
+  else if (len > NT)
+    residual<NT, 2, COL>(K, trow, scol, w, m, n, k, fixed, out);
+  else
+    residual<NT, 1, COL>(K, trow, scol, w, m, n, k, fixed, out);
+  tsync<NT>();
+}
+
+template <int NT>
+__device__ void aca_team(const KDev &K, const int32_t *tmap0, const int32_t *smap0, const AcaJob &jb,
+                         double eps, double *wsbase, AcaRes *res, TeamScratch *sc) {
+  const int t = trank<NT>();
   const int m = jb.m, n = jb.n, kcap = jb.kcap;
   WS w = ws_view(wsbase + jb.ws, m, n, kcap);
   const int32_t *trow = tmap0 + jb.rs, *scol = smap0 + jb.cs;
-  for (int j = lane; j < n; j += 32) {
+  for (int j = t; j < n; j += NT) {
     w.rrow[j] = 0.0;
     w.used_c[j] = 0;
   }
-  for (int i = lane; i < m; i += 32) {
+  for (int i = t; i < m; i += NT) {
     w.rcol[i] = 0.0;
     w.used_r[i] = 0;
   }
-  __syncwarp();
+  tsync<NT>();
   int k = 0, flags = 0;
-  // residual row I: K[I, :] - sum_q U[I, q] V[q, :], one term at a time (:43-49)
-  auto res_row = [&](int I) {
-    const int64_t ti = trow[I];
-    for (int j = lane; j < n; j += 32) {
-      double v = kentry(K, ti, scol[j]);
-      for (int q = 0; q < k; q++) v = dsub(v, dmul(w.U[I + static_cast<int64_t>(q) * m], w.V[static_cast<int64_t>(q) * n + j]));
-      w.rrow[j] = v;
-    }
-    __syncwarp();
-  };
-  // residual column J (:51-58)
-  auto res_col = [&](int J) {
-    const int64_t sj = scol[J];
-    for (int i = lane; i < m; i += 32) {
-      double v = kentry(K, trow[i], sj);
-      for (int q = 0; q < k; q++) v = dsub(v, dmul(w.U[i + static_cast<int64_t>(q) * m], w.V[static_cast<int64_t>(q) * n + J]));
-      w.rcol[i] = v;
-    }
-    __syncwarp();
-  };
   for (int it = 1; it <= jb.max_iter; it++) {
     int rp = 0, cp = 0;
     if (it > 1) {  // :72-73
-      cp = warp_argmax_unused(w.rrow, w.used_c, n);
-      rp = warp_argmax_unused(w.rcol, w.used_r, m);
+      cp = team_argmax_unused<NT>(w.rrow, w.used_c, n, sc);
+      rp = team_argmax_unused<NT>(w.rcol, w.used_r, m, sc);
     }
     const double cval = fabs(w.rrow[cp]), rval = fabs(w.rcol[rp]);
     if (rval > cval) {  // :79-82
-      res_row(rp);
-      cp = warp_argmax_unused(w.rrow, w.used_c, n);
-      res_col(cp);
+      residual_any<NT, false>(K, trow, scol, w, m, n, k, rp);
+      cp = team_argmax_unused<NT>(w.rrow, w.used_c, n, sc);
+      residual_any<NT, true>(K, trow, scol, w, m, n, k, cp);
     } else {  // :83-87
-      res_col(cp);
-      rp = warp_argmax_unused(w.rcol, w.used_r, m);
-      res_row(rp);
+      residual_any<NT, true>(K, trow, scol, w, m, n, k, cp);
+      rp = team_argmax_unused<NT>(w.rcol, w.used_r, m, sc);
+      residual_any<NT, false>(K, trow, scol, w, m, n, k, rp);
     }
     const double piv = w.rrow[cp];
     if (piv == 0.0 || !isfinite(piv)) {  // the reference would divide by zero here
       flags |= 1;
       break;
     }
-    double sv = 0.0, su = 0.0;
-    for (int j = lane; j < n; j += 32) {  // v_k = row / row[cp] (:92)
+    double s2[2] = {0.0, 0.0};  // sum(v.^2), sum(u.^2)
+    for (int j = t; j < n; j += NT) {  // v_k = row / row[cp] (:92)
       double v = ddiv(w.rrow[j], piv);
       w.V[static_cast<int64_t>(k) * n + j] = v;
-      sv = dadd(sv, dmul(v, v));
+      s2[0] = dadd(s2[0], dmul(v, v));
     }
-    for (int i = lane; i < m; i += 32) {  // u_k = col (:93)
+    for (int i = t; i < m; i += NT) {  // u_k = col (:93)
       double u = w.rcol[i];
       w.U[i + static_cast<int64_t>(k) * m] = u;
-      su = dadd(su, dmul(u, u));
+      s2[1] = dadd(s2[1], dmul(u, u));
     }
-    if (lane == 0) {
+    if (t == 0) {
       w.used_r[rp] = 1;
       w.used_c[cp] = 1;
     }
     k++;
-    sv = warp_sum(sv);
-    su = warp_sum(su);
-    __syncwarp();
-    if (sqrt(su * sv) < eps) break;  // :95-99
+    tsum<NT, 2>(s2, sc);
+    tsync<NT>();
+    if (sqrt(s2[1] * s2[0]) < eps) break;  // :95-99
     if (k == kcap && it < jb.max_iter) {
       flags |= 2;
       break;
     }
   }
-  if (lane == 0) {
+  if (t == 0) {
     res->k = k;
     res->flags = flags;
   }
 }
 
-__global__ void __launch_bounds__(256) aca_kernel(KDev K, const int32_t *__restrict__ tmap0,
-                                                  const int32_t *__restrict__ smap0,
-                                                  const AcaJob *__restrict__ jobs, int32_t njobs,
-                                                  double eps, double *ws, AcaRes *res,
-                                                  int32_t *ticket) {
-  for (;;) {
-    int j = 0;
-    if ((threadIdx.x & 31) == 0) j = atomicAdd(ticket, 1);
-    j = __shfl_sync(0xffffffffu, j, 0);
-    if (j >= njobs) return;
-    const AcaJob jb = jobs[j];
-    aca_warp(K, tmap0, smap0, jb, eps, ws, res + j);
-  }
+__global__ void __launch_bounds__(kBuildThreads, 3) aca_kernel(KDev K, const int32_t *__restrict__ tmap0,
+                                                            const int32_t *__restrict__ smap0,
+                                                            const AcaJob *__restrict__ jobs, int32_t nbig,
+                                                            int32_t njobs, double eps, double *ws, AcaRes *res,
+                                                            int32_t *ticket) {
+  __shared__ TeamScratch sc;
+  run_teams(
+      nbig, njobs, ticket, &sc,
+      [&](int j) { aca_team<kBuildThreads>(K, tmap0, smap0, jobs[j], eps, ws, res + j, &sc); },
+      [&](int j) { aca_team<32>(K, tmap0, smap0, jobs[j], eps, ws, res + j, &sc); });
 }
 
 // ---------------------------------------------------------------------------
-// QR + SVD recompression (src/aca.jl:123-143), one warp per block
+// QR + SVD recompression (src/aca.jl:123-143)
 // ---------------------------------------------------------------------------
 // Householder QR (LAPACK dgeqr2 conventions) of A (rows x cols, column-major,
-// leading dimension ld), in place; tau[j] per reflector.
-__device__ void warp_qr(double *A, int64_t ld, int rows, int cols, double *tau) {
-  const int lane = threadIdx.x & 31;
+// leading dimension ld), in place; tau[j] per reflector. The trailing columns
+// are updated kCols at a time (their dot products reduced together).
+template <int NT>
+__device__ void team_qr(double *A, int64_t ld, int rows, int cols, double *tau, TeamScratch *sc) {
+  const int t = trank<NT>();
   for (int j = 0; j < cols; j++) {
     double *x = A + j + j * ld;
     const int len = rows - j;
     double s = 0.0;
-    for (int i = 1 + lane; i < len; i += 32) s += x[i] * x[i];
-    const double xn = sqrt(warp_sum(s));
+    for (int i = 1 + t; i < len; i += NT) s += x[i] * x[i];
+    const double xn = sqrt(tsum1<NT>(s, sc));
     const double alpha = x[0];
-    double t = 0.0;
+    double tj = 0.0;
     if (xn != 0.0) {
       const double beta = -copysign(sqrt(alpha * alpha + xn * xn), alpha);
-      t = (beta - alpha) / beta;
-      const double sc = 1.0 / (alpha - beta);
-      for (int i = 1 + lane; i < len; i += 32) x[i] *= sc;
-      __syncwarp();
-      if (lane == 0) x[0] = beta;
+      tj = (beta - alpha) / beta;
+      const double scl = 1.0 / (alpha - beta);
+      for (int i = 1 + t; i < len; i += NT) x[i] *= scl;
+      tsync<NT>();
+      if (t == 0) x[0] = beta;
     }
-    if (lane == 0) tau[j] = t;
-    __syncwarp();
-    for (int c = j + 1; c < cols; c++) {
-      double *y = A + j + c * ld;
-      double d = 0.0;
-      for (int i = 1 + lane; i < len; i += 32) d += x[i] * y[i];
-      const double wv = (warp_sum(d) + y[0]) * t;
-      for (int i = 1 + lane; i < len; i += 32) y[i] -= wv * x[i];
-      __syncwarp();
-      if (lane == 0) y[0] -= wv;
-      __syncwarp();
+    if (t == 0) tau[j] = tj;
+    tsync<NT>();
+    for (int c0 = j + 1; c0 < cols; c0 += kCols) {
+      const int nc = min(kCols, cols - c0);
+      double *y0 = A + j + c0 * ld;
+      double d[kCols];
+#pragma unroll
+      for (int q = 0; q < kCols; q++) d[q] = 0.0;
+      for (int i = 1 + t; i < len; i += NT) {
+        const double xi = x[i];
+#pragma unroll
+        for (int q = 0; q < kCols; q++)
+          if (q < nc) d[q] += xi * y0[i + q * ld];
+      }
+      tsum<NT, kCols>(d, sc);
+      double wv[kCols];
+#pragma unroll
+      for (int q = 0; q < kCols; q++) wv[q] = q < nc ? (d[q] + y0[q * ld]) * tj : 0.0;
+      for (int i = 1 + t; i < len; i += NT) {
+        const double xi = x[i];
+#pragma unroll
+        for (int q = 0; q < kCols; q++)
+          if (q < nc) y0[i + q * ld] -= wv[q] * xi;
+      }
+      tsync<NT>();
+      if (t == 0)
+        for (int q = 0; q < nc; q++) y0[q * ld] -= wv[q];
+      tsync<NT>();
     }
   }
 }
 
-// y (length rows) := Q y with Q's reflectors in QR (rows x cols, ld) and tau.
-__device__ void warp_apply_q(const double *QR, int64_t ld, int rows, int cols, const double *tau,
-                             double *y) {
-  const int lane = threadIdx.x & 31;
-  for (int j = cols - 1; j >= 0; j--) {
-    const double *x = QR + j + j * ld;
-    double *yy = y + j;
-    const int len = rows - j;
-    double d = 0.0;
-    for (int i = 1 + lane; i < len; i += 32) d += x[i] * yy[i];
-    const double wv = (warp_sum(d) + yy[0]) * tau[j];
-    for (int i = 1 + lane; i < len; i += 32) yy[i] -= wv * x[i];
-    __syncwarp();
-    if (lane == 0) yy[0] -= wv;
-    __syncwarp();
+// QR of both factors and M = RU * RV' (k x k column-major), Z = I.
+template <int NT>
+__device__ void qr_team(const AcaJob &jb, const AcaRes &rs, int svd, double *ws, TeamScratch *sc) {
+  const int k = rs.k;
+  if (!svd || k == 0) return;
+  const int t = trank<NT>();
+  WS w = ws_view(ws + jb.ws, jb.m, jb.n, jb.kcap);
+  const int m = jb.m, n = jb.n;
+  team_qr<NT>(w.U, m, m, k, w.tauU, sc);  // qr(U) (:125)
+  team_qr<NT>(w.V, n, n, k, w.tauV, sc);  // qr(V') (:126): V row-major k x n == V' column-major
+  for (int e = t; e < k * k; e += NT) {   // M = RU * RV' (:129)
+    const int r = e % k, c = e / k;
+    double s = 0.0;
+    for (int q = max(r, c); q < k; q++) s += w.U[r + static_cast<int64_t>(q) * m] * w.V[c + static_cast<int64_t>(q) * n];
+    w.M[r + c * k] = s;
+    w.Z[r + c * k] = r == c ? 1.0 : 0.0;
   }
+  tsync<NT>();
 }
 
-__global__ void __launch_bounds__(256) recompress_kernel(const AcaJob *__restrict__ jobs,
-                                                         int32_t njobs, double eps, int svd,
-                                                         double *ws, AcaRes *res, int32_t *ticket) {
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    int jj = 0;
-    if (lane == 0) jj = atomicAdd(ticket, 1);
-    jj = __shfl_sync(0xffffffffu, jj, 0);
-    if (jj >= njobs) return;
-    const AcaJob jb = jobs[jj];
-    const int k = res[jj].k;
-    if (!svd || k == 0) {
-      if (lane == 0) res[jj].r = k;
-      continue;
-    }
-    WS w = ws_view(ws + jb.ws, jb.m, jb.n, jb.kcap);
-    const int m = jb.m, n = jb.n;
-    warp_qr(w.U, m, m, k, w.tauU);  // qr(U) (:125)
-    warp_qr(w.V, n, n, k, w.tauV);  // qr(V') (:126): V row-major k x n == V' column-major
-    // M = RU * RV' (:129), k x k column-major
-    for (int e = lane; e < k * k; e += 32) {
-      const int r = e % k, c = e / k;
-      double s = 0.0;
-      for (int q = max(r, c); q < k; q++)
-        s += w.U[r + static_cast<int64_t>(q) * m] * w.V[c + static_cast<int64_t>(q) * n];
-      w.M[r + c * k] = s;
-      w.Z[r + c * k] = r == c ? 1.0 : 0.0;
-    }
-    __syncwarp();
-    // one-sided Jacobi: rotate column pairs of M until orthogonal; Z collects
-    // the rotations, so M Z_0 = W Sigma with the columns of M = W Sigma.
-    int converged = 0;
-    for (int sweep = 0; sweep < 80 && !converged; sweep++) {
-      int rotated = 0;
-      for (int p = 0; p < k - 1; p++)
-        for (int q = p + 1; q < k; q++) {
-          double a = 0.0, b = 0.0, g = 0.0;
-          for (int i = lane; i < k; i += 32) {
-            const double u = w.M[i + p * k], v = w.M[i + q * k];
-            a += u * u;
-            b += v * v;
-            g += u * v;
-          }
-          a = warp_sum(a);
-          b = warp_sum(b);
-          g = warp_sum(g);
-          if (g == 0.0 || fabs(g) <= 1e-15 * sqrt(a * b)) continue;
-          rotated = 1;
-          const double zeta = (b - a) / (2.0 * g);
-          const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-          for (int i = lane; i < k; i += 32) {
-            const double u = w.M[i + p * k], v = w.M[i + q * k];
-            w.M[i + p * k] = c * u - s * v;
-            w.M[i + q * k] = s * u + c * v;
-            const double zu = w.Z[i + p * k], zv = w.Z[i + q * k];
-            w.Z[i + p * k] = c * zu - s * zv;
-            w.Z[i + q * k] = s * zu + c * zv;
-          }
-          __syncwarp();
+__global__ void __launch_bounds__(kBuildThreads) qr_kernel(const AcaJob *__restrict__ jobs, int32_t nbig,
+                                                           int32_t njobs, int svd, double *ws,
+                                                           const AcaRes *res, int32_t *ticket) {
+  __shared__ TeamScratch sc;
+  run_teams(
+      nbig, njobs, ticket, &sc, [&](int j) { qr_team<kBuildThreads>(jobs[j], res[j], svd, ws, &sc); },
+      [&](int j) { qr_team<32>(jobs[j], res[j], svd, ws, &sc); });
+}
+
+// One-sided (Hestenes) Jacobi SVD of M, one thread per block: columns of M
+// rotated into W*Sigma, Z collects the rotations; then the singular values in
+// decreasing order and the truncation rank from the tail norms (:130-136).
+__global__ void __launch_bounds__(kBuildThreads) jacobi_kernel(const AcaJob *__restrict__ jobs, int32_t njobs,
+                                                               double eps, int svd, double *ws, AcaRes *res) {
+  const int jj = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jj >= njobs) return;
+  const int k = res[jj].k;
+  if (!svd || k == 0) {
+    res[jj].r = k;
+    return;
+  }
+  const AcaJob jb = jobs[jj];
+  WS w = ws_view(ws + jb.ws, jb.m, jb.n, jb.kcap);
+  double *M = w.M, *Z = w.Z;
+  int converged = 0;
+  for (int sweep = 0; sweep < 80 && !converged; sweep++) {
+    int rotated = 0;
+    for (int p = 0; p < k - 1; p++)
+      for (int q = p + 1; q < k; q++) {
+        double *mp = M + p * k, *mq = M + q * k;
+        double a = 0.0, b = 0.0, g = 0.0;
+        for (int i = 0; i < k; i++) {
+          const double u = mp[i], v = mq[i];
+          a += u * u;
+          b += v * v;
+          g += u * v;
         }
-      converged = !rotated;
-    }
-    for (int j = 0; j < k; j++) {
-      double s = 0.0;
-      for (int i = lane; i < k; i += 32) s += w.M[i + j * k] * w.M[i + j * k];
-      s = warp_sum(s);
-      if (lane == 0) w.sig[j] = sqrt(s);
-    }
-    __syncwarp();
-    if (lane == 0) {
-      for (int j = 0; j < k; j++) w.ord[j] = j;
-      for (int i = 1; i < k; i++) {  // stable, decreasing sigma
-        int v = w.ord[i], j = i - 1;
-        while (j >= 0 && w.sig[w.ord[j]] < w.sig[v]) {
-          w.ord[j + 1] = w.ord[j];
-          j--;
+        if (g == 0.0 || fabs(g) <= 1e-15 * sqrt(a * b)) continue;
+        rotated = 1;
+        const double zeta = (b - a) / (2.0 * g);
+        const double tt = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + tt * tt), s = c * tt;
+        double *zp = Z + p * k, *zq = Z + q * k;
+        for (int i = 0; i < k; i++) {
+          const double u = mp[i], v = mq[i];
+          mp[i] = c * u - s * v;
+          mq[i] = s * u + c * v;
+          const double zu = zp[i], zv = zq[i];
+          zp[i] = c * zu - s * zv;
+          zq[i] = s * zu + c * zv;
         }
-        w.ord[j + 1] = v;
       }
-      // tail norms accumulated from the smallest singular value (:132-136);
-      // they grow as i falls, so the first i with tail < eps is where the
-      // downward scan last sees tail < eps.
-      int r = k;
-      double acc = 0.0;
-      for (int i = k - 1; i >= 0; i--) {
-        acc += w.sig[w.ord[i]] * w.sig[w.ord[i]];
-        if (sqrt(acc) < eps)
-          r = i;
-        else
-          break;
-      }
-      res[jj].r = r;
-      if (!converged) res[jj].flags |= 4;
+    converged = !rotated;
+  }
+  for (int j = 0; j < k; j++) {
+    double s = 0.0;
+    for (int i = 0; i < k; i++) s += M[i + j * k] * M[i + j * k];
+    w.sig[j] = sqrt(s);
+    w.ord[j] = j;
+  }
+  for (int i = 1; i < k; i++) {  // stable, decreasing sigma
+    const int v = w.ord[i];
+    int j = i - 1;
+    while (j >= 0 && w.sig[w.ord[j]] < w.sig[v]) {
+      w.ord[j + 1] = w.ord[j];
+      j--;
     }
-    __syncwarp();
+    w.ord[j + 1] = v;
+  }
+  // tail norms accumulated from the smallest singular value (:132-136); they
+  // grow as i falls, so the first i with tail < eps is where the downward scan
+  // last sees tail < eps.
+  int r = k;
+  double acc = 0.0;
+  for (int i = k - 1; i >= 0; i--) {
+    acc += w.sig[w.ord[i]] * w.sig[w.ord[i]];
+    if (sqrt(acc) < eps)
+      r = i;
+    else
+      break;
+  }
+  res[jj].r = r;
+  if (!converged) res[jj].flags |= 4;
+}
+
+// out(i, c) for c < r := (Q [C(:, ord[c]); 0])(i) with Q's k reflectors in QR
+// (rows x k, ld) and tau; C is k x k (ldc); out(i, c) lives at out[i*si + c*scs].
+// kCols output columns per pass.
+template <int NT>
+__device__ void team_apply_q(const double *QR, int64_t ld, int rows, int k, const double *tau, const double *C,
+                             const int32_t *ord, int r, double *out, int64_t si, int64_t scs, TeamScratch *sc) {
+  const int t = trank<NT>();
+  for (int c0 = 0; c0 < r; c0 += kCols) {
+    const int nc = min(kCols, r - c0);
+    double *o = out + c0 * scs;
+    for (int i = t; i < rows; i += NT)
+#pragma unroll
+      for (int q = 0; q < kCols; q++)
+        if (q < nc) o[i * si + q * scs] = i < k ? C[i + ord[c0 + q] * k] : 0.0;
+    tsync<NT>();
+    for (int j = k - 1; j >= 0; j--) {
+      const double *x = QR + j + j * ld;
+      const int len = rows - j;
+      double *y0 = o + j * si;
+      double d[kCols];
+#pragma unroll
+      for (int q = 0; q < kCols; q++) d[q] = 0.0;
+      for (int i = 1 + t; i < len; i += NT) {
+        const double xi = x[i];
+#pragma unroll
+        for (int q = 0; q < kCols; q++)
+          if (q < nc) d[q] += xi * y0[i * si + q * scs];
+      }
+      tsum<NT, kCols>(d, sc);
+      double wv[kCols];
+#pragma unroll
+      for (int q = 0; q < kCols; q++) wv[q] = q < nc ? (d[q] + y0[q * scs]) * tau[j] : 0.0;
+      for (int i = 1 + t; i < len; i += NT) {
+        const double xi = x[i];
+#pragma unroll
+        for (int q = 0; q < kCols; q++)
+          if (q < nc) y0[i * si + q * scs] -= wv[q] * xi;
+      }
+      tsync<NT>();
+      if (t == 0)
+        for (int q = 0; q < nc; q++) y0[q * scs] -= wv[q];
+      tsync<NT>();
+    }
   }
 }
 
-// Writes the final factors of block jj row-major: U' (m x r) at uo, V' (r x n) at vo.
-__global__ void __launch_bounds__(256) form_kernel(const AcaJob *__restrict__ jobs, int32_t njobs,
-                                                   int svd, double *ws, const AcaRes *res,
-                                                   const int64_t *uo, const int64_t *vo,
-                                                   double *ustore, double *vstore, int32_t *ticket) {
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    int jj = 0;
-    if (lane == 0) jj = atomicAdd(ticket, 1);
-    jj = __shfl_sync(0xffffffffu, jj, 0);
-    if (jj >= njobs) return;
-    if (uo[jj] < 0) continue;  // block stored dense
-    const AcaJob jb = jobs[jj];
-    const int m = jb.m, n = jb.n, k = res[jj].k, r = res[jj].r;
-    WS w = ws_view(ws + jb.ws, m, n, jb.kcap);
-    double *U = ustore + uo[jj], *V = vstore + vo[jj];
-    if (!svd) {
-      for (int64_t e = lane; e < static_cast<int64_t>(m) * k; e += 32) {
-        const int64_t i = e / k, q = e - i * k;
-        U[e] = w.U[i + q * m];
-      }
-      for (int64_t e = lane; e < static_cast<int64_t>(k) * n; e += 32) V[e] = w.V[e];
-      continue;
+// Final factors of one block, row-major: U' (m x r) at uo, V' (r x n) at vo.
+template <int NT>
+__device__ void form_team(const AcaJob &jb, const AcaRes &rs, int svd, double *ws, int64_t uo, int64_t vo,
+                          double *ustore, double *vstore, TeamScratch *sc) {
+  if (uo < 0) return;  // block stored dense
+  const int t = trank<NT>();
+  const int m = jb.m, n = jb.n, k = rs.k, r = rs.r;
+  WS w = ws_view(ws + jb.ws, m, n, jb.kcap);
+  double *U = ustore + uo, *V = vstore + vo;
+  if (!svd) {
+    for (int64_t e = t; e < static_cast<int64_t>(m) * k; e += NT) {
+      const int64_t i = e / k, q = e - i * k;
+      U[e] = w.U[i + q * m];
     }
-    for (int c = 0; c < r; c++) {  // U' = QU * (W_r Sigma_r) (:139)
-      const int src = w.ord[c];
-      for (int i = lane; i < m; i += 32) w.rcol[i] = i < k ? w.M[i + src * k] : 0.0;
-      __syncwarp();
-      warp_apply_q(w.U, m, m, k, w.tauU, w.rcol);
-      for (int i = lane; i < m; i += 32) U[static_cast<int64_t>(i) * r + c] = w.rcol[i];
-      __syncwarp();
-    }
-    for (int c = 0; c < r; c++) {  // V' = Z_r' * QV' (:140)
-      const int src = w.ord[c];
-      for (int i = lane; i < n; i += 32) w.rrow[i] = i < k ? w.Z[i + src * k] : 0.0;
-      __syncwarp();
-      warp_apply_q(w.V, n, n, k, w.tauV, w.rrow);
-      for (int i = lane; i < n; i += 32) V[static_cast<int64_t>(c) * n + i] = w.rrow[i];
-      __syncwarp();
-    }
+    for (int64_t e = t; e < static_cast<int64_t>(k) * n; e += NT) V[e] = w.V[e];
+    return;
   }
+  team_apply_q<NT>(w.U, m, m, k, w.tauU, w.M, w.ord, r, U, r, 1, sc);  // U' = QU * (W_r Sigma_r) (:139)
+  team_apply_q<NT>(w.V, n, n, k, w.tauV, w.Z, w.ord, r, V, 1, n, sc);  // V' = Z_r' * QV' (:140)
+}
+
+__global__ void __launch_bounds__(kBuildThreads) form_kernel(const AcaJob *__restrict__ jobs, int32_t nbig,
+                                                             int32_t njobs, int svd, double *ws,
+                                                             const AcaRes *res, const int64_t *uo,
+                                                             const int64_t *vo, double *ustore, double *vstore,
+                                                             int32_t *ticket) {
+  __shared__ TeamScratch sc;
+  run_teams(
+      nbig, njobs, ticket, &sc,
+      [&](int j) { form_team<kBuildThreads>(jobs[j], res[j], svd, ws, uo[j], vo[j], ustore, vstore, &sc); },
+      [&](int j) { form_team<32>(jobs[j], res[j], svd, ws, uo[j], vo[j], ustore, vstore, &sc); });
 }
 
 // Dense blocks generated straight into the product layout (kind-2 pack jobs).
@@ -598,11 +765,13 @@ struct DevBuf {
   }
 };
 
-static int persistent_grid() {
+// Resident CTAs of a persistent assembly kernel on the whole device.
+template <typename F>
+static int persistent_grid(F kernel) {
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, aca_kernel, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kBuildThreads, 0);
   return std::max(1, sms) * std::max(1, occ);
 }
 
@@ -619,7 +788,7 @@ struct Compressor {
   double eps_aca, eps_svd;
   int svd;
   int64_t budget;  // doubles of workspace per batch
-  int grid;
+  int grid_aca = 1, grid_qr = 1, grid_form = 1;
   int64_t batches = 0, ws_bytes = 0;  // statistics of all run() calls
 
   // Processes jobs[idx] for idx in `sel`, writing results into res (indexed like jobs).
@@ -630,7 +799,7 @@ struct Compressor {
           Keep keep, Place place) {
     size_t pos = 0;
     DevBuf ws, djobs, dres, dtick, duo, dvo;
-    if (int rc = dtick.alloc(4 * sizeof(int32_t))) return rc;
+    if (int rc = dtick.alloc(8 * sizeof(int32_t))) return rc;
     while (pos < sel.size()) {
       std::vector<AcaJob> batch;
       std::vector<int> ids;
@@ -645,7 +814,24 @@ struct Compressor {
         ids.push_back(sel[pos]);
         pos++;
       }
+      // blocks worked on by whole CTAs first (the kernels take them before the rest)
+      {
+        std::vector<AcaJob> b2;
+        std::vector<int> i2;
+        b2.reserve(batch.size());
+        i2.reserve(ids.size());
+        for (int pass = 0; pass < 2; pass++)
+          for (size_t q = 0; q < batch.size(); q++)
+            if (team_job(batch[q]) == (pass == 0)) {
+              b2.push_back(batch[q]);
+              i2.push_back(ids[q]);
+            }
+        batch.swap(b2);
+        ids.swap(i2);
+      }
       const int nb = static_cast<int>(batch.size());
+      int nbig = 0;
+      while (nbig < nb && team_job(batch[nbig])) nbig++;
       batches++;
       ws_bytes += used * static_cast<int64_t>(sizeof(double));
       int rc;
@@ -654,12 +840,14 @@ struct Compressor {
         return rc;
       cudaMemcpy(djobs.p, batch.data(), nb * sizeof(AcaJob), cudaMemcpyHostToDevice);
       cudaMemset(dres.p, 0, nb * sizeof(AcaRes));
-      cudaMemset(dtick.p, 0, 4 * sizeof(int32_t));
+      cudaMemset(dtick.p, 0, 8 * sizeof(int32_t));
       int32_t *tk = dtick.as<int32_t>();
-      aca_kernel<<<grid, 256>>>(K, tmap0, smap0, djobs.as<AcaJob>(), nb, eps_aca, ws.as<double>(),
-                                dres.as<AcaRes>(), tk);
-      recompress_kernel<<<grid, 256>>>(djobs.as<AcaJob>(), nb, eps_svd, svd, ws.as<double>(),
-                                       dres.as<AcaRes>(), tk + 1);
+      aca_kernel<<<grid_aca, kBuildThreads>>>(K, tmap0, smap0, djobs.as<AcaJob>(), nbig, nb, eps_aca,
+                                          ws.as<double>(), dres.as<AcaRes>(), tk);
+      qr_kernel<<<grid_qr, kBuildThreads>>>(djobs.as<AcaJob>(), nbig, nb, svd, ws.as<double>(), dres.as<AcaRes>(),
+                                         tk + 2);
+      jacobi_kernel<<<(nb + kBuildThreads - 1) / kBuildThreads, kBuildThreads>>>(
+          djobs.as<AcaJob>(), nb, eps_svd, svd, ws.as<double>(), dres.as<AcaRes>());
       std::vector<AcaRes> hr(nb);
       cudaError_t e = cudaMemcpy(hr.data(), dres.p, nb * sizeof(AcaRes), cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) return cuda_fail(e, "ACA / recompression kernels");
@@ -679,8 +867,8 @@ struct Compressor {
       if ((rc = duo.alloc(nb * sizeof(int64_t))) || (rc = dvo.alloc(nb * sizeof(int64_t)))) return rc;
       cudaMemcpy(duo.p, uo.data(), nb * sizeof(int64_t), cudaMemcpyHostToDevice);
       cudaMemcpy(dvo.p, vo.data(), nb * sizeof(int64_t), cudaMemcpyHostToDevice);
-      form_kernel<<<grid, 256>>>(djobs.as<AcaJob>(), nb, svd, ws.as<double>(), dres.as<AcaRes>(),
-                                 duo.as<int64_t>(), dvo.as<int64_t>(), ust, vst, tk + 2);
+      form_kernel<<<grid_form, kBuildThreads>>>(djobs.as<AcaJob>(), nbig, nb, svd, ws.as<double>(), dres.as<AcaRes>(),
+                                           duo.as<int64_t>(), dvo.as<int64_t>(), ust, vst, tk + 4);
       e = cudaDeviceSynchronize();
       if (e != cudaSuccess) return cuda_fail(e, "factor formation");
     }
@@ -853,7 +1041,9 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   C.eps_svd = eps;         // src/hmatrix.jl:198
   C.svd = svd_recompress ? 1 : 0;
   C.budget = static_cast<int64_t>(std::min<size_t>(free_b / 4, size_t(16) << 30) / sizeof(double));
-  C.grid = persistent_grid();
+  C.grid_aca = persistent_grid(aca_kernel);
+  C.grid_qr = persistent_grid(qr_kernel);
+  C.grid_form = persistent_grid(form_kernel);
 
   H.build_phase[1] = clk.lap();
   std::vector<AcaRes> res(na);
@@ -1010,8 +1200,8 @@ extern "C" int hmgpu_aca_plus(const double *A, int64_t lda, int64_t m, int64_t n
   cudaMemset(dr.p, 0, sizeof(AcaRes));
   cudaMemset(dtk.p, 0, 16);
   KDev K{HMGPU_KERNEL_EXPLICIT, nullptr, nullptr, dA.as<double>(), lda};
-  aca_kernel<<<1, 32>>>(K, dt.as<int32_t>(), ds.as<int32_t>(), dj.as<AcaJob>(), 1, eps,
-                        dws.as<double>(), dr.as<AcaRes>(), dtk.as<int32_t>());
+  aca_kernel<<<1, kBuildThreads>>>(K, dt.as<int32_t>(), ds.as<int32_t>(), dj.as<AcaJob>(), team_job(j) ? 1 : 0, 1,
+                                   eps, dws.as<double>(), dr.as<AcaRes>(), dtk.as<int32_t>());
   AcaRes r;
   cudaError_t e = cudaMemcpy(&r, dr.p, sizeof r, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "ACA kernel");
@@ -1054,10 +1244,12 @@ extern "C" int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const doubl
   int64_t zero = 0;
   cudaMemcpy(duo.p, &zero, 8, cudaMemcpyHostToDevice);
   cudaMemcpy(dvo.p, &zero, 8, cudaMemcpyHostToDevice);
-  recompress_kernel<<<1, 32>>>(dj.as<AcaJob>(), 1, eps, 1, dws.as<double>(), dr.as<AcaRes>(),
-                               dtk.as<int32_t>());
-  form_kernel<<<1, 32>>>(dj.as<AcaJob>(), 1, 1, dws.as<double>(), dr.as<AcaRes>(), duo.as<int64_t>(),
-                         dvo.as<int64_t>(), dus.as<double>(), dvs.as<double>(), dtk.as<int32_t>() + 1);
+  const int big = team_job(j) ? 1 : 0;
+  qr_kernel<<<1, kBuildThreads>>>(dj.as<AcaJob>(), big, 1, 1, dws.as<double>(), dr.as<AcaRes>(), dtk.as<int32_t>());
+  jacobi_kernel<<<1, 32>>>(dj.as<AcaJob>(), 1, eps, 1, dws.as<double>(), dr.as<AcaRes>());
+  form_kernel<<<1, kBuildThreads>>>(dj.as<AcaJob>(), big, 1, 1, dws.as<double>(), dr.as<AcaRes>(),
+                                    duo.as<int64_t>(), dvo.as<int64_t>(), dus.as<double>(), dvs.as<double>(),
+                                    dtk.as<int32_t>() + 2);
   AcaRes r;
   cudaError_t e = cudaMemcpy(&r, dr.p, sizeof r, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "recompression kernels");

@@ -39,6 +39,25 @@ def test_aca_plus_known_answer_and_oracle(gpu):
     np.testing.assert_allclose(Us @ Vs, Uso @ Vso, rtol=0, atol=1e-13 * np.abs(blk).max())
 
 
+def test_aca_plus_large_block_cta_team(gpu):
+    """A block large enough (m + n >= 4096) to be worked on by a whole CTA:
+    pivots, factors and the recompressed product equal the oracle's."""
+    rng = np.random.default_rng(21)
+    X = rng.random((3000, 3))
+    Y = rng.random((2500, 3)) + np.array([3.0, 0.5, 0.0])
+    blk = 1.0 / np.linalg.norm(X[:, None, :] - Y[None, :, :], axis=2)
+    eps = 1e-7
+    U, V = hmgpu.ACA_plus(3000, 2500, lambda I: blk[I - 1, :], lambda J: blk[:, J - 1], eps)
+    Uo, Vo = O.aca_plus(O.Kernel("explicit", A=blk), np.arange(1, 3001), np.arange(1, 2501), eps)
+    assert U.shape == Uo.shape and 5 < U.shape[1] < 60
+    np.testing.assert_array_equal(U, Uo)
+    np.testing.assert_array_equal(V, Vo)
+    Us, Vs = hmgpu.SVD_recompress(U, V, eps * 10)
+    Uso, Vso = O.svd_recompress(U, V, eps * 10)
+    assert Us.shape == Uso.shape
+    np.testing.assert_allclose(Us @ Vs, Uso @ Vso, rtol=0, atol=1e-12 * np.abs(blk).max())
+
+
 def test_svd_recompress_random(gpu):
     rng = np.random.default_rng(5)
     for m, n, k, eps in [(50, 40, 9, 1e-3), (7, 90, 7, 0.0), (64, 64, 30, 1e-8)]:
