@@ -428,6 +428,52 @@ __global__ void __launch_bounds__(kBuildThreads, 3) aca_kernel(KDev K, const int
 // ---------------------------------------------------------------------------
 // QR + SVD recompression (src/aca.jl:123-143)
 // ---------------------------------------------------------------------------
+// Applies the reflector I - tau v v' (v = [1; x[1..len)]) to NC columns:
+// entry i of column q at y0[i*si + q*scs]. The NC dot products are reduced
+// together, each exactly as a single one would be.
+template <int NT, int NC>
+__device__ __forceinline__ void reflect_cols(const double *x, int len, double tau, double *y0, int64_t si,
+                                             int64_t scs, TeamScratch *sc) {
+  const int t = trank<NT>();
+  double d[NC];
+#pragma unroll
+  for (int q = 0; q < NC; q++) d[q] = 0.0;
+  for (int i = 1 + t; i < len; i += NT) {
+    const double xi = x[i];
+#pragma unroll
+    for (int q = 0; q < NC; q++) d[q] += xi * y0[i * si + q * scs];
+  }
+  tsum<NT, NC>(d, sc);
+  double wv[NC];
+#pragma unroll
+  for (int q = 0; q < NC; q++) wv[q] = (d[q] + y0[q * scs]) * tau;
+  for (int i = 1 + t; i < len; i += NT) {
+    const double xi = x[i];
+#pragma unroll
+    for (int q = 0; q < NC; q++) y0[i * si + q * scs] -= wv[q] * xi;
+  }
+  tsync<NT>();
+  if (t == 0)
+#pragma unroll
+    for (int q = 0; q < NC; q++) y0[q * scs] -= wv[q];
+  tsync<NT>();
+}
+
+template <int NT>
+__device__ void reflect_any(int nc, const double *x, int len, double tau, double *y0, int64_t si, int64_t scs,
+                            TeamScratch *sc) {
+  switch (nc) {
+    case 1: reflect_cols<NT, 1>(x, len, tau, y0, si, scs, sc); break;
+    case 2: reflect_cols<NT, 2>(x, len, tau, y0, si, scs, sc); break;
+    case 3: reflect_cols<NT, 3>(x, len, tau, y0, si, scs, sc); break;
+    case 4: reflect_cols<NT, 4>(x, len, tau, y0, si, scs, sc); break;
+    case 5: reflect_cols<NT, 5>(x, len, tau, y0, si, scs, sc); break;
+    case 6: reflect_cols<NT, 6>(x, len, tau, y0, si, scs, sc); break;
+    case 7: reflect_cols<NT, 7>(x, len, tau, y0, si, scs, sc); break;
+    default: reflect_cols<NT, 8>(x, len, tau, y0, si, scs, sc); break;
+  }
+}
+
 // Householder QR (LAPACK dgeqr2 conventions) of A (rows x cols, column-major,
 // leading dimension ld), in place; tau[j] per reflector. The trailing columns
 // are updated kCols at a time (their dot products reduced together).
@@ -452,33 +498,8 @@ __device__ void team_qr(double *A, int64_t ld, int rows, int cols, double *tau, 
     }
     if (t == 0) tau[j] = tj;
     tsync<NT>();
-    for (int c0 = j + 1; c0 < cols; c0 += kCols) {
-      const int nc = min(kCols, cols - c0);
-      double *y0 = A + j + c0 * ld;
-      double d[kCols];
-#pragma unroll
-      for (int q = 0; q < kCols; q++) d[q] = 0.0;
-      for (int i = 1 + t; i < len; i += NT) {
-        const double xi = x[i];
-#pragma unroll
-        for (int q = 0; q < kCols; q++)
-          if (q < nc) d[q] += xi * y0[i + q * ld];
-      }
-      tsum<NT, kCols>(d, sc);
-      double wv[kCols];
-#pragma unroll
-      for (int q = 0; q < kCols; q++) wv[q] = q < nc ? (d[q] + y0[q * ld]) * tj : 0.0;
-      for (int i = 1 + t; i < len; i += NT) {
-        const double xi = x[i];
-#pragma unroll
-        for (int q = 0; q < kCols; q++)
-          if (q < nc) y0[i + q * ld] -= wv[q] * xi;
-      }
-      tsync<NT>();
-      if (t == 0)
-        for (int q = 0; q < nc; q++) y0[q * ld] -= wv[q];
-      tsync<NT>();
-    }
+    for (int c0 = j + 1; c0 < cols; c0 += kCols)
+      reflect_any<NT>(min(kCols, cols - c0), x, len, tj, A + j + c0 * ld, 1, ld, sc);
   }
 }
 
@@ -588,7 +609,7 @@ __global__ void __launch_bounds__(kBuildThreads) jacobi_kernel(const AcaJob *__r
 }
 
 // out(i, c) for c < r := (Q [C(:, ord[c]); 0])(i) with Q's k reflectors in QR
-// (rows x k, ld) and tau; C is k x k (ldc); out(i, c) lives at out[i*si + c*scs].
+// (rows x k, ld) and tau; C is k x k; out(i, c) lives at out[i*si + c*scs].
 // kCols output columns per pass.
 template <int NT>
 __device__ void team_apply_q(const double *QR, int64_t ld, int rows, int k, const double *tau, const double *C,
@@ -602,34 +623,8 @@ __device__ void team_apply_q(const double *QR, int64_t ld, int rows, int k, cons
       for (int q = 0; q < kCols; q++)
         if (q < nc) o[i * si + q * scs] = i < k ? C[i + ord[c0 + q] * k] : 0.0;
     tsync<NT>();
-    for (int j = k - 1; j >= 0; j--) {
-      const double *x = QR + j + j * ld;
-      const int len = rows - j;
-      double *y0 = o + j * si;
-      double d[kCols];
-#pragma unroll
-      for (int q = 0; q < kCols; q++) d[q] = 0.0;
-      for (int i = 1 + t; i < len; i += NT) {
-        const double xi = x[i];
-#pragma unroll
-        for (int q = 0; q < kCols; q++)
-          if (q < nc) d[q] += xi * y0[i * si + q * scs];
-      }
-      tsum<NT, kCols>(d, sc);
-      double wv[kCols];
-#pragma unroll
-      for (int q = 0; q < kCols; q++) wv[q] = q < nc ? (d[q] + y0[q * scs]) * tau[j] : 0.0;
-      for (int i = 1 + t; i < len; i += NT) {
-        const double xi = x[i];
-#pragma unroll
-        for (int q = 0; q < kCols; q++)
-          if (q < nc) y0[i * si + q * scs] -= wv[q] * xi;
-      }
-      tsync<NT>();
-      if (t == 0)
-        for (int q = 0; q < nc; q++) y0[q * scs] -= wv[q];
-      tsync<NT>();
-    }
+    for (int j = k - 1; j >= 0; j--)
+      reflect_any<NT>(nc, QR + j + j * ld, rows - j, tau[j], o + j * si, si, scs, sc);
   }
 }
 
@@ -745,20 +740,25 @@ __global__ void __launch_bounds__(256) gather_kernel(const CopyJob *__restrict__
 // ---------------------------------------------------------------------------
 struct DevBuf {
   void *p = nullptr;
+  size_t cap = 0;
   ~DevBuf() {
     if (p) cudaFree(p);
   }
   int alloc(size_t bytes) {
     if (p) cudaFree(p);
     p = nullptr;
+    cap = 0;
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
     if (e != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
       return fail(HMGPU_ERR_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
     }
+    cap = bytes ? bytes : 16;
     return HMGPU_OK;
   }
+  // Keeps the current allocation when it is large enough.
+  int reserve(size_t bytes) { return p && cap >= bytes ? HMGPU_OK : alloc(bytes); }
   template <typename V>
   V *as() const {
     return static_cast<V *>(p);
@@ -835,8 +835,8 @@ struct Compressor {
       batches++;
       ws_bytes += used * static_cast<int64_t>(sizeof(double));
       int rc;
-      if ((rc = ws.alloc(used * sizeof(double))) || (rc = djobs.alloc(nb * sizeof(AcaJob))) ||
-          (rc = dres.alloc(nb * sizeof(AcaRes))))
+      if ((rc = ws.reserve(used * sizeof(double))) || (rc = djobs.reserve(nb * sizeof(AcaJob))) ||
+          (rc = dres.reserve(nb * sizeof(AcaRes))))
         return rc;
       cudaMemcpy(djobs.p, batch.data(), nb * sizeof(AcaJob), cudaMemcpyHostToDevice);
       cudaMemset(dres.p, 0, nb * sizeof(AcaRes));
@@ -864,7 +864,7 @@ struct Compressor {
       }
       double *ust = nullptr, *vst = nullptr;
       if ((rc = place(ids, uo, vo, ulen, vlen, &ust, &vst))) return rc;
-      if ((rc = duo.alloc(nb * sizeof(int64_t))) || (rc = dvo.alloc(nb * sizeof(int64_t)))) return rc;
+      if ((rc = duo.reserve(nb * sizeof(int64_t))) || (rc = dvo.reserve(nb * sizeof(int64_t)))) return rc;
       cudaMemcpy(duo.p, uo.data(), nb * sizeof(int64_t), cudaMemcpyHostToDevice);
       cudaMemcpy(dvo.p, vo.data(), nb * sizeof(int64_t), cudaMemcpyHostToDevice);
       form_kernel<<<grid_form, kBuildThreads>>>(djobs.as<AcaJob>(), nbig, nb, svd, ws.as<double>(), dres.as<AcaRes>(),
