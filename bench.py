@@ -254,11 +254,22 @@ def run_gpu(args):
 
     P = film_points()
     t0 = time.time()
-    T = hmgpu.ClusterTree(P, max_points_per_leaf=LEAF)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=LEAF, gpu=True)
+    tree_s = time.time() - t0
     H = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=ETA, eps=TOL, precision="f32")
     torch.cuda.synchronize()
     build_s = time.time() - t0
+    build = {"seconds": build_s, "cluster_tree_s": tree_s, **{k + "_s": v for k, v in H.build_profile().items()}}
     inf = H.info()
+    if args.build_only:  # assembly of the workload alone (for launch lists of the build)
+        if rank == 0:
+            print(json.dumps({"metric": "assembly seconds", "value": build_s, "unit": "s", "n_gpus": world,
+                              "higher_is_better": False, "config": {"workload": WORKLOAD, "N": P.shape[1]},
+                              "build": build, "lowrank_blocks": inf["admissible_leaves"],
+                              "dense_blocks": inf["full_leaves"]}), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
     n = P.shape[1]
     x = torch.randn(n, device=dev, generator=torch.Generator(dev).manual_seed(rank))
     y = torch.empty(n, device=dev)
@@ -374,7 +385,7 @@ def run_gpu(args):
         "structure": {"dense_blocks": inf["full_leaves"], "lowrank_blocks": inf["admissible_leaves"],
                       "dense_entries": inf["dense_entries"], "far_entries": inf["far_entries"],
                       "total_rank": R, "max_rank": inf["max_rank"], "algorithmic_bytes": alg_bytes,
-                      "stored_bytes": inf["matrix_bytes"], "build_seconds": build_s},
+                      "stored_bytes": inf["matrix_bytes"], "build_seconds": build_s, "build": build},
         "phases_ms": {"permute": ph[0], "v_pass": ph[1], "near_u_pass": ph[2]},
         "roofline": {"bound": "hbm", "kernel": "du_rows_kernel<float,0> (near field + U t)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -406,6 +417,7 @@ def main():
     ap.add_argument("--grid", type=int, default=1024, help="film side (1024 = the headline workload)")
     ap.add_argument("--skip-rhs32", action="store_true", help="leave out the 32-RHS plain / mixed lines")
     ap.add_argument("--skip-batch", action="store_true", help="leave out the 32-H-matrix batch lines")
+    ap.add_argument("--build-only", action="store_true", help="assemble the workload, print its build line, exit")
     args = ap.parse_args()
     set_grid(args.grid)
     if args.impl == "reference":

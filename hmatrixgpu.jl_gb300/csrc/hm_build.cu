@@ -965,7 +965,8 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   PhaseClock clk;
   Blocks blk;
   try {
-    build_blocks(X, Y, eta, true, blk);  // src/hmatrix.jl:74-78
+    // src/hmatrix.jl:74-78, on the device (bit-identical to the host build)
+    if (int rc = build_blocks_device(X, Y, eta, true, blk)) return rc;
   } catch (const std::bad_alloc &) {
     return fail(HMGPU_ERR_NOMEM, "host allocation failed");
   }
@@ -1277,7 +1278,8 @@ extern "C" int hmgpu_sparsify(const hmgpu_kernel *kd, const hmgpu_tree *Xh, cons
   if (int rc = check_kernel(kd, m, n)) return rc;
   Blocks blk;
   try {
-    build_blocks(X, Y, eta, true, blk);  // BlockTree + merge_dense_matrices! + traverse (:236-239)
+    // BlockTree + merge_dense_matrices! + traverse (:236-239), on the device
+    if (int rc = build_blocks_device(X, Y, eta, true, blk)) return rc;
   } catch (const std::bad_alloc &) {
     return fail(HMGPU_ERR_NOMEM, "host allocation failed");
   }
