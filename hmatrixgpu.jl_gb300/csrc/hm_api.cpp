@@ -1,5 +1,6 @@
 // C ABI of libhmgpu: H-matrix objects, import of the reference's flattened
 // layout, the product entry points and the info/export queries.
+#include <algorithm>
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
@@ -118,7 +119,11 @@ int upload_plan(HMatrix &H, const std::vector<int32_t> &tmap0, const std::vector
   cudaMemset(H.dp.counter, 0, 64);
   H.dp.status = H.dp.counter + 4;  // its own 16-byte slot of the same allocation
   H.dp.ntiles = static_cast<int32_t>(p.tiles.size());
-  if ((rc = upload(H, &H.dp.mv_items, p.mv_items))) return rc;
+  {  // device order: by first XT row, so pieces reading the same x rows share them in L2
+    std::vector<MVItem> ms = p.mv_items;
+    std::stable_sort(ms.begin(), ms.end(), [](const MVItem &a, const MVItem &b) { return a.x_off < b.x_off; });
+    if ((rc = upload(H, &H.dp.mv_items, ms))) return rc;
+  }
   if ((rc = upload(H, &H.dp.mv_reduce, p.mv_reduce))) return rc;
   H.dp.nmv = static_cast<int32_t>(p.mv_items.size());
   H.dp.nmvr = static_cast<int32_t>(p.mv_reduce.size());
@@ -203,7 +208,12 @@ int build_tc(HMatrix &H) {
   int rc;
   if ((rc = H.dalloc(&t.adata, tp.bytes))) return rc;
   H.tc_bytes = tp.bytes;
-  if ((rc = upload(H, &t.v_items, tp.v_items)) || (rc = upload(H, &t.du_items, tp.du_items)) ||
+  // V items run in order of their first XT row, so that the pieces of every
+  // level that read the same x rows run close together and share them in L2
+  // (the packing below keeps the plan's order).
+  std::vector<TcItem> vs = tp.v_items;
+  std::stable_sort(vs.begin(), vs.end(), [](const TcItem &a, const TcItem &b) { return a.map < b.map; });
+  if ((rc = upload(H, &t.v_items, vs)) || (rc = upload(H, &t.du_items, tp.du_items)) ||
       (rc = upload(H, &t.colmap, tp.colmap)))
     return rc;
   t.reduce = H.dp.mv_reduce;
