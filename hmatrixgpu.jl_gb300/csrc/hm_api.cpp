@@ -473,10 +473,23 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
         e = hm::launch_matvec_tc(H.dp, H.tc, reinterpret_cast<const float *>(static_cast<const char *>(x) + k0 * ldx * es),
                                  ldx, nr, reinterpret_cast<float *>(static_cast<char *>(y) + k0 * ldy * es), ldy,
                                  s, ev, &nl);
-      else
-        e = hm::launch_matvec_multi(f64, H.dp, H.panels, H.vdata, H.xt_multi, H.p_multi,
+      else {
+        // each pass width has its own XT (zeroed once): rows that no pass
+        // writes (padding, the zero row) must read as zero in that width's layout
+        const int w = hm::multi_width(nr);
+        void *xt = H.xt_multi;
+        if (w < per) {
+          void *&xw = H.xt_multi_w[w == 8 ? 0 : 1];
+          if (!xw) {
+            if ((rc = H.dalloc(&xw, H.plan.xt_len * w * es))) return rc;
+            cudaMemset(xw, 0, H.plan.xt_len * w * es);
+          }
+          xt = xw;
+        }
+        e = hm::launch_matvec_multi(f64, H.dp, H.panels, H.vdata, xt, H.p_multi,
                                     static_cast<const char *>(x) + k0 * ldx * es, ldx, nr,
                                     static_cast<char *>(y) + k0 * ldy * es, ldy, H.grid_du_multi, s, ev, &nl);
+      }
       if (e != cudaSuccess) return hm::cuda_fail(e, "multi-RHS matvec launch");
       if (H.profiling) H.prof_launches += nl;
     }

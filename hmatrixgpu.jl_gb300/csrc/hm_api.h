@@ -33,6 +33,7 @@ struct HMatrix {
   std::vector<int64_t> u_src_off, v_src_off;
   // multi-right-hand-side scratch, allocated on first use
   void *xt_multi = nullptr, *p_multi = nullptr;
+  void *xt_multi_w[2] = {nullptr, nullptr};  // XT of the 8- and 16-wide passes (xt_multi: 32-wide)
   int grid_du_multi = 0;
   int multi_from = 3;  // right-hand sides from which one multi-RHS pass runs (autotuned)
   // tensor-core copy of the matrix (mixed precision)

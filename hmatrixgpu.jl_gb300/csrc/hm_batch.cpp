@@ -296,14 +296,25 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
         best[1] = kib;
       }
     }
-  // crossover: a multi-RHS pass (up to rhs_per_pass() columns) against
-  // repeated single-RHS products
+  // crossover: one multi-RHS pass (8, 16 or rhs_per_pass() wide) against
+  // repeated single-RHS products; the threshold is the first k from which
+  // every k' up to a full pass is faster as one pass of its width
   if (rc == HMGPU_OK && (rc = apply(H, best[0], best[1], 2)) == HMGPU_OK) {
-    float tm = 0.0f;
-    rc = time_products(h, x, y, per, n, m, s, e0, e1, 1, 3, &tm);
+    const int64_t widths[3] = {8, 16, per};
+    float tw[3] = {0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < 3 && rc == HMGPU_OK; i++)
+      rc = time_products(h, x, y, widths[i], n, m, s, e0, e1, 1, 3, &tw[i]);
     if (rc == HMGPU_OK) {
-      const int64_t k = static_cast<int64_t>(tm / t1) + 1;  // first k with k * t1 > tm
-      best[2] = k > per ? (1 << 30) : static_cast<int32_t>(std::max<int64_t>(k, 2));
+      int32_t from = 1 << 30;
+      for (int64_t k = per; k >= 2; k--) {
+        const int w = hm::multi_width(static_cast<int>(k));
+        const float tm = tw[w == 8 ? 0 : w == 16 ? 1 : 2];
+        if (static_cast<float>(k) * t1 > tm)
+          from = static_cast<int32_t>(k);
+        else
+          break;
+      }
+      best[2] = from;
       rc = apply(H, best[0], best[1], best[2]);
     }
   }

@@ -64,6 +64,8 @@ namespace hm {
 // Multi-right-hand-side plain product (hm_multi.cu): up to rhs_per_pass()
 // right-hand sides per call; xt holds x_len + R rows of rhs_per_pass() values.
 int rhs_per_pass();
+// Width (8, 16 or rhs_per_pass()) of the XT rows of a pass over nr columns.
+int multi_width(int nr);
 // Mixed-precision tensor-core product (hm_tc.cu), 32 right-hand sides per pass.
 struct TcPack {  // one item's FP32 row-major source -> canonical BF16 chunks
   int64_t src_off, a_off;

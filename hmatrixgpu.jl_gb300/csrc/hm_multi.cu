@@ -1,10 +1,12 @@
 // Multi-right-hand-side H-matrix product, plain form (FP32 or FP64 on the CUDA
 // cores): Y = H X for up to kRhs right-hand sides per pass.
 //
-// XT holds, for every permuted source index and every rank row, the kRhs values
-// of that row contiguously (row-major, 128 bytes per row in FP32). The matrix
-// is read once per pass and every element feeds kRhs FMAs, so this form is
-// bound by the CUDA cores' FMA rate, not by HBM.
+// A pass is W right-hand sides wide (W = 8, 16 or 32: the narrowest that holds
+// the pass's columns). XT holds, for every permuted source index and every
+// rank row, the W values of that row contiguously (row-major, 4W bytes per row
+// in FP32). The matrix is read once per pass and every element feeds W FMAs,
+// so the 32-wide form is bound by the CUDA cores' FMA rate and the 8-wide one
+// by HBM.
 //
 // Both passes run the same register-tiled micro-kernel over panels of at most
 // 128 rows (multi_panel below); partial sums of the column slices meet in
@@ -15,11 +17,11 @@
 
 namespace hm {
 
-constexpr int kRhs = 32;  // right-hand sides per pass (row length of XT)
+constexpr int kRhs = 32;  // right-hand sides per pass at most (row length of XT)
 
-template <typename T>
+template <typename T, int W>
 struct Cols {
-  static constexpr int value = 16384 / (kRhs * sizeof(T));  // XT rows staged at once
+  static constexpr int value = 16384 / (W * sizeof(T));  // XT rows staged at once
 };
 
 template <typename T>
@@ -62,44 +64,44 @@ __device__ __forceinline__ void lds8(const T *p, T (&v)[8]) {
   }
 }
 
-// XT rows from X in its own order: X[j + r ldx] goes to XT[sinv[j] kRhs + r]
+// XT rows from X in its own order: X[j + r ldx] goes to XT[sinv[j] W + r]
 // (0 for r >= nr). Reads of X are coalesced along j and every XT row is written
-// whole; the x-region rows that no source index maps to stay zero from the
-// allocation. Also re-arms both ticket counters.
-template <typename T>
+// whole; the x-region rows that no source index maps to stay zero (the buffer
+// is cleared whenever the pass width changes). Also re-arms both ticket counters.
+template <typename T, int W>
 __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int nr,
                                      const int32_t *__restrict__ sinv0, int64_t n_src,
                                      T *__restrict__ xt, int32_t *__restrict__ counter) {
-  __shared__ T tile[64][kRhs + 1];
+  __shared__ T tile[64][W + 1];
   if (blockIdx.x == 0 && threadIdx.x < 2) counter[threadIdx.x] = 0;  // both ticket slots
   for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
-    for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {
+    for (int e = threadIdx.x; e < 64 * W; e += blockDim.x) {
       const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
       const int64_t j = j0 + jj;
       tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] : T(0);
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 64 * kRhs; e += blockDim.x) {
-      const int jj = e / kRhs, r = e % kRhs;
-      if (j0 + jj < n_src) xt[static_cast<int64_t>(sinv0[j0 + jj]) * kRhs + r] = tile[jj][r];
+    for (int e = threadIdx.x; e < 64 * W; e += blockDim.x) {
+      const int jj = e / W, r = e % W;
+      if (j0 + jj < n_src) xt[static_cast<int64_t>(sinv0[j0 + jj]) * W + r] = tile[jj][r];
     }
     __syncthreads();
   }
 }
 
 // One panel of m <= 128 rows (row-major, stride lda, rows padded with zeros to
-// a multiple of 4 columns) times the kRhs-wide XT rows of its columns. Thread
-// layout: RQ = ceil(m / 4) row quads x 4 groups of 8 right-hand sides x S
-// column slices (S = 256 / (4 RQ)); a thread keeps 4 x 8 accumulators and
+// a multiple of 4 columns) times the W-wide XT rows of its columns. Thread
+// layout: RQ = ceil(m / 4) row quads x W/8 groups of 8 right-hand sides x S
+// column slices (S = 256 / (RQ W/8)); a thread keeps 4 x 8 accumulators and
 // steps 4 columns at a time (four 16-byte loads of A, eight 16-byte shared
 // loads of XT rows, 128 FMAs). `stage(c0, cn, xs)` fills xs with the XT rows
 // of columns [c0, c0 + cn). The slices meet in shared memory in slice order.
-template <typename T, typename Stage, typename Emit>
+template <typename T, int W, typename Stage, typename Emit>
 __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int ncols_pad, T *xs,
                                             T *red, Stage stage, Emit emit) {
-  constexpr int CC = Cols<T>::value;
+  constexpr int CC = Cols<T, W>::value;
   const int tid = threadIdx.x;
-  const int RQ = (m + 3) / 4, per = RQ * 4;
+  const int RQ = (m + 3) / 4, per = RQ * (W / 8);
   int S = kThreads / per;
   if (S < 1) S = 1;
   const int ks = tid / per, r = tid - ks * per, rq = r % RQ, rg = r / RQ;
@@ -130,7 +132,7 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
 #pragma unroll
         for (int k = 0; k < 4; k++) {
           T b[8];
-          lds8(xs + (c + k) * kRhs + rg * 8, b);
+          lds8(xs + (c + k) * W + rg * 8, b);
 #pragma unroll
           for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -143,20 +145,20 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
-      for (int j = 0; j < 8; j++) red[((ks * RQ + rq) * 4 + i) * kRhs + rg * 8 + j] = acc[i][j];
+      for (int j = 0; j < 8; j++) red[((ks * RQ + rq) * 4 + i) * W + rg * 8 + j] = acc[i][j];
   __syncthreads();
-  for (int o = tid; o < m * kRhs; o += kThreads) {
-    const int row = o / kRhs, q = o % kRhs;
+  for (int o = tid; o < m * W; o += kThreads) {
+    const int row = o / W, q = o % W;
     T s = T(0);
-    for (int sl = 0; sl < S; sl++) s += red[(sl * RQ * 4 + row) * kRhs + q];
+    for (int sl = 0; sl < S; sl++) s += red[(sl * RQ * 4 + row) * W + q];
     emit(row, q, s);
   }
 }
 
-// V pass: for every multi-RHS V item (ticket order, largest first)
-//   out[(I.out + k) * kRhs + r] = sum_j V[k, j] XT[(I.x_off + j) * kRhs + r],
+// V pass: for every multi-RHS V item (ticket order)
+//   out[(I.out + k) * W + r] = sum_j V[k, j] XT[(I.x_off + j) * W + r],
 // out = XT (t rows) or the partial rows P of a cut group.
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kThreads) v_multi_kernel(const T *__restrict__ V,
                                                            const MVItem *__restrict__ items,
                                                            int32_t nitems, T *__restrict__ xt,
@@ -170,29 +172,30 @@ __global__ void __launch_bounds__(kThreads) v_multi_kernel(const T *__restrict__
     const int32_t u = s_ticket[it & 1];
     if (u >= nitems) break;
     const MVItem I = items[u];
-    const T *src = xt + static_cast<int64_t>(I.x_off) * kRhs;
+    const T *src = xt + static_cast<int64_t>(I.x_off) * W;
     T *out = I.kind == 0 ? xt : P;
-    multi_panel<T>(
+    multi_panel<T, W>(
         V + I.v_off, I.stride, I.nrows, I.ncols, buf, buf,
         [&](int c0, int cn, T *xs) {
-          for (int e = threadIdx.x; e < cn * kRhs; e += kThreads) xs[e] = src[static_cast<int64_t>(c0) * kRhs + e];
+          for (int e = threadIdx.x; e < cn * W; e += kThreads) xs[e] = src[static_cast<int64_t>(c0) * W + e];
         },
-        [&](int row, int q, T s) { out[static_cast<int64_t>(I.out + row) * kRhs + q] = s; });
+        [&](int row, int q, T s) { out[static_cast<int64_t>(I.out + row) * W + q] = s; });
   }
 }
 
 // t rows of cut groups: pieces summed in order (one warp per row, lane = RHS).
-template <typename T>
+template <typename T, int W>
 __global__ void reduce_multi_kernel(const MVReduce *__restrict__ red, int32_t nred, const T *__restrict__ P,
                                     T *__restrict__ xt) {
   const int lane = threadIdx.x & 31;
+  if (lane >= W) return;
   for (int32_t e = static_cast<int32_t>(blockIdx.x); e < nred; e += gridDim.x) {
     const MVReduce R = red[e];
     for (int row = threadIdx.x >> 5; row < R.nrows; row += blockDim.x >> 5) {
       T s = T(0);
       for (int j = 0; j < R.npieces; j++)
-        s += P[(static_cast<int64_t>(R.p_row) + static_cast<int64_t>(j) * R.nrows + row) * kRhs + lane];
-      xt[static_cast<int64_t>(R.t_row + row) * kRhs + lane] = s;
+        s += P[(static_cast<int64_t>(R.p_row) + static_cast<int64_t>(j) * R.nrows + row) * W + lane];
+      xt[static_cast<int64_t>(R.t_row + row) * W + lane] = s;
     }
   }
 }
@@ -213,9 +216,9 @@ struct DuMultiArgs {
   int32_t *counter;
 };
 
-template <typename T>
+template <typename T, int W>
 __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
-  constexpr int CC = Cols<T>::value;
+  constexpr int CC = Cols<T, W>::value;
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   T *buf = reinterpret_cast<T *>(dyn_smem);  // kThreads * 32 values
   __shared__ int32_t cmap[CC];
@@ -228,7 +231,7 @@ __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
     if (u >= a.ntiles) break;
     const TileDesc d = a.tiles[a.order[u]];
     const Seg *S = a.segs + d.seg0;
-    multi_panel<T>(
+    multi_panel<T, W>(
         a.panels + d.data_off, d.ld, d.m, d.ld, buf, buf,
         [&](int c0, int cn, T *xs) {
           for (int j = threadIdx.x; j < cn; j += kThreads) {  // column -> XT row
@@ -248,12 +251,12 @@ __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
             cmap[j] = v;
           }
           __syncthreads();
-          for (int e = threadIdx.x; e < cn * (kRhs / 4); e += kThreads) {  // 16-byte copies
-            const int j = e / (kRhs / 4), q = (e % (kRhs / 4)) * 4;
+          for (int e = threadIdx.x; e < cn * (W / 4); e += kThreads) {  // 16-byte copies
+            const int j = e / (W / 4), q = (e % (W / 4)) * 4;
             const int v = cmap[j];
 #pragma unroll
             for (int w = 0; w < 4; w++)
-              xs[j * kRhs + q + w] = v >= 0 ? a.xt[static_cast<int64_t>(v) * kRhs + q + w] : T(0);
+              xs[j * W + q + w] = v >= 0 ? a.xt[static_cast<int64_t>(v) * W + q + w] : T(0);
           }
         },
         [&](int row, int q, T s) {
@@ -269,40 +272,40 @@ constexpr size_t multi_smem() {
   return static_cast<size_t>(kThreads) * 32 * sizeof(T);
 }
 
-template <typename T>
+template <typename T, int W>
 static void multi_attrs() {
   static bool done = false;  // once per process (the attribute is per function)
   if (done) return;
-  cudaFuncSetAttribute(v_multi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(v_multi_kernel<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        static_cast<int>(multi_smem<T>()));
-  cudaFuncSetAttribute(du_multi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(du_multi_kernel<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        static_cast<int>(multi_smem<T>()));
   done = true;
 }
 
-template <typename T>
+template <typename T, int W>
 static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, T *xt, T *P, const T *X,
                              int64_t ldx, int nr, T *Y, int64_t ldy, int grid_du,
                              cudaStream_t s, cudaEvent_t *ev, int *launches) {
-  multi_attrs<T>();
+  multi_attrs<T, W>();
   int gp = static_cast<int>((p.n_src + 63) / 64);
   if (gp > 2048) gp = 2048;
   int nl = 0;
   if (ev) cudaEventRecord(ev[0], s);
-  permute_multi_kernel<T><<<gp, kThreads, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xt, p.counter);
+  permute_multi_kernel<T, W><<<gp, kThreads, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xt, p.counter);
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
   if (p.nmv > 0) {
-    v_multi_kernel<T><<<grid_du, kThreads, multi_smem<T>(), s>>>(vdata, p.mv_items, p.nmv, xt, P, p.counter);
+    v_multi_kernel<T, W><<<grid_du, kThreads, multi_smem<T>(), s>>>(vdata, p.mv_items, p.nmv, xt, P, p.counter);
     nl++;
     if (p.nmvr > 0) {
-      reduce_multi_kernel<T><<<p.nmvr < 4096 ? p.nmvr : 4096, kThreads, 0, s>>>(p.mv_reduce, p.nmvr, P, xt);
+      reduce_multi_kernel<T, W><<<p.nmvr < 4096 ? p.nmvr : 4096, kThreads, 0, s>>>(p.mv_reduce, p.nmvr, P, xt);
       nl++;
     }
   }
   if (ev) cudaEventRecord(ev[2], s);
   DuMultiArgs<T> a{panels, p.tiles, p.tile_order, p.ntiles, p.segs, xt, p.tmap0, Y, ldy, nr, p.counter + 1};
-  du_multi_kernel<T><<<grid_du, kThreads, multi_smem<T>(), s>>>(a);
+  du_multi_kernel<T, W><<<grid_du, kThreads, multi_smem<T>(), s>>>(a);
   nl++;
   if (ev) cudaEventRecord(ev[3], s);
   if (launches) *launches = nl;
@@ -311,16 +314,29 @@ static cudaError_t run_multi(const DevPlan &p, const T *panels, const T *vdata, 
 
 int rhs_per_pass() { return kRhs; }
 
+int multi_width(int nr) { return nr <= 8 ? 8 : nr <= 16 ? 16 : kRhs; }
+
 int occupancy_du_multi(bool f64) {
   int n = 0;
   if (f64) {
-    multi_attrs<double>();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<double>, kThreads, multi_smem<double>());
+    multi_attrs<double, kRhs>();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<double, kRhs>, kThreads, multi_smem<double>());
   } else {
-    multi_attrs<float>();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<float>, kThreads, multi_smem<float>());
+    multi_attrs<float, kRhs>();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, du_multi_kernel<float, kRhs>, kThreads, multi_smem<float>());
   }
   return n > 0 ? n : 1;
+}
+
+template <typename T>
+static cudaError_t run_multi_w(const DevPlan &p, const T *panels, const T *vdata, T *xt, T *P, const T *X,
+                               int64_t ldx, int nr, T *Y, int64_t ldy, int grid_du, cudaStream_t s,
+                               cudaEvent_t *ev, int *launches) {
+  switch (multi_width(nr)) {
+    case 8: return run_multi<T, 8>(p, panels, vdata, xt, P, X, ldx, nr, Y, ldy, grid_du, s, ev, launches);
+    case 16: return run_multi<T, 16>(p, panels, vdata, xt, P, X, ldx, nr, Y, ldy, grid_du, s, ev, launches);
+    default: return run_multi<T, kRhs>(p, panels, vdata, xt, P, X, ldx, nr, Y, ldy, grid_du, s, ev, launches);
+  }
 }
 
 cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, const void *vdata,
@@ -328,11 +344,11 @@ cudaError_t launch_matvec_multi(bool f64, const DevPlan &p, const void *panels, 
                                 int64_t ldy, int grid_du, cudaStream_t s, cudaEvent_t *ev,
                                 int *launches) {
   if (f64)
-    return run_multi<double>(p, static_cast<const double *>(panels), static_cast<const double *>(vdata),
+    return run_multi_w<double>(p, static_cast<const double *>(panels), static_cast<const double *>(vdata),
                              static_cast<double *>(xt), static_cast<double *>(P),
                              static_cast<const double *>(X), ldx, nr, static_cast<double *>(Y), ldy,
                              grid_du, s, ev, launches);
-  return run_multi<float>(p, static_cast<const float *>(panels), static_cast<const float *>(vdata),
+  return run_multi_w<float>(p, static_cast<const float *>(panels), static_cast<const float *>(vdata),
                           static_cast<float *>(xt), static_cast<float *>(P), static_cast<const float *>(X),
                           ldx, nr, static_cast<float *>(Y), ldy, grid_du, s, ev, launches);
 }

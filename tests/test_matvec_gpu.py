@@ -138,6 +138,25 @@ def test_many_rhs_two_passes(case, gpu, prec, tol):
     assert rel(Y[:, 0], y0) <= tol
 
 
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-5)])
+def test_pass_widths(case, gpu, prec, tol):
+    """Passes 8, 16 and 32 wide (chosen by the column count), in alternating
+    order on one H-matrix, each column against the oracle's product."""
+    import torch
+    _, _, Ho = case
+    H = hmgpu.HMatrix.from_flat(**_flat(Ho), precision=prec)
+    dt = torch.float64 if prec == "f64" else torch.float32
+    rng = np.random.default_rng(17)
+    for nrhs in (8, 30, 3, 16, 9, 17, 8, 32, 12):
+        X = rng.standard_normal((Ho.n, nrhs))
+        Xd = torch.tensor(X, dtype=dt, device=gpu).t().contiguous().t()
+        Y = (H * Xd).double().cpu().numpy()
+        Xr = X.astype(np.float32).astype(np.float64) if prec == "f32" else X
+        for k in range(nrhs):
+            assert rel(Y[:, k], Ho.mul(Xr[:, k])) <= tol, (nrhs, k)
+    assert H.status() == 0
+
+
 def test_device_status_clean(case, gpu):
     """No bounded device wait expires in a product, plain or compensated."""
     import ctypes as C
