@@ -76,14 +76,23 @@ mutable struct ClusterTree
     coordinates::Matrix{Float64}
 end
 
-function ClusterTree(coordinates::AbstractMatrix; max_points_per_leaf::Int=32, dims::Int=1)
+# gpu=true builds the same tree (bit for bit) on the current CUDA device
+# (hmgpu_tree_build_device).
+function ClusterTree(coordinates::AbstractMatrix; max_points_per_leaf::Int=32, dims::Int=1,
+                     gpu::Bool=false)
     dims <= 0 && error("Parameter `dims` must be a positive integer.")
     c = Matrix{Float64}(coordinates)
     size(c, 1) == 3 || error("coordinates must be 3 x N")
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:hmgpu_tree_build, libhmgpu), Cint,
-                (Ptr{Float64}, Int64, Int64, Int64, Ref{Ptr{Cvoid}}),
-                c, size(c, 2), max_points_per_leaf, dims, h))
+    if gpu
+        check(ccall((:hmgpu_tree_build_device, libhmgpu), Cint,
+                    (Ptr{Float64}, Int64, Int64, Int64, Ref{Ptr{Cvoid}}),
+                    c, size(c, 2), max_points_per_leaf, dims, h))
+    else
+        check(ccall((:hmgpu_tree_build, libhmgpu), Cint,
+                    (Ptr{Float64}, Int64, Int64, Int64, Ref{Ptr{Cvoid}}),
+                    c, size(c, 2), max_points_per_leaf, dims, h))
+    end
     nn, il = Ref{Int64}(0), Ref{Int64}(0)
     check(ccall((:hmgpu_tree_info, libhmgpu), Cint,
                 (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}),
