@@ -89,17 +89,30 @@ __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int n
   }
 }
 
+// 16-byte asynchronous copy global -> shared; zeros when `valid` is false
+// (then nothing is read from `src`).
+__device__ __forceinline__ void cp16(void *dst, const void *src, bool valid) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // One panel of m <= 128 rows (row-major, stride lda, rows padded with zeros to
 // a multiple of 4 columns) times the W-wide XT rows of its columns. Thread
 // layout: RQ = ceil(m / 4) row quads x W/8 groups of 8 right-hand sides x S
 // column slices (S = 256 / (RQ W/8)); a thread keeps 4 x 8 accumulators and
 // steps 4 columns at a time (four 16-byte loads of A, eight 16-byte shared
-// loads of XT rows, 128 FMAs). `stage(c0, cn, xs)` fills xs with the XT rows
-// of columns [c0, c0 + cn). The slices meet in shared memory in slice order.
+// loads of XT rows, 128 FMAs). `stage(c0, cn, xs)` issues the asynchronous
+// copies (cp16) of the XT rows of columns [c0, c0 + cn) into xs; the XT rows of
+// the next CC columns are copied into the other half of `buf` while the FMAs
+// of the current ones run. The slices meet in shared memory in slice order.
 template <typename T, int W, typename Stage, typename Emit>
-__device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int ncols_pad, T *xs,
-                                            T *red, Stage stage, Emit emit) {
+__device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int ncols_pad, T *buf,
+                                            Stage stage, Emit emit) {
   constexpr int CC = Cols<T, W>::value;
+  T *red = buf;
   const int tid = threadIdx.x;
   const int RQ = (m + 3) / 4, per = RQ * (W / 8);
   int S = kThreads / per;
@@ -114,21 +127,30 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
   bool ok[4];
 #pragma unroll
   for (int i = 0; i < 4; i++) ok[i] = rq * 4 + i < m;
-  for (int c0 = 0; c0 < ncols_pad; c0 += CC) {
-    const int cn = min(CC, ncols_pad - c0);
-    __syncthreads();  // xs free
-    stage(c0, cn, xs);
-    __syncthreads();
-    if (active)
-      for (int c = 4 * ks; c < cn; c += 4 * S) {
-        T a[4][4];
+  const int nst = (ncols_pad + CC - 1) / CC;
+  __syncthreads();  // buf free (the previous panel's slice sums are read)
+  if (nst > 0) stage(0, min(CC, ncols_pad), buf);
+  cp_commit();
+  for (int st = 0; st < nst; st++) {
+    const int c0 = st * CC, cn = min(CC, ncols_pad - c0);
+    const T *xs = buf + (st & 1) * CC * W;
+    cp_wait_all();
+    __syncthreads();  // stage st in place everywhere; stage st - 1's half is free
+    if (st + 1 < nst) stage(c0 + CC, min(CC, ncols_pad - c0 - CC), buf + ((st + 1) & 1) * CC * W);
+    cp_commit();
+    if (active) {
+      // the A entries of the next step are loaded before this step's FMAs
+      const int step = 4 * S;
+      auto load = [&](int c, T (&d)[4][4]) {
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          if (ok[i])
-            ld4(A + static_cast<int64_t>(rq * 4 + i) * lda + c0 + c, a[i]);
+          if (ok[i] && c < cn)
+            ld4(A + static_cast<int64_t>(rq * 4 + i) * lda + c0 + c, d[i]);
           else
-            a[i][0] = a[i][1] = a[i][2] = a[i][3] = T(0);
+            d[i][0] = d[i][1] = d[i][2] = d[i][3] = T(0);
         }
+      };
+      auto step_fma = [&](int c, const T (&a)[4][4]) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
           T b[8];
@@ -138,7 +160,20 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
 #pragma unroll
             for (int j = 0; j < 8; j++) acc[i][j] = fma(a[i][k], b[j], acc[i][j]);
         }
+      };
+      T a0[4][4], a1[4][4];
+      int c = 4 * ks;
+      load(c, a0);
+      while (c < cn) {
+        load(c + step, a1);
+        step_fma(c, a0);
+        c += step;
+        if (c >= cn) break;
+        load(c + step, a0);
+        step_fma(c, a1);
+        c += step;
       }
+    }
   }
   __syncthreads();  // red aliases xs
   if (active)
@@ -175,9 +210,11 @@ __global__ void __launch_bounds__(kThreads) v_multi_kernel(const T *__restrict__
     const T *src = xt + static_cast<int64_t>(I.x_off) * W;
     T *out = I.kind == 0 ? xt : P;
     multi_panel<T, W>(
-        V + I.v_off, I.stride, I.nrows, I.ncols, buf, buf,
-        [&](int c0, int cn, T *xs) {
-          for (int e = threadIdx.x; e < cn * W; e += kThreads) xs[e] = src[static_cast<int64_t>(c0) * W + e];
+        V + I.v_off, I.stride, I.nrows, I.ncols, buf,
+        [&](int c0, int cn, T *xs) {  // contiguous XT rows
+          constexpr int kV = 16 / sizeof(T);  // values per 16-byte copy
+          for (int e = threadIdx.x; e < cn * W / kV; e += kThreads)
+            cp16(xs + e * kV, src + static_cast<int64_t>(c0) * W + e * kV, true);
         },
         [&](int row, int q, T s) { out[static_cast<int64_t>(I.out + row) * W + q] = s; });
   }
@@ -218,10 +255,8 @@ struct DuMultiArgs {
 
 template <typename T, int W>
 __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
-  constexpr int CC = Cols<T, W>::value;
   extern __shared__ __align__(16) unsigned char dyn_smem[];
-  T *buf = reinterpret_cast<T *>(dyn_smem);  // kThreads * 32 values
-  __shared__ int32_t cmap[CC];
+  T *buf = reinterpret_cast<T *>(dyn_smem);  // two halves of staged XT rows, slice sums after
   __shared__ int32_t s_ticket[2];
   const int tid = threadIdx.x;
   for (int it = 0;; it++) {
@@ -232,9 +267,10 @@ __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
     const TileDesc d = a.tiles[a.order[u]];
     const Seg *S = a.segs + d.seg0;
     multi_panel<T, W>(
-        a.panels + d.data_off, d.ld, d.m, d.ld, buf, buf,
-        [&](int c0, int cn, T *xs) {
-          for (int j = threadIdx.x; j < cn; j += kThreads) {  // column -> XT row
+        a.panels + d.data_off, d.ld, d.m, d.ld, buf,
+        [&](int c0, int cn, T *xs) {  // one thread per column: its XT row, then its copies
+          constexpr int kP = W * static_cast<int>(sizeof(T)) / 16;  // 16-byte pieces per XT row
+          for (int j = threadIdx.x; j < cn; j += kThreads) {
             const int c = c0 + j;
             int v = -1;
             if (c < d.ncols) {
@@ -248,15 +284,9 @@ __global__ void __launch_bounds__(kThreads) du_multi_kernel(DuMultiArgs<T> a) {
               }
               v = S[lo].vec_off + (c - S[lo].col0);
             }
-            cmap[j] = v;
-          }
-          __syncthreads();
-          for (int e = threadIdx.x; e < cn * (W / 4); e += kThreads) {  // 16-byte copies
-            const int j = e / (W / 4), q = (e % (W / 4)) * 4;
-            const int v = cmap[j];
+            const T *src = a.xt + static_cast<int64_t>(v >= 0 ? v : 0) * W;
 #pragma unroll
-            for (int w = 0; w < 4; w++)
-              xs[j * W + q + w] = v >= 0 ? a.xt[static_cast<int64_t>(v) * W + q + w] : T(0);
+            for (int q = 0; q < kP; q++) cp16(xs + j * W + q * (16 / sizeof(T)), src + q * (16 / sizeof(T)), v >= 0);
           }
         },
         [&](int row, int q, T s) {
