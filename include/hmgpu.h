@@ -43,9 +43,12 @@ extern "C" {
 /* storage / arithmetic modes of an H-matrix */
 #define HMGPU_F64 0   /* all factors FP64, FP64 arithmetic; x, y are double        */
 #define HMGPU_F32 1   /* all factors FP32, FP32 arithmetic; x, y are float         */
-#define HMGPU_MIXED 2 /* near field FP32; far field hi+lo BF16 with per-column
-                         FP32 scales (hi only where the block tolerance allows);
-                         compensated FP32 accumulation; x, y are float           */
+#define HMGPU_MIXED 2 /* FP32 factors with compensated FP32 accumulation for
+                         few right-hand sides; for more, a copy of every block
+                         as BF16 pairs hi + lo (hi = bf16(a), lo = bf16(a - hi))
+                         multiplied on the tensor cores with FP32 accumulation
+                         (the threshold is hmgpu_hmatrix_autotune's); x, y are
+                         float                                                 */
 
 /* matrix entry generators for on-device assembly */
 #define HMGPU_KERNEL_EXPLICIT 0  /* entries of a given column-major matrix        */
