@@ -293,14 +293,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
           break;
         }
         {  // A: the chunk's hi rows to tile rows 0.., its lo rows to tile rows 64..
+          // (read once: evict-first in L2, so the gathered XTS rows stay resident)
+          uint64_t pol;
+          asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
           const int G = (I.m + 7) >> 3;
           const int units = G * kc;  // 16-byte units of each half
           const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
           const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
           for (int u = lane; u < units; u += 32) {
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(hi + 16u * u), "l"(src + 16 * u) : "memory");
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(lo + 16u * u),
-                         "l"(src + 16 * (units + u))
+            asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(hi + 16u * u),
+                         "l"(src + 16 * u), "l"(pol)
+                         : "memory");
+            asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(lo + 16u * u),
+                         "l"(src + 16 * (units + u)), "l"(pol)
                          : "memory");
           }
         }
