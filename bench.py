@@ -207,6 +207,79 @@ def cpu_sample(threads, target_s=15.0, more_threads=()):
         "cores": threads, "seconds": dt * reps, "more": more}
 
 
+def cube_measurement(dev, steps, hbm):
+    """The plain drop-in case: N = 2^18 points uniform in [0,1]^3, Laplace
+    1/(4 pi r), leaf 64, eta 2, tol 1e-6, FP32 storage, one RHS. Device build
+    (trees included), autotuned layout, product time with its phases, the
+    passes' bandwidth against the measured peak, and the error of 256 rows of y
+    against the exact kernel sums (FP64 on the host)."""
+    import torch
+
+    import hmgpu
+    from tests import geometry
+    P = geometry.cube(1 << 18, seed=2)
+    n = P.shape[1]
+    t0 = time.time()
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=64, gpu=True)
+    H = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=1e-6, precision="f32")
+    torch.cuda.synchronize()
+    build = time.time() - t0
+    tune = H.autotune()
+    x = torch.randn(n, device=dev, generator=torch.Generator(dev).manual_seed(11))
+    y = torch.empty(n, device=dev)
+    for _ in range(3):
+        hmgpu.mul_(y, H, x)
+    lib = hmgpu._lib.lib()
+    hmgpu.check(lib.hmgpu_hmatrix_set_profiling(H._h, 1))
+    stream = torch.cuda.current_stream(dev)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(10, min(steps // 5, 100))
+    torch.cuda.synchronize()
+    s.record(stream)
+    for _ in range(reps):
+        hmgpu.mul_(y, H, x)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / reps
+    import ctypes as C
+    ph = np.zeros(3)
+    nl, npd = C.c_int64(), C.c_int64()
+    hmgpu.check(lib.hmgpu_hmatrix_phase_times(H._h, hmgpu.ptr(ph), C.byref(nl), C.byref(npd)))
+    hmgpu.check(lib.hmgpu_hmatrix_set_profiling(H._h, 0))
+    ph = ph / max(npd.value, 1)
+    inf = H.info()
+    R = inf["total_rank"]
+    d, a = H.blocks()
+    u_entries = int(((a[:, 1] - a[:, 0] + 1) * a[:, 4]).sum()) if len(a) else 0
+    v_entries = inf["far_entries"] - u_entries
+    alg = 4 * (inf["dense_entries"] + inf["far_entries"]) + 4 * (2 * n + 2 * R)
+    du_b = 4 * (inf["dense_entries"] + u_entries) + 4 * (2 * n + R)
+    v_b = 4 * v_entries + 4 * R
+    rows = np.random.default_rng(12).choice(n, 256, replace=False)
+    xs = x.double().cpu().numpy()
+    ys = y.double().cpu().numpy()
+    Pt = P.T
+    exact = np.empty(len(rows))
+    for k, i in enumerate(rows):  # K(x_i, x_j) = 1/(4 pi r), 0 at r = 0
+        r = np.linalg.norm(Pt - Pt[i], axis=1)
+        w = np.zeros(n)
+        nz = r > 0
+        w[nz] = 1.0 / (4.0 * np.pi * r[nz])
+        exact[k] = w @ xs
+    err = float(np.linalg.norm(ys[rows] - exact) / np.linalg.norm(exact))
+    return {"workload": "cube-2^18 Laplace leaf64 eta2 tol1e-6, 1 RHS, FP32 storage",
+            "build_seconds": build, "build": H.build_profile(), "autotuned": tune,
+            "dense_entries": inf["dense_entries"], "far_entries": inf["far_entries"],
+            "lowrank_blocks": inf["admissible_leaves"], "dense_blocks": inf["full_leaves"],
+            "max_rank": inf["max_rank"], "ms_per_product": ms, "matvec_per_s": 1e3 / ms,
+            "hbm_gbs": alg / (ms * 1e-3) / 1e9,
+            "phases_ms": {"permute": ph[0], "v_pass": ph[1], "near_u_pass": ph[2]},
+            "v_pass_gbs": v_b / (ph[1] * 1e-3) / 1e9, "near_u_gbs": du_b / (ph[2] * 1e-3) / 1e9,
+            "near_u_frac_of_measured": du_b / (ph[2] * 1e-3) / 1e9 / hbm,
+            "v_pass_frac_of_measured": v_b / (ph[1] * 1e-3) / 1e9 / hbm,
+            "rel_err_256_exact_rows": err}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -378,6 +451,7 @@ def run_gpu(args):
     du_ms = ph[2]
     achieved = du_bytes / (du_ms * 1e-3) / 1e9
     batch32 = None if args.skip_batch else batch_measurement(dev, args.steps)
+    cube18 = None if args.skip_cube else cube_measurement(dev, args.steps, hbm)
     cpu_v, cpu_d = cpu_sample(1, target_s=10.0, more_threads=(os.cpu_count() or 1,))
     value = job_rate(world, ms * 1e-3)
     line = {
@@ -411,6 +485,7 @@ def run_gpu(args):
         "gpu_launches": int(nl.value),
         "rhs32": rhs32,
         "batch32": batch32,
+        "cube18": cube18,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -428,6 +503,7 @@ def main():
     ap.add_argument("--skip-rhs32", action="store_true", help="leave out the 32-RHS plain / mixed lines")
     ap.add_argument("--skip-batch", action="store_true", help="leave out the 32-H-matrix batch lines")
     ap.add_argument("--build-only", action="store_true", help="assemble the workload, print its build line, exit")
+    ap.add_argument("--skip-cube", action="store_true", help="leave out the 2^18-cube tol 1e-6 line")
     args = ap.parse_args()
     set_grid(args.grid)
     if args.impl == "reference":
