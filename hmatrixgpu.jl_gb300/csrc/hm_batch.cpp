@@ -187,7 +187,7 @@ uint64_t structure_hash(const HMatrix &H) {
   return h;
 }
 
-bool cache_lookup(const char *path, uint64_t key, int32_t (&v)[3]) {
+bool cache_lookup(const char *path, uint64_t key, int32_t (&v)[4]) {
   if (!path) return false;
   FILE *f = std::fopen(path, "r");
   if (!f) return false;
@@ -195,11 +195,12 @@ bool cache_lookup(const char *path, uint64_t key, int32_t (&v)[3]) {
   bool found = false;
   while (std::fgets(line, sizeof line, f)) {
     unsigned long long k;
-    int a, b, c;
-    if (std::sscanf(line, "hmgpu-tune %llx %d %d %d", &k, &a, &b, &c) == 4 && k == key) {
+    int a, b, c, d;
+    if (std::sscanf(line, "hmgpu-tune %llx %d %d %d %d", &k, &a, &b, &c, &d) == 5 && k == key) {
       v[0] = a;
       v[1] = b;
       v[2] = c;
+      v[3] = d;
       found = true;  // the last line for a key wins
     }
   }
@@ -207,18 +208,20 @@ bool cache_lookup(const char *path, uint64_t key, int32_t (&v)[3]) {
   return found;
 }
 
-void cache_store(const char *path, uint64_t key, const int32_t (&v)[3]) {
+void cache_store(const char *path, uint64_t key, const int32_t (&v)[4]) {
   if (!path) return;
   FILE *f = std::fopen(path, "a");
   if (!f) return;
-  std::fprintf(f, "hmgpu-tune %016llx %d %d %d\n", static_cast<unsigned long long>(key), v[0], v[1], v[2]);
+  std::fprintf(f, "hmgpu-tune %016llx %d %d %d %d\n", static_cast<unsigned long long>(key), v[0], v[1], v[2],
+               v[3]);
   std::fclose(f);
 }
 
-int apply(HMatrix &H, int32_t unit_rows, int32_t vunit_kib, int32_t multi_from) {
+int apply(HMatrix &H, int32_t unit_rows, int32_t vunit_kib, int32_t multi_from, int32_t v_dynamic) {
   hm::make_units(H.plan, unit_rows);
   hm::make_vunits(H.plan, static_cast<int64_t>(vunit_kib) * 1024, H.grid_v * (hm::kThreads / 32));
   H.multi_from = multi_from;
+  H.dp.v_dynamic = v_dynamic != 0;
   return hm::upload_units(H);
 }
 
@@ -244,9 +247,9 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
   if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
   HMatrix &H = *reinterpret_cast<HMatrix *>(h);
   const uint64_t key = structure_hash(H);
-  int32_t best[3];
+  int32_t best[4];
   if (cache_lookup(cache_path, key, best)) {
-    if (int rc = apply(H, best[0], best[1], best[2])) return rc;
+    if (int rc = apply(H, best[0], best[1], best[2], best[3])) return rc;
     if (result) {
       std::copy(best, best + 3, result);
       result[3] = 1;
@@ -280,26 +283,29 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
     cudaGetLastError();
     return hm::fail(HMGPU_ERR_NOMEM, std::string("autotune scratch: ") + cudaGetErrorString(e));
   }
-  // single-RHS layout parameters
+  // single-RHS layout parameters and the V schedule
   const int32_t cand_rows[2] = {8, 16}, cand_kib[3] = {32, 64, 128};
   float t1 = 0.0f;
   best[0] = 16;
   best[1] = 64;
+  best[3] = 0;
   for (int32_t ur : cand_rows)
-    for (int32_t kib : cand_kib) {
-      if ((rc = apply(H, ur, kib, H.multi_from))) break;
-      float ms = 0.0f;
-      if ((rc = time_products(h, x, y, 1, n, m, s, e0, e1, 2, 5, &ms))) break;
-      if (t1 == 0.0f || ms < t1) {
-        t1 = ms;
-        best[0] = ur;
-        best[1] = kib;
+    for (int32_t kib : cand_kib)
+      for (int32_t vd = 0; vd < 2 && rc == HMGPU_OK; vd++) {
+        if ((rc = apply(H, ur, kib, H.multi_from, vd))) break;
+        float ms = 0.0f;
+        if ((rc = time_products(h, x, y, 1, n, m, s, e0, e1, 2, 5, &ms))) break;
+        if (t1 == 0.0f || ms < t1) {
+          t1 = ms;
+          best[0] = ur;
+          best[1] = kib;
+          best[3] = vd;
+        }
       }
-    }
   // crossover: one multi-RHS pass (8, 16 or rhs_per_pass() wide) against
   // repeated single-RHS products; the threshold is the first k from which
   // every k' up to a full pass is faster as one pass of its width
-  if (rc == HMGPU_OK && (rc = apply(H, best[0], best[1], 2)) == HMGPU_OK) {
+  if (rc == HMGPU_OK && (rc = apply(H, best[0], best[1], 2, best[3])) == HMGPU_OK) {
     const int64_t widths[3] = {8, 16, per};
     float tw[3] = {0.0f, 0.0f, 0.0f};
     for (int i = 0; i < 3 && rc == HMGPU_OK; i++)
@@ -315,7 +321,7 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
           break;
       }
       best[2] = from;
-      rc = apply(H, best[0], best[1], best[2]);
+      rc = apply(H, best[0], best[1], best[2], best[3]);
     }
   }
   cleanup();
@@ -325,5 +331,14 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
     std::copy(best, best + 3, result);
     result[3] = 0;
   }
+  return HMGPU_OK;
+}
+
+extern "C" int hmgpu_hmatrix_tuning(const hmgpu_hmatrix *h, int32_t *v, int32_t n) {
+  if (!h || (!v && n > 0)) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
+  const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);
+  const int32_t all[4] = {H.plan.unit_rows, static_cast<int32_t>(H.plan.vunit_bytes / 1024), H.multi_from,
+                          H.dp.v_dynamic ? 1 : 0};
+  for (int32_t i = 0; i < n && i < 4; i++) v[i] = all[i];
   return HMGPU_OK;
 }

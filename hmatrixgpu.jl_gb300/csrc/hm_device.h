@@ -19,6 +19,7 @@ struct DevPlan {
   int32_t *warp_begin = nullptr;
   int32_t nwarps = 0;
   bool warp_begin_empty = true;  // no V units (no low-rank blocks)
+  bool v_dynamic = false;        // V units from a ticket counter instead of warp ranges
   MVItem *mv_items = nullptr;  // multi-RHS V items, largest first
   int32_t nmv = 0;
   MVReduce *mv_reduce = nullptr;

@@ -441,7 +441,15 @@ class HMatrix:
         r = (C.c_int32 * 4)()
         path = None if cache_path is None else str(cache_path).encode()
         check(lib().hmgpu_hmatrix_autotune(self._h, path, r))
-        return {"unit_rows": r[0], "vunit_kib": r[1], "multi_rhs_from": r[2], "from_cache": bool(r[3])}
+        out = {"unit_rows": r[0], "vunit_kib": r[1], "multi_rhs_from": r[2], "from_cache": bool(r[3])}
+        out["v_schedule"] = "dynamic" if self.tuning()["v_dynamic"] else "static"
+        return out
+
+    def tuning(self):
+        """The product parameters in force (hmgpu_hmatrix_tuning)."""
+        v = (C.c_int32 * 4)()
+        check(lib().hmgpu_hmatrix_tuning(self._h, v, 4))
+        return {"unit_rows": v[0], "vunit_kib": v[1], "multi_rhs_from": v[2], "v_dynamic": bool(v[3])}
 
     def status(self):
         """Device error word of the products so far (0 = clean; synchronises the

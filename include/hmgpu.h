@@ -312,13 +312,19 @@ int hmgpu_graph_free(hmgpu_graph *G);
 
 /* Times the product's free parameters on H's own data (about a second of
  * products) and keeps the fastest: rows per near/U unit (8 or 16), bytes per
- * V unit (32, 64 or 128 KiB) and the number of right-hand sides from which one
- * multi-RHS pass replaces repeated single-RHS products. None of them changes
+ * V unit (32, 64 or 128 KiB), the V schedule (see hmgpu_hmatrix_tuning) and
+ * the number of right-hand sides from which one multi-RHS pass replaces
+ * repeated single-RHS products. None of them changes
  * any result. With `cache_path` (a text file; NULL for none) the choice is
  * looked up first and stored after, keyed by the H-matrix's structure and the
  * device. result (optional, 4 values): unit rows, V unit KiB, multi-RHS
  * threshold (1 << 30: never), 1 if it came from the cache. */
 int hmgpu_hmatrix_autotune(hmgpu_hmatrix *H, const char *cache_path, int32_t *result);
+/* The product parameters in force (no counterpart in the reference): rows per
+ * near/U unit, V unit KiB, multi-RHS threshold, V schedule (0: each warp owns
+ * a byte-balanced range of V units, 1: warps take V units from a ticket
+ * counter; the autotuner times both). Writes min(n, 4) values. */
+int hmgpu_hmatrix_tuning(const hmgpu_hmatrix *H, int32_t *values, int32_t n);
 
 /* An assembled H-matrix on disk (no counterpart in the reference; the
  * reference's flattened HMatrix has no file form): the device layout, index
