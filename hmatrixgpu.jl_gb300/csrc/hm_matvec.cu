@@ -182,15 +182,70 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads, 6) v_pass_kernel(const T *__restrict__ V,
                                                           const VUnit *__restrict__ units,
                                                           const int32_t *__restrict__ warp_begin,
-                                                          T *__restrict__ xt, int32_t nunits,
-                                                          int32_t *__restrict__ ticket) {
+                                                          T *__restrict__ xt) {
+  using VT = typename Vec16<T>::type;
+  constexpr int VEC = Vec16<T>::N;
   const int warp = static_cast<int>((blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
-  if (!ticket) {
-    const int u0 = warp_begin[warp], u1 = warp_begin[warp + 1];
-    for (int u = u0; u < u1; u++) v_unit(V, units[u], xt, lane);
-    return;
+  const int u0 = warp_begin[warp], u1 = warp_begin[warp + 1];
+  for (int u = u0; u < u1; u++) {
+    const VUnit U = units[u];
+    const int g = U.lanes, slot = lane / g, sub = lane - slot * g, per = 32 / g;
+    const int nv = U.stride / VEC;
+    const VT *X = reinterpret_cast<const VT *>(xt + U.x_off);
+    for (int k0 = 0; k0 < U.nrows; k0 += per) {
+      const int k = k0 + slot;
+      T acc = T(0);
+      if (k < U.nrows) {
+        const VT *row = reinterpret_cast<const VT *>(V + U.v_off + static_cast<int64_t>(k) * U.stride);
+        int p = sub;
+        for (; p + 3 * g < nv; p += 4 * g) {  // four 16-byte loads of V in flight per lane
+          VT a0 = ld_stream(row + p), a1 = ld_stream(row + p + g);
+          VT a2 = ld_stream(row + p + 2 * g), a3 = ld_stream(row + p + 3 * g);
+          VT b0 = __ldg(X + p), b1 = __ldg(X + p + g), b2 = __ldg(X + p + 2 * g), b3 = __ldg(X + p + 3 * g);
+          const T *ea0 = reinterpret_cast<const T *>(&a0), *eb0 = reinterpret_cast<const T *>(&b0);
+          const T *ea1 = reinterpret_cast<const T *>(&a1), *eb1 = reinterpret_cast<const T *>(&b1);
+          const T *ea2 = reinterpret_cast<const T *>(&a2), *eb2 = reinterpret_cast<const T *>(&b2);
+          const T *ea3 = reinterpret_cast<const T *>(&a3), *eb3 = reinterpret_cast<const T *>(&b3);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea0[q], eb0[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea1[q], eb1[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea2[q], eb2[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea3[q], eb3[q], acc);
+        }
+        for (; p + g < nv; p += 2 * g) {
+          VT a0 = ld_stream(row + p), a1 = ld_stream(row + p + g);
+          VT b0 = __ldg(X + p), b1 = __ldg(X + p + g);
+          const T *ea0 = reinterpret_cast<const T *>(&a0), *eb0 = reinterpret_cast<const T *>(&b0);
+          const T *ea1 = reinterpret_cast<const T *>(&a1), *eb1 = reinterpret_cast<const T *>(&b1);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea0[q], eb0[q], acc);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea1[q], eb1[q], acc);
+        }
+        if (p < nv) {
+          VT a0 = ld_stream(row + p);
+          VT b0 = __ldg(X + p);
+          const T *ea0 = reinterpret_cast<const T *>(&a0), *eb0 = reinterpret_cast<const T *>(&b0);
+#pragma unroll
+          for (int q = 0; q < VEC; q++) acc = fma_(ea0[q], eb0[q], acc);
+        }
+      }
+      for (int o = g >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (sub == 0 && k < U.nrows) xt[U.t_off + k] = acc;
+    }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 6) v_pass_dyn_kernel(const T *__restrict__ V,
+                                                              const VUnit *__restrict__ units,
+                                                              int32_t nunits, T *__restrict__ xt,
+                                                              int32_t *__restrict__ ticket) {
+  const int lane = threadIdx.x & 31;
   int u = 0;
   if (lane == 0) u = atomicAdd(ticket, 1);
   u = __shfl_sync(0xffffffffu, u, 0);
@@ -364,8 +419,10 @@ static cudaError_t run(const DevPlan &p, const T *panels, const T *vdata, T *xt,
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
   if (!p.warp_begin_empty) {
-    v_pass_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.warp_begin, xt, p.nvunits,
-                                                 p.v_dynamic ? p.counter + 8 : nullptr);
+    if (p.v_dynamic)
+      v_pass_dyn_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.nvunits, xt, p.counter + 8);
+    else
+      v_pass_kernel<T><<<grid_v, kThreads, 0, s>>>(vdata, p.vunits, p.warp_begin, xt);
     nl++;
   }
   if (ev) cudaEventRecord(ev[2], s);
