@@ -8,11 +8,13 @@
 // first), leaf iff the node holds at most max_points_per_leaf points.
 //
 // Here the tree grows level by level, one CTA per node of the level:
-//   pass 1  bounding box (any order: only min/max) and the centroid sums; a sum
-//           is one floating-point chain in the points' current order, exactly
-//           as `sum(x; dims=2)` over the node's columns in src/tree.jl:83,
-//           kept sequential by one lane per axis while the other warps stage
-//           the next chunk of coordinates in shared memory;
+//   pass 1  bounding box (any order: only min/max, as ordered integer keys)
+//           and the centroid sums; a sum is one floating-point chain in the
+//           points' current order, exactly as `sum(x; dims=2)` over the node's
+//           columns in src/tree.jl:83, evaluated by one warp per axis 32
+//           values at a time (seq_sum32: an exact integer form of the chain
+//           while it stays in one binade, the plain chain otherwise) while the
+//           other warps stage the next chunk of coordinates in shared memory;
 //   pass 2  count of the points left of the centroid;
 //   pass 3  stable scatter of the point indices and their coordinates into the
 //           other buffer (left part in order, then the right part in order).
@@ -22,11 +24,13 @@
 // finish; the shared host step renumbers them into pre-order, so the slot order
 // does not matter.
 //
-// All arithmetic goes through the _rn intrinsics (no contraction); the norm is
-// LinearAlgebra.generic_norm2 of a 3-vector as in the host build.
+// All floating-point arithmetic goes through the _rn intrinsics (no
+// contraction); the norm is LinearAlgebra.generic_norm2 of a 3-vector as in the
+// host build. Comparisons of coordinates run on their bits as integers.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -64,18 +68,100 @@ struct Level {
   int32_t *ctl;  // [0] next-level slots taken, [1] error code, [2] size of the failed node
 };
 
-__device__ __forceinline__ double nan_min(double a, double b) {
-  return (isnan(a) || isnan(b)) ? __longlong_as_double(0x7ff8000000000000ll) : (b < a ? b : a);
-}
-__device__ __forceinline__ double nan_max(double a, double b) {
-  return (isnan(a) || isnan(b)) ? __longlong_as_double(0x7ff8000000000000ll) : (b > a ? b : a);
-}
-
 // Base.isless ordering used by argmax: NaN above all numbers.
 __device__ __forceinline__ bool isless_gt(double a, double b) {
   if (isnan(a)) return !isnan(b);
   if (isnan(b)) return false;
   return a > b;
+}
+
+// Bits of a double as an int64 that orders like the number (NaN excluded; -0
+// sorts just below +0, which no result here depends on).
+__device__ __forceinline__ long long ord_key(double v) {
+  const long long b = __double_as_longlong(v);
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double from_key(long long k) {
+  return __longlong_as_double(k >= 0 ? k : (k ^ 0x7fffffffffffffffll));
+}
+__device__ __forceinline__ bool is_nan_bits(long long b) {
+  return (b & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+// a < b for non-NaN doubles as integers (+0 and -0 equal)
+__device__ __forceinline__ long long less_key(double v) {
+  long long b = __double_as_longlong(v);
+  if (b == static_cast<long long>(0x8000000000000000ull)) b = 0;
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffll);
+}
+
+// The sequential sum s + v_0 + v_1 + ... + v_{cnt-1} (each addition rounded to
+// nearest even, left to right) of the values lane j holds, returned in every
+// lane; bit for bit the chain of __dadd_rn. Fast path: with s = S 2^e (S the
+// 53-bit significand), each step rounds S + v_j / 2^e to an integer as long as
+// the sum stays inside [2^52, 2^53): then the rounded increments r_j (integer
+// parts of v_j / 2^e, rounded to nearest) are independent of the order and
+// the partial sums are S plus a prefix sum of the r_j, computed by a warp
+// scan. The fast path is taken when every partial sum stays strictly inside
+// that range with a margin and no v_j / 2^e has a fractional part of exactly
+// one half (where the rounding would depend on the parity of the partial
+// sum); otherwise, and for zero, subnormal, infinite or NaN operands, the
+// values are added one by one.
+__device__ double seq_sum32(double s, double v, int cnt) {
+  const int lane = threadIdx.x & 31;
+  const long long sb = __double_as_longlong(s);
+  const int E = static_cast<int>((sb >> 52) & 0x7ff);
+  if (E != 0 && E != 0x7ff) {
+    const bool neg = sb < 0;
+    long long vb = __double_as_longlong(v);
+    if (neg) vb ^= static_cast<long long>(0x8000000000000000ull);  // the mirror image: RNE is symmetric
+    const int vexp = static_cast<int>((vb >> 52) & 0x7ff);
+    bool ok = vexp != 0x7ff, tie = false;
+    long long m = vb & 0x000fffffffffffffll;
+    int ve = vexp;
+    if (vexp != 0)
+      m |= 0x0010000000000000ll;
+    else
+      ve = 1;  // subnormal: m 2^(1 - 1075)
+    const int d = ve - E;  // v / 2^e = m 2^d
+    long long r = 0;
+    if (m != 0) {
+      if (d >= 0) {
+        if (d > 0)
+          ok = false;  // |v| >= 2^53 ulp: the sum leaves the binade (and no sum can overflow)
+        else
+          r = m;
+      } else if (-d < 62) {
+        const int sh = -d;
+        const long long q = m >> sh, rem = m & ((1ll << sh) - 1), half = 1ll << (sh - 1);
+        r = q + (rem > half ? 1 : 0);
+        tie = rem == half;
+      }  // else |v| < 2^-9 ulp: rounds to nothing, never a tie
+    }
+    if (vb < 0) r = -r;
+    if (lane >= cnt) {
+      r = 0;
+      ok = true;
+      tie = false;
+    }
+    long long pre = r;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += t;
+    }
+    const long long S = (sb & 0x000fffffffffffffll) | 0x0010000000000000ll;
+    const long long P = S + pre;
+    const bool inside = P >= 0x0010000000000001ll && P <= 0x001ffffffffffffell;
+    if (__all_sync(0xffffffffu, ok && !tie && inside)) {
+      const long long Pend = __shfl_sync(0xffffffffu, P, 31);
+      long long nb = (static_cast<long long>(E) << 52) | (Pend - 0x0010000000000000ll);
+      if (neg) nb |= static_cast<long long>(0x8000000000000000ull);
+      return __longlong_as_double(nb);
+    }
+  }
+  double acc = s;
+  for (int i = 0; i < cnt; i++) acc = __dadd_rn(acc, __shfl_sync(0xffffffffu, v, i));
+  return acc;
 }
 
 // LinearAlgebra.generic_norm2 of a 3-vector, as the host build computes it.
@@ -142,7 +228,9 @@ __device__ int block_exclusive_scan(int v, int *warp_tot, int *total) {
 
 __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
   __shared__ double stage[2][3][kChunk];
-  __shared__ double red_lo[kWarps][3], red_hi[kWarps][3], sums[3];
+  __shared__ long long red_lo[kWarps][3], red_hi[kWarps][3];
+  __shared__ int red_nan[kWarps];
+  __shared__ double sums[3];
   __shared__ double s_center;
   __shared__ int s_axis, s_split;
   __shared__ int warp_tot[kWarps + 1];
@@ -153,37 +241,41 @@ __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
   const double *src[3] = {L.cx + start, L.cy + start, L.cz + start};
 
   // ---- pass 1: bounding box and the three sequential sums -----------------
-  const double inf = __longlong_as_double(0x7ff0000000000000ll);
-  double lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
-  double acc = 0.0;  // lanes 0..2 of warp 0: the sum of axis `lane`
+  // warps 0..2 sum axis 0..2 (seq_sum32, 32 values per step); the other
+  // warps stage the next chunk and keep the box as ordered integer keys
+  constexpr int kSum = 3;
+  long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
+  int nan_seen = 0;
+  double acc = 0.0;  // warp a < 3: the sum of axis a
   const int nch = (cnt + kChunk - 1) / kChunk;
   for (int k = 0; k <= nch; k++) {
-    if (warp != 0) {
+    if (warp >= kSum) {
       if (k < nch) {
         const int base = k * kChunk, len = min(kChunk, cnt - base);
         double(*buf)[kChunk] = stage[k & 1];
-        for (int i = tid - 32; i < len; i += kTreeThreads - 32) {
+        for (int i = tid - 32 * kSum; i < len; i += kTreeThreads - 32 * kSum) {
 #pragma unroll
           for (int a = 0; a < 3; a++) {
             const double v = src[a][base + i];
             buf[a][i] = v;
-            lo[a] = nan_min(lo[a], v);
-            hi[a] = nan_max(hi[a], v);
+            const long long b = __double_as_longlong(v);
+            if (is_nan_bits(b)) {
+              nan_seen |= 1 << a;
+            } else {
+              const long long kk = ord_key(v);
+              lo[a] = kk < lo[a] ? kk : lo[a];
+              hi[a] = kk > hi[a] ? kk : hi[a];
+            }
           }
         }
       }
-    } else if (lane < 3 && k > 0) {
+    } else if (k > 0) {
       const int base = (k - 1) * kChunk, len = min(kChunk, cnt - base);
-      const double *row = stage[(k - 1) & 1][lane];
-      int i = 0;
-      for (; i + 8 <= len; i += 8) {
-        double v[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) v[j] = row[i + j];
-#pragma unroll
-        for (int j = 0; j < 8; j++) acc = __dadd_rn(acc, v[j]);
+      const double *row = stage[(k - 1) & 1][warp];
+      for (int i0 = 0; i0 < len; i0 += 32) {
+        const int n = min(32, len - i0);
+        acc = seq_sum32(acc, lane < n ? row[i0 + lane] : 0.0, n);
       }
-      for (; i < len; i++) acc = __dadd_rn(acc, row[i]);
     }
     __syncthreads();
   }
@@ -191,27 +283,35 @@ __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
   for (int a = 0; a < 3; a++) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      lo[a] = nan_min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-      hi[a] = nan_max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+      const long long ol = __shfl_xor_sync(0xffffffffu, lo[a], o), oh = __shfl_xor_sync(0xffffffffu, hi[a], o);
+      lo[a] = ol < lo[a] ? ol : lo[a];
+      hi[a] = oh > hi[a] ? oh : hi[a];
     }
   }
-  if (lane == 0)
+  nan_seen = __reduce_or_sync(0xffffffffu, nan_seen);
+  if (lane == 0) {
     for (int a = 0; a < 3; a++) {
       red_lo[warp][a] = lo[a];
       red_hi[warp][a] = hi[a];
     }
-  if (warp == 0 && lane < 3) sums[lane] = acc;
+    red_nan[warp] = nan_seen;
+  }
+  if (warp < kSum && lane == 0) sums[warp] = acc;
   __syncthreads();
   if (tid == 0) {
     double blo[3], bhi[3], len[3];
     DNode nd;
+    int nans = 0;
+    for (int w = 0; w < kWarps; w++) nans |= red_nan[w];
     for (int a = 0; a < 3; a++) {
-      blo[a] = red_lo[1][a];
-      bhi[a] = red_hi[1][a];
-      for (int w = 2; w < kWarps; w++) {
-        blo[a] = nan_min(blo[a], red_lo[w][a]);
-        bhi[a] = nan_max(bhi[a], red_hi[w][a]);
+      long long kl = LLONG_MAX, kh = LLONG_MIN;
+      for (int w = 0; w < kWarps; w++) {
+        kl = red_lo[w][a] < kl ? red_lo[w][a] : kl;
+        kh = red_hi[w][a] > kh ? red_hi[w][a] : kh;
       }
+      const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+      blo[a] = (nans >> a) & 1 ? qnan : from_key(kl);  // minimum/maximum propagate NaN
+      bhi[a] = (nans >> a) & 1 ? qnan : from_key(kh);
       len[a] = __dsub_rn(bhi[a], blo[a]);
       nd.center[a] = __ddiv_rn(sums[a], static_cast<double>(cnt));
     }
@@ -239,12 +339,17 @@ __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
     for (int i = tid; i < cnt; i += kTreeThreads) L.final_perm[start + i] = L.cperm[start + i];
     return;
   }
-  const double c = s_center;
+  // v < c as integers: never true for a NaN on either side
+  const bool c_nan = isnan(s_center);
+  const long long ck = less_key(s_center);
   const double *key = s_axis == 0 ? src[0] : (s_axis == 1 ? src[1] : src[2]);
+  auto left_of = [&](double v) {
+    return !c_nan && !is_nan_bits(__double_as_longlong(v)) && less_key(v) < ck;
+  };
 
   // ---- pass 2: size of the left part ---------------------------------------
   int nleft = 0;
-  for (int i = tid; i < cnt; i += kTreeThreads) nleft += key[i] < c ? 1 : 0;
+  for (int i = tid; i < cnt; i += kTreeThreads) nleft += left_of(key[i]) ? 1 : 0;
   int nl = 0;
   block_exclusive_scan(nleft, warp_tot, &nl);
   if (nl == 0 || nl == cnt) {  // a coincident cluster: the host reports it
@@ -266,7 +371,7 @@ __global__ void __launch_bounds__(kTreeThreads) tree_level_kernel(Level L) {
     int nf = 0;
 #pragma unroll
     for (int j = 0; j < kItems; j++) {
-      f[j] = i0 + j < cnt && key[i0 + j] < c;
+      f[j] = i0 + j < cnt && left_of(key[i0 + j]);
       nf += f[j] ? 1 : 0;
     }
     int step_total = 0;

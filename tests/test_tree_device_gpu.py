@@ -45,6 +45,12 @@ CASES = [
     ("flat_plane", lambda: geometry.square_z0(3000), 24, 1),
     ("huge_offsets", lambda: geometry.cube(2000, seed=8) * 1e150 + 1e160, 16, 1),
     ("tiny_scale", lambda: geometry.cube(2000, seed=9) * 1e-160, 16, 1),
+    # centroid sums with exact ties at half units, sign changes and wide ranges
+    ("half_units", lambda: np.round(np.random.default_rng(10).uniform(-50, 50, (3, 30000)) * 2) / 2, 20, 1),
+    ("mixed_scales", lambda: np.random.default_rng(11).standard_normal((3, 30000))
+     * np.exp2(np.random.default_rng(12).integers(-30, 30, (3, 30000))), 20, 1),
+    ("small_then_large", lambda: np.concatenate([np.random.default_rng(13).uniform(0, 4, (3, 20000)),
+                                                 np.random.default_rng(14).uniform(500, 520, (3, 20000))], 1), 32, 1),
 ]
 
 
