@@ -49,6 +49,24 @@ __device__ __forceinline__ void ld4(const T *p, T (&v)[4]) {
   }
 }
 
+template <typename T, int N>
+__device__ __forceinline__ void ldsn(const T *p, T (&v)[N]) {
+  if constexpr (sizeof(T) == 4) {
+#pragma unroll
+    for (int q = 0; q < N / 4; q++) {
+      const float4 a = reinterpret_cast<const float4 *>(p)[q];
+      v[4 * q] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < N / 2; q++) {
+      const double2 a = reinterpret_cast<const double2 *>(p)[q];
+      v[2 * q] = a.x;
+      v[2 * q + 1] = a.y;
+    }
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void lds8(const T *p, T (&v)[8]) {
   if constexpr (sizeof(T) == 4) {
@@ -100,11 +118,12 @@ __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_grou
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // One panel of m <= 128 rows (row-major, stride lda, rows padded with zeros to
-// a multiple of 4 columns) times the W-wide XT rows of its columns. Thread
-// layout: RQ = ceil(m / 4) row quads x W/8 groups of 8 right-hand sides x S
-// column slices (S = 256 / (RQ W/8)); a thread keeps 4 x 8 accumulators and
-// steps 4 columns at a time (four 16-byte loads of A, eight 16-byte shared
-// loads of XT rows, 128 FMAs). `stage(c0, cn, xs)` issues the asynchronous
+// a multiple of 4 columns) times the W-wide XT rows of its columns. A thread
+// keeps TR rows x TW right-hand sides of accumulators (4 x 8 for W = 8, 2 x 16
+// otherwise, so that fewer threads load the same A entries); the layout is
+// ceil(m / TR) row groups x W / TW right-hand-side groups x S column slices,
+// and a thread steps 4 columns at a time (TR 16-byte loads of A, 4 TW values
+// of XT rows from shared memory, 4 TR TW FMAs). `stage(c0, cn, xs)` issues the asynchronous
 // copies (cp16) of the XT rows of columns [c0, c0 + cn) into xs; the XT rows of
 // the next CC columns are copied into the other half of `buf` while the FMAs
 // of the current ones run. The slices meet in shared memory in slice order.
@@ -112,21 +131,24 @@ template <typename T, int W, typename Stage, typename Emit>
 __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int ncols_pad, T *buf,
                                             Stage stage, Emit emit) {
   constexpr int CC = Cols<T, W>::value;
+  constexpr int TW = W == 8 ? 8 : 16;  // right-hand sides per thread
+  constexpr int TR = 32 / TW;          // rows per thread
+  constexpr int G = W / TW;            // threads sharing a row group (each loads its A)
   T *red = buf;
   const int tid = threadIdx.x;
-  const int RQ = (m + 3) / 4, per = RQ * (W / 8);
+  const int RQ = (m + TR - 1) / TR, per = RQ * G;
   int S = kThreads / per;
   if (S < 1) S = 1;
   const int ks = tid / per, r = tid - ks * per, rq = r % RQ, rg = r / RQ;
   const bool active = ks < S;
-  T acc[4][8];
+  T acc[TR][TW];
 #pragma unroll
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < TR; i++)
 #pragma unroll
-    for (int j = 0; j < 8; j++) acc[i][j] = T(0);
-  bool ok[4];
+    for (int j = 0; j < TW; j++) acc[i][j] = T(0);
+  bool ok[TR];
 #pragma unroll
-  for (int i = 0; i < 4; i++) ok[i] = rq * 4 + i < m;
+  for (int i = 0; i < TR; i++) ok[i] = rq * TR + i < m;
   const int nst = (ncols_pad + CC - 1) / CC;
   __syncthreads();  // buf free (the previous panel's slice sums are read)
   if (nst > 0) stage(0, min(CC, ncols_pad), buf);
@@ -141,27 +163,27 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
     if (active) {
       // the A entries of the next step are loaded before this step's FMAs
       const int step = 4 * S;
-      auto load = [&](int c, T (&d)[4][4]) {
+      auto load = [&](int c, T (&d)[TR][4]) {
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
+        for (int i = 0; i < TR; i++) {
           if (ok[i] && c < cn)
-            ld4(A + static_cast<int64_t>(rq * 4 + i) * lda + c0 + c, d[i]);
+            ld4(A + static_cast<int64_t>(rq * TR + i) * lda + c0 + c, d[i]);
           else
             d[i][0] = d[i][1] = d[i][2] = d[i][3] = T(0);
         }
       };
-      auto step_fma = [&](int c, const T (&a)[4][4]) {
+      auto step_fma = [&](int c, const T (&a)[TR][4]) {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-          T b[8];
-          lds8(xs + (c + k) * W + rg * 8, b);
+          T b[TW];
+          ldsn<T, TW>(xs + (c + k) * W + rg * TW, b);
 #pragma unroll
-          for (int i = 0; i < 4; i++)
+          for (int i = 0; i < TR; i++)
 #pragma unroll
-            for (int j = 0; j < 8; j++) acc[i][j] = fma(a[i][k], b[j], acc[i][j]);
+            for (int j = 0; j < TW; j++) acc[i][j] = fma(a[i][k], b[j], acc[i][j]);
         }
       };
-      T a0[4][4], a1[4][4];
+      T a0[TR][4], a1[TR][4];
       int c = 4 * ks;
       load(c, a0);
       while (c < cn) {
@@ -178,14 +200,14 @@ __device__ __forceinline__ void multi_panel(const T *A, int64_t lda, int m, int 
   __syncthreads();  // red aliases xs
   if (active)
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < TR; i++)
 #pragma unroll
-      for (int j = 0; j < 8; j++) red[((ks * RQ + rq) * 4 + i) * W + rg * 8 + j] = acc[i][j];
+      for (int j = 0; j < TW; j++) red[((ks * RQ + rq) * TR + i) * W + rg * TW + j] = acc[i][j];
   __syncthreads();
   for (int o = tid; o < m * W; o += kThreads) {
     const int row = o / W, q = o % W;
     T s = T(0);
-    for (int sl = 0; sl < S; sl++) s += red[(sl * RQ * 4 + row) * W + q];
+    for (int sl = 0; sl < S; sl++) s += red[(sl * RQ * TR + row) * W + q];
     emit(row, q, s);
   }
 }
