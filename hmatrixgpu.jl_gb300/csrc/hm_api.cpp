@@ -306,7 +306,7 @@ extern "C" int hmgpu_hmatrix_import_flat(const hmgpu_options *opt, int64_t m, in
     return hm::fail(HMGPU_ERR_INVALID, "matrix size out of range");
   if (nD < 0 || nA < 0 || R < 0 || dense_len < 0 || U_len < 0 || V_len < 0)
     return hm::fail(HMGPU_ERR_INVALID, "negative count");
-  hmgpu_options o{HMGPU_F32, 0, 0, 0};
+  hmgpu_options o{HMGPU_F32, 0, 0, 0, nullptr};
   if (opt) o = *opt;
   if (o.precision != HMGPU_F64 && o.precision != HMGPU_F32 && o.precision != HMGPU_MIXED)
     return hm::fail(HMGPU_ERR_INVALID, "unknown precision mode");
@@ -667,8 +667,8 @@ extern "C" int hmgpu_hmatrix_block_factors(const hmgpu_hmatrix *h, int64_t blk, 
     return hm::fail(HMGPU_ERR_INVALID, "block index out of range");
   int64_t mb = b.a_re[blk] - b.a_rs[blk], nb = b.a_ce[blk] - b.a_cs[blk], r = b.a_r[blk];
   cudaError_t e = cudaSuccess;
-  if (U && mb * r) e = cudaMemcpy(U, H.u64 + H.u_src_off[blk], mb * r * 8, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess && V && nb * r)
+  if (U && mb * r > 0) e = cudaMemcpy(U, H.u64 + H.u_src_off[blk], mb * r * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && V && nb * r > 0)
     e = cudaMemcpy(V, H.v64 + H.v_src_off[blk], nb * r * 8, cudaMemcpyDeviceToHost);
   return e == cudaSuccess ? HMGPU_OK : hm::cuda_fail(e, "copying factors");
 }

@@ -20,7 +20,7 @@ struct DenseGenerator {
 
 struct HMatrix {
   int device = 0;
-  hmgpu_options opt{HMGPU_F32, 0, 0, 0};
+  hmgpu_options opt{HMGPU_F32, 0, 0, 0, nullptr};
   BlockSet bs;
   Plan plan;
   DevPlan dp;

@@ -949,7 +949,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   *out = nullptr;
   const Tree &X = Xh->t;
   const Tree &Y = Yh->t;
-  hmgpu_options o{HMGPU_F32, 0, 0, 0};
+  hmgpu_options o{HMGPU_F32, 0, 0, 0, nullptr};
   if (opt) o = *opt;
   if (o.precision != HMGPU_F64 && o.precision != HMGPU_F32 && o.precision != HMGPU_MIXED)
     return fail(HMGPU_ERR_INVALID, "unknown precision mode");

@@ -67,25 +67,10 @@ __device__ __forceinline__ void ldsn(const T *p, T (&v)[N]) {
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void lds8(const T *p, T (&v)[8]) {
-  if constexpr (sizeof(T) == 4) {
-    const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-  } else {
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const double2 a = reinterpret_cast<const double2 *>(p)[q];
-      v[2 * q] = a.x;
-      v[2 * q + 1] = a.y;
-    }
-  }
-}
-
 // XT rows from X in its own order: X[j + r ldx] goes to XT[sinv[j] W + r]
 // (0 for r >= nr). Reads of X are coalesced along j and every XT row is written
-// whole; the x-region rows that no source index maps to stay zero (the buffer
-// is cleared whenever the pass width changes). Also re-arms both ticket counters.
+// whole; the x-region rows that no source index maps to stay zero (every pass
+// width has its own XT, zeroed once). Also re-arms both ticket counters.
 template <typename T, int W>
 __global__ void permute_multi_kernel(const T *__restrict__ X, int64_t ldx, int nr,
                                      const int32_t *__restrict__ sinv0, int64_t n_src,

@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
         if (elect_one()) {
           for (int h = 0; h < two; h++) {
             const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
-            const uint64_t db = sdesc(su32(S.b[s2[h]]), kBGroupK, kBGroupN);
+            const uint64_t db = sdesc(su32(S.b[s2[h]]), kBLbo, kBSbo);
             for (int ks = 0; ks < kc2[h] / 16; ks++) {
               // the start address field counts 16-byte units
               const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4, ob = static_cast<uint64_t>(ks * 2 * kBGroupK) >> 4;
