@@ -342,3 +342,12 @@ extern "C" int hmgpu_hmatrix_tuning(const hmgpu_hmatrix *h, int32_t *v, int32_t 
   for (int32_t i = 0; i < n && i < 4; i++) v[i] = all[i];
   return HMGPU_OK;
 }
+
+extern "C" int hmgpu_hmatrix_set_tuning(hmgpu_hmatrix *h, const int32_t *v, int32_t n) {
+  if (!h || !v || n < 4) return hm::fail(HMGPU_ERR_INVALID, "need H and 4 values");
+  HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  if ((v[0] != 8 && v[0] != 16) || (v[1] != 32 && v[1] != 64 && v[1] != 128) || v[2] < 2 || (v[3] != 0 && v[3] != 1))
+    return hm::fail(HMGPU_ERR_INVALID, "tuning values out of range (unit rows 8|16, V unit KiB 32|64|128, "
+                                       "multi-RHS threshold >= 2, V schedule 0|1)");
+  return apply(H, v[0], v[1], v[2], v[3]);
+}

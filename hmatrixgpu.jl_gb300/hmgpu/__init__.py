@@ -445,6 +445,11 @@ class HMatrix:
         out["v_schedule"] = "dynamic" if self.tuning()["v_dynamic"] else "static"
         return out
 
+    def set_tuning(self, unit_rows, vunit_kib, multi_rhs_from, v_dynamic):
+        """Sets the product parameters directly (hmgpu_hmatrix_set_tuning)."""
+        v = (C.c_int32 * 4)(int(unit_rows), int(vunit_kib), int(multi_rhs_from), int(v_dynamic))
+        check(lib().hmgpu_hmatrix_set_tuning(self._h, v, 4))
+
     def tuning(self):
         """The product parameters in force (hmgpu_hmatrix_tuning)."""
         v = (C.c_int32 * 4)()

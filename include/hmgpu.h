@@ -325,6 +325,9 @@ int hmgpu_hmatrix_autotune(hmgpu_hmatrix *H, const char *cache_path, int32_t *re
  * a byte-balanced range of V units, 1: warps take V units from a ticket
  * counter; the autotuner times both). Writes min(n, 4) values. */
 int hmgpu_hmatrix_tuning(const hmgpu_hmatrix *H, int32_t *values, int32_t n);
+/* Sets those four parameters directly (for instance from an earlier autotune
+ * on the same structure); n must be 4. Results do not depend on them. */
+int hmgpu_hmatrix_set_tuning(hmgpu_hmatrix *H, const int32_t *values, int32_t n);
 
 /* An assembled H-matrix on disk (no counterpart in the reference; the
  * reference's flattened HMatrix has no file form): the device layout, index

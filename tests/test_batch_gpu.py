@@ -122,3 +122,26 @@ def test_autotune_keeps_results_and_caches(gpu, tmp_path):
     for k in range(6):
         yk = H * X[:, k].contiguous()
         assert float((Y[:, k] - yk).norm() / yk.norm()) < 1e-5
+
+
+def test_tuning_parameters_never_change_results(gpu):
+    """Every combination of near/U unit rows, V unit size and V schedule (byte-
+    balanced warp ranges or tickets) gives the same product bit for bit; bad
+    values are rejected."""
+    import torch
+    P = geometry.cube(20000, seed=21)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=32, gpu=True)
+    H = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=1e-6, precision="f32")
+    x = torch.randn(P.shape[1], device=gpu)
+    y0 = H * x
+    for ur in (8, 16):
+        for kib in (32, 64, 128):
+            for vd in (0, 1):
+                H.set_tuning(ur, kib, 3, vd)
+                assert H.tuning() == {"unit_rows": ur, "vunit_kib": kib, "multi_rhs_from": 3, "v_dynamic": bool(vd)}
+                assert torch.equal(H * x, y0), (ur, kib, vd)
+    with pytest.raises(hmgpu.HMGPUError):
+        H.set_tuning(12, 64, 3, 0)
+    with pytest.raises(hmgpu.HMGPUError):
+        H.set_tuning(16, 64, 3, 2)
+    assert H.status() == 0
