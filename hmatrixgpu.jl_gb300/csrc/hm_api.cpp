@@ -136,11 +136,13 @@ int upload_plan(HMatrix &H, const std::vector<int32_t> &tmap0, const std::vector
   return HMGPU_OK;
 }
 
-// Builds the product layout from the block set and the FP64 row-major factors
-// held on the device (d64: dense, u64/v64: low-rank; per-block offsets).
+// Builds the product layout from the block set and the row-major factors held
+// on the device (d64: dense, u64/v64: low-rank; per-block offsets). The
+// low-rank factors are FP64, or FP32 when src32 (FP32 storage with generated
+// dense blocks only).
 int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
-                    const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
-                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen) {
+                    const void *u64, const std::vector<int64_t> &u_src_off, const void *v64,
+                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen, bool src32) {
   const bool f64 = H.opt.precision == HMGPU_F64;
   int rc;
   PhaseClock clk;
@@ -162,7 +164,8 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   // pack panels
   PackJob *djobs = nullptr;
   if ((rc = upload(H, &djobs, p.pjobs))) return rc;
-  e = launch_pack_panels(f64, djobs, static_cast<int64_t>(p.pjobs.size()), d64, u64, H.panels, 0);
+  if (src32 && (f64 || d64)) return fail(HMGPU_ERR_INVALID, "FP32 factors need FP32 storage and generated dense blocks");
+  e = launch_pack_panels(f64, src32, djobs, static_cast<int64_t>(p.pjobs.size()), d64, u64, H.panels, 0);
   if (e != cudaSuccess) return cuda_fail(e, "pack panels");
   if (gen) {
     rc = gen->generate(H, djobs, static_cast<int64_t>(p.pjobs.size()));
@@ -183,7 +186,7 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   }
   VPackJob *dvj = nullptr;
   if ((rc = upload(H, &dvj, vj))) return rc;
-  e = launch_pack_v(f64, dvj, static_cast<int64_t>(vj.size()), v64, H.vdata, 0);
+  e = launch_pack_v(f64, src32, dvj, static_cast<int64_t>(vj.size()), v64, H.vdata, 0);
   if (e != cudaSuccess) return cuda_fail(e, "pack V");
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "layout packing");

@@ -80,7 +80,7 @@ int build_tc(HMatrix &H);
 // The 8 rank-predictor features of admissible block (x, y) at tolerance eps.
 void block_features(const Node &x, const Node &y, double eps, float *f);
 int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &dense_src_off,
-                    const double *u64, const std::vector<int64_t> &u_src_off, const double *v64,
-                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen);
+                    const void *u_src, const std::vector<int64_t> &u_src_off, const void *v_src,
+                    const std::vector<int64_t> &v_src_off, DenseGenerator *gen, bool src32 = false);
 
 }  // namespace hm

@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cmath>
 #include <memory>
+#include <type_traits>
 
 #include <math_constants.h>
 
@@ -720,17 +721,27 @@ struct KernelGen : DenseGenerator {
 
 // Gather of the kept blocks' factors from the per-batch buffers into one
 // store: one warp per copy.
+template <typename E>
 struct CopyJob {
-  const double *src;
-  double *dst;
+  const E *src;
+  E *dst;
   int64_t n;
 };
 
-__global__ void __launch_bounds__(256) gather_kernel(const CopyJob *__restrict__ jobs, int64_t njobs) {
+// FP64 factors of one batch rounded to FP32 (FP32 storage keeps no FP64 copy).
+__global__ void __launch_bounds__(256) round_kernel(const double *__restrict__ src, float *__restrict__ dst,
+                                                   int64_t n) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    dst[i] = static_cast<float>(src[i]);
+}
+
+template <typename E>
+__global__ void __launch_bounds__(256) gather_kernel(const CopyJob<E> *__restrict__ jobs, int64_t njobs) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < njobs; w += warps) {
-    const CopyJob j = jobs[w];
+    const CopyJob<E> j = jobs[w];
     for (int64_t i = lane; i < j.n; i += 32) j.dst[i] = j.src[i];
   }
 }
@@ -794,9 +805,9 @@ struct Compressor {
   // Processes jobs[idx] for idx in `sel`, writing results into res (indexed like jobs).
   // keep(jj, k, r) -> bool decides whether low-rank factors are written; factors
   // of kept blocks go to (ustore + uoff[jj], vstore + voff[jj]) allocated by `place`.
-  template <typename Keep, typename Place>
+  template <typename Keep, typename Place, typename After>
   int run(std::vector<AcaJob> &jobs, std::vector<AcaRes> &res, const std::vector<int> &sel,
-          Keep keep, Place place) {
+          Keep keep, Place place, After after) {
     size_t pos = 0;
     DevBuf ws, djobs, dres, dtick, duo, dvo;
     if (int rc = dtick.alloc(8 * sizeof(int32_t))) return rc;
@@ -871,6 +882,7 @@ struct Compressor {
                                            duo.as<int64_t>(), dvo.as<int64_t>(), ust, vst, tk + 4);
       e = cudaDeviceSynchronize();
       if (e != cudaSuccess) return cuda_fail(e, "factor formation");
+      if ((rc = after())) return rc;
     }
     return HMGPU_OK;
   }
@@ -1076,7 +1088,31 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
     *vst = vbufs.back()->as<double>();
     return HMGPU_OK;
   };
-  if ((rc = C.run(jobs, res, order, keep, place))) return rc;
+  // FP32 storage keeps no FP64 factors: each batch's factors are rounded to
+  // FP32 as soon as they are formed (half the memory of the build's factors)
+  const bool f32_factors = o.precision != HMGPU_F64 && !o.keep_factors;
+  std::vector<std::unique_ptr<DevBuf>> ubufs32, vbufs32;
+  size_t rounded = 0;  // batches already rounded
+  auto after = [&]() {
+    if (!f32_factors) return HMGPU_OK;
+    for (; rounded < ubufs.size(); rounded++) {
+      DevBuf *src[2] = {ubufs[rounded].get(), vbufs[rounded].get()};
+      for (int h = 0; h < 2; h++) {
+        std::unique_ptr<DevBuf> d(new DevBuf);
+        const int64_t len = static_cast<int64_t>(src[h]->cap / sizeof(double));
+        int r2;
+        if ((r2 = d->alloc(len * sizeof(float)))) return r2;
+        const int grid = static_cast<int>(std::min<int64_t>((len + 255) / 256, 152 * 32));
+        if (len > 0) round_kernel<<<grid, 256>>>(src[h]->as<double>(), d->as<float>(), len);
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "rounding factors");
+        src[h]->alloc(0);  // the FP64 copy is no longer needed
+        (h == 0 ? ubufs32 : vbufs32).push_back(std::move(d));
+      }
+    }
+    return HMGPU_OK;
+  };
+  if ((rc = C.run(jobs, res, order, keep, place, after))) return rc;
   // blocks that exhausted their workspace: rerun with room for min(m, n) terms
   std::vector<int> again;
   for (int a : order)
@@ -1084,7 +1120,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
       jobs[a].kcap = jobs[a].max_iter;
       again.push_back(a);
     }
-  if (!again.empty() && (rc = C.run(jobs, res, again, keep, place))) return rc;
+  if (!again.empty() && (rc = C.run(jobs, res, again, keep, place, after))) return rc;
   H.aca_batches = C.batches;
   H.aca_reruns = static_cast<int64_t>(again.size());
   H.aca_ws_bytes = C.ws_bytes;
@@ -1123,50 +1159,62 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
       bs.d_ce.push_back(j.cs + j.n);
     }
   }
-  // gather the factors into one FP64 store in block order
-  double *u64 = nullptr, *v64 = nullptr;
-  if ((rc = H.dalloc(reinterpret_cast<void **>(&u64), ulen * 8)) ||
-      (rc = H.dalloc(reinterpret_cast<void **>(&v64), vlen * 8)))
-    return rc;
+  // gather the factors into one store in block order (FP32 or FP64)
+  void *ust = nullptr, *vst = nullptr;
+  const size_t fes = f32_factors ? sizeof(float) : sizeof(double);
+  if ((rc = H.dalloc(&ust, ulen * fes)) || (rc = H.dalloc(&vst, vlen * fes))) return rc;
   {
-    std::vector<CopyJob> cj;
-    cj.reserve(2 * usrc.size());
-    size_t q = 0;
-    for (size_t a = 0; a < na; a++) {
-      if (!kept[a]) continue;
-      const int64_t r = res[a].r;
-      const int64_t un = static_cast<int64_t>(jobs[a].m) * r, vn = static_cast<int64_t>(jobs[a].n) * r;
-      if (un) cj.push_back(CopyJob{ubufs[buf_of[a]]->as<double>() + loc_u[a], u64 + usrc[q], un});
-      if (vn) cj.push_back(CopyJob{vbufs[buf_of[a]]->as<double>() + loc_v[a], v64 + vsrc[q], vn});
-      q++;
-    }
-    DevBuf dcj;
-    if ((rc = dcj.alloc(cj.size() * sizeof(CopyJob)))) return rc;
-    cudaError_t e = cudaMemcpy(dcj.p, cj.data(), cj.size() * sizeof(CopyJob), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && !cj.empty()) {
-      const int grid = static_cast<int>(std::min<int64_t>((static_cast<int64_t>(cj.size()) + 7) / 8, 152 * 16));
-      gather_kernel<<<grid, 256>>>(dcj.as<CopyJob>(), static_cast<int64_t>(cj.size()));
-      e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) return cuda_fail(e, "gathering factors");
+    auto gather = [&](auto *ud, auto *vd, auto getu, auto getv) -> int {
+      using E = std::remove_pointer_t<decltype(ud)>;
+      std::vector<CopyJob<E>> cj;
+      cj.reserve(2 * usrc.size());
+      size_t q = 0;
+      for (size_t a = 0; a < na; a++) {
+        if (!kept[a]) continue;
+        const int64_t r = res[a].r;
+        const int64_t un = static_cast<int64_t>(jobs[a].m) * r, vn = static_cast<int64_t>(jobs[a].n) * r;
+        if (un) cj.push_back(CopyJob<E>{getu(buf_of[a]) + loc_u[a], ud + usrc[q], un});
+        if (vn) cj.push_back(CopyJob<E>{getv(buf_of[a]) + loc_v[a], vd + vsrc[q], vn});
+        q++;
+      }
+      DevBuf dcj;
+      int r3;
+      if ((r3 = dcj.alloc(cj.size() * sizeof(CopyJob<E>)))) return r3;
+      cudaError_t e = cudaMemcpy(dcj.p, cj.data(), cj.size() * sizeof(CopyJob<E>), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess && !cj.empty()) {
+        const int grid = static_cast<int>(std::min<int64_t>((static_cast<int64_t>(cj.size()) + 7) / 8, 152 * 16));
+        gather_kernel<E><<<grid, 256>>>(dcj.as<CopyJob<E>>(), static_cast<int64_t>(cj.size()));
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      return e == cudaSuccess ? HMGPU_OK : cuda_fail(e, "gathering factors");
+    };
+    if (f32_factors)
+      rc = gather(static_cast<float *>(ust), static_cast<float *>(vst),
+                  [&](int b) { return ubufs32[b]->as<float>(); }, [&](int b) { return vbufs32[b]->as<float>(); });
+    else
+      rc = gather(static_cast<double *>(ust), static_cast<double *>(vst),
+                  [&](int b) { return ubufs[b]->as<double>(); }, [&](int b) { return vbufs[b]->as<double>(); });
+    if (rc) return rc;
   }
+  ubufs32.clear();
+  vbufs32.clear();
   ubufs.clear();
   vbufs.clear();
   H.build_phase[3] = clk.lap();
   std::vector<int64_t> dsrc(bs.d_rs.size(), -1);
   KernelGen gen;
   gen.K = K;
-  if ((rc = finalize_layout(H, nullptr, dsrc, u64, usrc, v64, vsrc, &gen))) return rc;
+  if ((rc = finalize_layout(H, nullptr, dsrc, ust, usrc, vst, vsrc, &gen, f32_factors))) return rc;
   if (o.keep_factors) {
-    H.u64 = u64;
-    H.v64 = v64;
+    H.u64 = static_cast<double *>(ust);
+    H.v64 = static_cast<double *>(vst);
     H.u_src_off = usrc;
     H.v_src_off = vsrc;
   } else {
-    H.dfree(u64);
-    H.dfree(v64);
-    H.device_bytes -= (ulen + vlen) * 8;
+    H.dfree(ust);
+    H.dfree(vst);
+    H.device_bytes -= (ulen + vlen) * static_cast<int64_t>(fes);
   }
   H.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   *out = reinterpret_cast<hmgpu_hmatrix *>(Hp.release());

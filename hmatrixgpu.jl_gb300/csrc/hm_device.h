@@ -49,14 +49,15 @@ cudaError_t launch_matvec(bool f64, bool comp, const DevPlan &p, const void *pan
                           const void *vdata, void *xt, const void *x, void *y, int grid_v,
                           int grid_du, cudaStream_t stream, cudaEvent_t *ev, int *launches);
 
-// Packing of FP64 row-major block factors into the product layout.
-cudaError_t launch_pack_panels(bool f64, const PackJob *jobs, int64_t njobs, const double *dsrc,
-                               const double *usrc, void *panels, cudaStream_t stream);
+// Packing of row-major block factors into the product layout: FP64 sources,
+// or FP32 sources (src32) for FP32 storage.
+cudaError_t launch_pack_panels(bool f64, bool src32, const PackJob *jobs, int64_t njobs, const void *dsrc,
+                               const void *usrc, void *panels, cudaStream_t stream);
 struct VPackJob {
   int64_t src_off, dst_off;
   int32_t n, r, stride, phase;
 };
-cudaError_t launch_pack_v(bool f64, const VPackJob *jobs, int64_t njobs, const double *vsrc,
+cudaError_t launch_pack_v(bool f64, bool src32, const VPackJob *jobs, int64_t njobs, const void *vsrc,
                           void *vdata, cudaStream_t stream);
 
 }  // namespace hm

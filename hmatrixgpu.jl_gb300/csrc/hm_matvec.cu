@@ -452,19 +452,19 @@ cudaError_t launch_matvec(bool f64, bool comp, const DevPlan &p, const void *pan
 }
 
 // ---------------------------------------------------------------------------
-// packing: FP64 row-major factors -> product layout (one warp per job)
+// packing: row-major factors (FP64, or FP32 for FP32 storage) -> product
+// layout (one warp per job)
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void pack_panels_kernel(const PackJob *__restrict__ jobs, int64_t njobs,
-                                   const double *__restrict__ dsrc, const double *__restrict__ usrc,
-                                   T *__restrict__ panels) {
+template <typename T, typename S>
+__global__ void pack_panels_kernel(const PackJob *__restrict__ jobs, int64_t njobs, const S *__restrict__ dsrc,
+                                   const S *__restrict__ usrc, T *__restrict__ panels) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t w = w0; w < njobs; w += nw) {
     const PackJob j = jobs[w];
     if (j.kind == 2) continue;
-    const double *src = (j.kind == 0 ? dsrc : usrc) + j.src_off;
+    const S *src = (j.kind == 0 ? dsrc : usrc) + j.src_off;
     for (int i = 0; i < j.m; i++)
       for (int c = lane; c < j.ncols; c += 32)
         panels[j.dst_off + static_cast<int64_t>(i) * j.dst_ld + c] =
@@ -472,9 +472,9 @@ __global__ void pack_panels_kernel(const PackJob *__restrict__ jobs, int64_t njo
   }
 }
 
-template <typename T>
-__global__ void pack_v_kernel(const VPackJob *__restrict__ jobs, int64_t njobs,
-                              const double *__restrict__ vsrc, T *__restrict__ vdata) {
+template <typename T, typename S>
+__global__ void pack_v_kernel(const VPackJob *__restrict__ jobs, int64_t njobs, const S *__restrict__ vsrc,
+                              T *__restrict__ vdata) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -488,29 +488,40 @@ __global__ void pack_v_kernel(const VPackJob *__restrict__ jobs, int64_t njobs,
   }
 }
 
-cudaError_t launch_pack_panels(bool f64, const PackJob *jobs, int64_t njobs, const double *dsrc,
-                               const double *usrc, void *panels, cudaStream_t s) {
+cudaError_t launch_pack_panels(bool f64, bool src32, const PackJob *jobs, int64_t njobs, const void *dsrc,
+                               const void *usrc, void *panels, cudaStream_t s) {
   if (njobs == 0) return cudaSuccess;
   int grid = static_cast<int>((njobs + 7) / 8);
   if (grid > 65535) grid = 65535;
-  if (f64)
-    pack_panels_kernel<double><<<grid, kThreads, 0, s>>>(jobs, njobs, dsrc, usrc,
-                                                         static_cast<double *>(panels));
+  if (src32)  // FP32 factors go to FP32 storage only
+    pack_panels_kernel<float, float><<<grid, kThreads, 0, s>>>(jobs, njobs, static_cast<const float *>(dsrc),
+                                                               static_cast<const float *>(usrc),
+                                                               static_cast<float *>(panels));
+  else if (f64)
+    pack_panels_kernel<double, double><<<grid, kThreads, 0, s>>>(jobs, njobs, static_cast<const double *>(dsrc),
+                                                                 static_cast<const double *>(usrc),
+                                                                 static_cast<double *>(panels));
   else
-    pack_panels_kernel<float><<<grid, kThreads, 0, s>>>(jobs, njobs, dsrc, usrc,
-                                                        static_cast<float *>(panels));
+    pack_panels_kernel<float, double><<<grid, kThreads, 0, s>>>(jobs, njobs, static_cast<const double *>(dsrc),
+                                                                static_cast<const double *>(usrc),
+                                                                static_cast<float *>(panels));
   return cudaGetLastError();
 }
 
-cudaError_t launch_pack_v(bool f64, const VPackJob *jobs, int64_t njobs, const double *vsrc,
-                          void *vdata, cudaStream_t s) {
+cudaError_t launch_pack_v(bool f64, bool src32, const VPackJob *jobs, int64_t njobs, const void *vsrc, void *vdata,
+                          cudaStream_t s) {
   if (njobs == 0) return cudaSuccess;
   int grid = static_cast<int>((njobs + 7) / 8);
   if (grid > 65535) grid = 65535;
-  if (f64)
-    pack_v_kernel<double><<<grid, kThreads, 0, s>>>(jobs, njobs, vsrc, static_cast<double *>(vdata));
+  if (src32)
+    pack_v_kernel<float, float><<<grid, kThreads, 0, s>>>(jobs, njobs, static_cast<const float *>(vsrc),
+                                                          static_cast<float *>(vdata));
+  else if (f64)
+    pack_v_kernel<double, double><<<grid, kThreads, 0, s>>>(jobs, njobs, static_cast<const double *>(vsrc),
+                                                            static_cast<double *>(vdata));
   else
-    pack_v_kernel<float><<<grid, kThreads, 0, s>>>(jobs, njobs, vsrc, static_cast<float *>(vdata));
+    pack_v_kernel<float, double><<<grid, kThreads, 0, s>>>(jobs, njobs, static_cast<const double *>(vsrc),
+                                                           static_cast<float *>(vdata));
   return cudaGetLastError();
 }
 
