@@ -314,6 +314,89 @@ def cube_measurement(dev, steps, hbm):
             "rel_err_256_exact_rows": err, "rhs64": rhs64}
 
 
+def learned_measurement(dev):
+    """The learned rank predictor at scale: N = 2^20 points uniform in [0,1]^3,
+    Laplace, leaf 64, eta 2, tol 1e-4, FP32 storage. The MLP is trained on
+    (block features, ACA rank) pairs from plain device ACA runs on smaller
+    cube, film and sphere geometries (6000 to 65536 points, leaves of 32 and
+    64, tol 1e-4 and 1e-6); the matrix is then
+    assembled without and with it. Reported: assembly time and phases, ACA
+    workspace, batches, blocks rerun after outgrowing their predicted cap (the
+    misprediction rate), bitwise equality of the two products, the product
+    time and the error of 256 rows against exact kernel sums. At tol 1e-6 the
+    same cube would hold about four times the low-rank entries (about 500 GB),
+    more than one GPU has, so only tol 1e-4 is run."""
+    import torch
+
+    import hmgpu
+    from tests import geometry
+    t0 = time.time()
+    feats, ranks = [], []
+    for Pg, leaf in ((geometry.cube(6000, seed=1), 32), (geometry.film(80, 80), 32), (geometry.sphere(6000, seed=2), 32),
+                     (geometry.cube(1 << 16, seed=3), 64), (geometry.film(256, 256, seed=4), 64),
+                     (geometry.sphere(1 << 16, seed=6), 64)):
+        Tg = hmgpu.ClusterTree(Pg, max_points_per_leaf=leaf, gpu=True)
+        for eps in (1e-4, 1e-6):
+            Hg = hmgpu.HMatrix(hmgpu.Kernel("laplace", Pg), Tg, Tg, eta=2.0, eps=eps, precision="f32")
+            f = hmgpu.block_features(Tg, Tg, 2.0, eps)
+            a, _ = Hg.aca_ranks(len(f))
+            feats.append(f)
+            ranks.append(a.astype(np.float32))
+            del Hg
+    X = np.concatenate(feats)
+    y = np.concatenate(ranks)
+    model = hmgpu.RankModel(seed=1)
+    loss = model.train(X, y, epochs=60, batch=512, lr=2e-3, seed=1)
+    train_s = time.time() - t0
+    P = geometry.cube(1 << 20, seed=5)
+    n = P.shape[1]
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=64, gpu=True)
+    x = torch.randn(n, device=dev, generator=torch.Generator(dev).manual_seed(17))
+    out = {"workload": "cube-2^20 Laplace leaf64 eta2 tol1e-4, FP32 storage, 1 RHS",
+           "training": {"samples": int(len(y)), "final_loss": float(loss), "seconds": train_s}}
+    y_first = None
+    for name, rm in (("plain", None), ("learned", model)):
+        t1 = time.time()
+        H = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=1e-4, precision="f32", rank_model=rm)
+        torch.cuda.synchronize()
+        build = time.time() - t1
+        inf = H.info()
+        yv = torch.empty(n, device=dev)
+        for _ in range(3):
+            hmgpu.mul_(yv, H, x)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s.record()
+        for _ in range(10):
+            hmgpu.mul_(yv, H, x)
+        e.record()
+        torch.cuda.synchronize()
+        rec = {"build_seconds": build, "build": H.build_profile(), "aca_batches": inf["aca_batches"],
+               "aca_workspace_gb": inf["aca_workspace_bytes"] / 1e9, "aca_reruns": inf["aca_reruns"],
+               "misprediction_rate": inf["aca_reruns"] / max(1, inf["admissible_leaves"]),
+               "lowrank_blocks": inf["admissible_leaves"], "dense_blocks": inf["full_leaves"],
+               "stored_gb": inf["matrix_bytes"] / 1e9, "ms_per_product": s.elapsed_time(e) / 10}
+        if y_first is None:
+            y_first = yv.clone()
+            rows = np.random.default_rng(18).choice(n, 256, replace=False)
+            xs, ys, Pt = x.double().cpu().numpy(), yv.double().cpu().numpy(), P.T
+            exact = np.empty(len(rows))
+            for k, i in enumerate(rows):
+                r = np.linalg.norm(Pt - Pt[i], axis=1)
+                w = np.zeros(n)
+                nz = r > 0
+                w[nz] = 1.0 / (4.0 * np.pi * r[nz])
+                exact[k] = w @ xs
+            rec["rel_err_256_exact_rows"] = float(np.linalg.norm(ys[rows] - exact) / np.linalg.norm(exact))
+        else:
+            rec["product_equals_plain_bitwise"] = bool(torch.equal(yv, y_first))
+        out[name] = rec
+        del H
+    out["workspace_ratio_learned_vs_plain"] = out["learned"]["aca_workspace_gb"] / max(out["plain"]["aca_workspace_gb"], 1e-9)
+    out["build_ratio_learned_vs_plain"] = out["learned"]["build_seconds"] / out["plain"]["build_seconds"]
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -486,6 +569,7 @@ def run_gpu(args):
     achieved = du_bytes / (du_ms * 1e-3) / 1e9
     batch32 = None if args.skip_batch else batch_measurement(dev, args.steps)
     cube18 = None if args.skip_cube else cube_measurement(dev, args.steps, hbm)
+    learned = learned_measurement(dev) if args.learned else None
     cpu_v, cpu_d = cpu_sample(1, target_s=10.0, more_threads=(os.cpu_count() or 1,))
     value = job_rate(world, ms * 1e-3)
     line = {
@@ -520,6 +604,7 @@ def run_gpu(args):
         "rhs32": rhs32,
         "batch32": batch32,
         "cube18": cube18,
+        "learned_cube20": learned,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -538,6 +623,8 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="leave out the 32-H-matrix batch lines")
     ap.add_argument("--build-only", action="store_true", help="assemble the workload, print its build line, exit")
     ap.add_argument("--skip-cube", action="store_true", help="leave out the 2^18-cube tol 1e-6 line")
+    ap.add_argument("--learned", action="store_true",
+                    help="also assemble the 2^20 cube (tol 1e-4) without and with the learned rank predictor")
     args = ap.parse_args()
     set_grid(args.grid)
     if args.impl == "reference":

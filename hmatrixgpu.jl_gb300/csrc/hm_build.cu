@@ -1032,7 +1032,9 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
     for (size_t a = 0; a < na; a++) {
       const float p = std::isfinite(pred[a]) ? std::max(pred[a], 0.0f) : 1e9f;
       const int64_t cap = static_cast<int64_t>(std::ceil(1.25 * p)) + 4;
-      jobs[a].kcap = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(cap, jobs[a].max_iter)));
+      // never above the fixed cap: a prediction can only shrink the workspace
+      // (a block that needs more is rerun with room for min(m, n) terms either way)
+      jobs[a].kcap = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(cap, jobs[a].kcap)));
     }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
       if (jobs[a].kcap != jobs[b].kcap) return jobs[a].kcap > jobs[b].kcap;
