@@ -1115,16 +1115,23 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
     return HMGPU_OK;
   };
   if ((rc = C.run(jobs, res, order, keep, place, after))) return rc;
-  // blocks that exhausted their workspace: rerun with room for min(m, n) terms
-  std::vector<int> again;
-  for (int a : order)
-    if (res[a].flags & 2) {
-      jobs[a].kcap = jobs[a].max_iter;
-      again.push_back(a);
-    }
-  if (!again.empty() && (rc = C.run(jobs, res, again, keep, place, after))) return rc;
+  // blocks that exhausted their workspace are rerun, first with the fixed cap
+  // (blocks whose learned cap was below it), then with room for min(m, n) terms
+  int64_t reruns = 0;
+  for (int round = 0; round < 2; round++) {
+    std::vector<int> again;
+    for (int a : order)
+      if (res[a].flags & 2) {
+        const int32_t fixed = std::min(jobs[a].max_iter, 48);
+        jobs[a].kcap = jobs[a].kcap < fixed ? fixed : jobs[a].max_iter;
+        again.push_back(a);
+      }
+    if (again.empty()) break;
+    reruns += static_cast<int64_t>(again.size());
+    if ((rc = C.run(jobs, res, again, keep, place, after))) return rc;
+  }
   H.aca_batches = C.batches;
-  H.aca_reruns = static_cast<int64_t>(again.size());
+  H.aca_reruns = reruns;
   H.aca_ws_bytes = C.ws_bytes;
   H.build_phase[2] = clk.lap();
 
