@@ -132,7 +132,7 @@ def batch_measurement(dev, steps):
     members = []
     for i, N in enumerate(sizes):
         P = geometry.sphere(int(N), seed=100 + i)
-        T = hmgpu.ClusterTree(P, max_points_per_leaf=32)
+        T = hmgpu.ClusterTree(P, max_points_per_leaf=32, gpu=True)
         members.append(hmgpu.HMatrix(hmgpu.Kernel("yukawa", P), T, T, eta=1.5, eps=1e-5, precision="f32"))
     B = hmgpu.batch(members)
     build = time.time() - t0
