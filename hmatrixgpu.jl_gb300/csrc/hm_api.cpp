@@ -19,6 +19,7 @@ int cuda_fail(cudaError_t e, const char *what) {
 HMatrix::~HMatrix() {
   for (auto &q : prof_ev)
     for (cudaEvent_t e : q) cudaEventDestroy(e);
+  if (io_stream) cudaStreamDestroy(io_stream);
   release();
 }
 
@@ -521,11 +522,19 @@ extern "C" int hmgpu_matvec_host(hmgpu_hmatrix *h, const void *x, void *y, int64
   const size_t es = H.opt.precision == HMGPU_F64 ? 8 : 4;
   int rc = H.ensure_io(nrhs * H.bs.n * es, nrhs * H.bs.m * es);
   if (rc) return rc;
-  cudaError_t e = cudaMemcpy2D(H.io_x, H.bs.n * es, x, ldx * es, H.bs.n * es, nrhs, cudaMemcpyDefault);
+  cudaError_t e = cudaSuccess;
+  // a blocking stream: ordered after work on the legacy default stream, as the
+  // default stream itself would be
+  if (!H.io_stream && (e = cudaStreamCreateWithFlags(&H.io_stream, cudaStreamDefault)) != cudaSuccess)
+    return hm::cuda_fail(e, "creating the copy stream");
+  // copy in, product, copy out on one stream, then one wait (pinned host
+  // buffers make both copies asynchronous)
+  e = cudaMemcpy2DAsync(H.io_x, H.bs.n * es, x, ldx * es, H.bs.n * es, nrhs, cudaMemcpyDefault, H.io_stream);
   if (e != cudaSuccess) return hm::cuda_fail(e, "copying x to the device");
-  rc = hmgpu_matvec(h, H.io_x, H.io_y, nrhs, H.bs.n, H.bs.m, nullptr);
+  rc = hmgpu_matvec(h, H.io_x, H.io_y, nrhs, H.bs.n, H.bs.m, H.io_stream);
   if (rc) return rc;
-  e = cudaMemcpy2D(y, ldy * es, H.io_y, H.bs.m * es, H.bs.m * es, nrhs, cudaMemcpyDefault);
+  e = cudaMemcpy2DAsync(y, ldy * es, H.io_y, H.bs.m * es, H.bs.m * es, nrhs, cudaMemcpyDefault, H.io_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(H.io_stream);
   if (e != cudaSuccess) return hm::cuda_fail(e, "copying y to the host");
   return HMGPU_OK;
 }

@@ -42,6 +42,7 @@ struct HMatrix {
   // staging of hmgpu_matvec_host
   void *io_x = nullptr, *io_y = nullptr;
   size_t io_x_bytes = 0, io_y_bytes = 0;
+  cudaStream_t io_stream = nullptr;  // hmgpu_matvec_host: copies and product in order, one wait
   // phase profiling (hmgpu_hmatrix_set_profiling)
   bool profiling = false;
   std::vector<std::array<cudaEvent_t, 4>> prof_ev;
