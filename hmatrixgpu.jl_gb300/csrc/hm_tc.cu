@@ -55,6 +55,8 @@ constexpr int kConsumers = kBProducers + 1 + 4;  // warps that read each queued 
 // apart from the release before.
 static_assert(kBProducers == kStages, "one producer warp per stage");
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kWaitIters = 1ull << 26;   // backstop if the timer stood still
+constexpr int kSelfTestCode = 90;                        // status of the self-test's wait
 
 // MN-major B with N = 64: the hi and lo halves of the 32 right-hand sides are
 // stacked along N, so one XTS row (128 bytes) is one K row of B. Core
@@ -150,19 +152,25 @@ __device__ __forceinline__ bool try_bar(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-__device__ __forceinline__ bool wait_bar(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
-                                         int code) {
+// The bounded wait itself: an iteration cap backs up the timer.
+__device__ __forceinline__ bool wait_bar_bounded(uint64_t *bar, uint32_t parity, volatile int32_t *abort,
+                                                 int32_t *status, int code, unsigned long long limit_ns) {
   if (try_bar(bar, parity)) return true;  // the common case reads no timer
   const unsigned long long t0 = now_ns();
-  for (;;) {
+  for (unsigned long long it = 0;; it++) {
     if (try_bar(bar, parity)) return true;
-    if (S.abort) return false;
-    if (now_ns() - t0 > kWaitNs) {
+    if (*abort) return false;
+    if (now_ns() - t0 > limit_ns || it > kWaitIters) {
       atomicCAS(status, 0, code);
-      S.abort = 1;
+      *abort = 1;
       return false;
     }
   }
+}
+
+__device__ __forceinline__ bool wait_bar(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
+                                         int code) {
+  return wait_bar_bounded(bar, parity, &S.abort, status, code, kWaitNs);
 }
 
 // wait_bar by every lane of a warp, with one answer for the whole warp
@@ -197,6 +205,21 @@ __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo) {
   hi = make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
   lo = make_uint4(pack2(v[0] - h[0], v[1] - h[1]), pack2(v[2] - h[2], v[3] - h[3]),
                   pack2(v[4] - h[4], v[5] - h[5]), pack2(v[6] - h[6], v[7] - h[7]));
+}
+
+// Self-test of the bounded wait: a barrier nobody arrives at, waited on with
+// a short limit; the wait must give up, record kSelfTestCode and return.
+__global__ void wait_selftest_kernel(unsigned long long limit_ns, int32_t *status, unsigned long long *waited) {
+  __shared__ uint64_t bar;
+  __shared__ int32_t abort_flag;
+  if (threadIdx.x != 0) return;
+  abort_flag = 0;
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&bar)));
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const unsigned long long t0 = now_ns();
+  const bool done = wait_bar_bounded(&bar, 0, &abort_flag, status, kSelfTestCode, limit_ns);
+  *waited = now_ns() - t0;
+  if (done) atomicCAS(status, 0, -1);  // the phase cannot complete
 }
 
 struct TcArgs {
@@ -598,3 +621,29 @@ cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, i
 }
 
 }  // namespace hm
+
+extern "C" int hmgpu_selftest_bounded_wait(int64_t limit_ns, int32_t *code, double *waited_ms) {
+  if (!code || !waited_ms) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
+  if (limit_ns < 1000000 || limit_ns > 2000000000)
+    return hm::fail(HMGPU_ERR_INVALID, "limit must lie in [1 ms, 2 s]");
+  int32_t *dst = nullptr;
+  unsigned long long *dw = nullptr;
+  cudaError_t e = cudaMalloc(&dst, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&dw, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(dst, 0, sizeof(int32_t));
+  if (e == cudaSuccess) {
+    hm::wait_selftest_kernel<<<1, 32>>>(static_cast<unsigned long long>(limit_ns), dst, dw);
+    e = cudaGetLastError();
+  }
+  int32_t st = 0;
+  unsigned long long w = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&st, dst, sizeof st, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&w, dw, sizeof w, cudaMemcpyDeviceToHost);
+  if (dst) cudaFree(dst);
+  if (dw) cudaFree(dw);
+  if (e != cudaSuccess)
+    return hm::fail(HMGPU_ERR_CUDA, std::string("bounded-wait self-test: ") + cudaGetErrorString(e));
+  *code = st;
+  *waited_ms = static_cast<double>(w) * 1e-6;
+  return HMGPU_OK;
+}

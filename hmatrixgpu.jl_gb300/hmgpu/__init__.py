@@ -604,3 +604,14 @@ def mul_(y, H, x, stream=None):
 def info(obj):
     """info(tree) / info(hmatrix)."""
     return obj.info()
+
+
+def selftest_bounded_wait(limit_ms=20.0):
+    """Runs the bounded device-side wait of the tensor-core product against a
+    barrier that nothing completes, limited to limit_ms. Returns (code, waited_ms):
+    code 90 means the wait expired and reported itself, as it must."""
+    L = lib()
+    code = C.c_int32(0)
+    waited = C.c_double(0.0)
+    check(L.hmgpu_selftest_bounded_wait(int(limit_ms * 1e6), C.byref(code), C.byref(waited)))
+    return code.value, waited.value

@@ -104,6 +104,7 @@ SIGNATURES = {
     "hmgpu_hmatrix_autotune": (C.c_int, [VP, C.c_char_p, C.POINTER(C.c_int32)]),
     "hmgpu_hmatrix_tuning": (C.c_int, [VP, C.POINTER(C.c_int32), C.c_int32]),
     "hmgpu_hmatrix_set_tuning": (C.c_int, [VP, C.POINTER(C.c_int32), C.c_int32]),
+    "hmgpu_selftest_bounded_wait": (C.c_int, [C.c_int64, C.POINTER(C.c_int32), F64P]),
     "hmgpu_hmatrix_save": (C.c_int, [VP, C.c_char_p]),
     "hmgpu_hmatrix_load": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
 }

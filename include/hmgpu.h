@@ -235,6 +235,13 @@ int hmgpu_hmatrix_build_profile(const hmgpu_hmatrix *H, double *seconds, int32_t
  * kernels completed, else the code of the first one that expired (then
  * returns HMGPU_ERR_TIMEOUT and clears the code). */
 int hmgpu_hmatrix_status(hmgpu_hmatrix *H, int *status);
+/* Self-test of the bounded device-side wait that the tensor-core product uses
+ * (no counterpart in the reference): one thread waits, with the same code
+ * path, on a barrier that nothing completes, limited to limit_ns (1 ms to
+ * 2 s). The wait must give up and record its code; *code receives the device
+ * status (90 when the wait expired as it should) and *waited_ms the device
+ * time spent waiting. The context stays usable afterwards. */
+int hmgpu_selftest_bounded_wait(int64_t limit_ns, int32_t *code, double *waited_ms);
 
 /* Phase timing (no counterpart in the reference): while on, every product
  * records CUDA events on its stream between its kernels.  phase_times
