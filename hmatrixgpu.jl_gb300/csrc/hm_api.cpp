@@ -450,21 +450,30 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
   };
   if (nrhs >= H.multi_from) {
     // several right-hand sides: one pass per rhs_per_pass() columns, the
-    // matrix read once per pass (hm_multi.cu; hm_tc.cu for mixed precision)
-    const int per = hm::rhs_per_pass();
+    // matrix read once per pass (hm_multi.cu); for mixed precision one pass
+    // per 64 columns on the tensor cores (hm_tc.cu), 32 wide when at most 32
+    // columns remain
     const bool tc = H.opt.precision == HMGPU_MIXED;
+    const int per = tc ? hm::kTcMaxRhs : hm::rhs_per_pass();
     int rc;
     if (tc && !H.tc.xts) {
-      if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts), H.plan.xt_len * 2 * per * 2)) ||
-          (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.prow), std::max<int64_t>(H.plan.p_rows, 1) * per * 4)))
+      const int64_t xb = H.plan.xt_len * 2 * 32 * 2;
+      if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts), xb)) ||
+          (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.prow),
+                         std::max<int64_t>(H.plan.p_rows, 1) * hm::kTcMaxRhs * 4)))
         return rc;
-      cudaMemset(H.tc.xts, 0, H.plan.xt_len * 2 * per * 2);
+      cudaMemsetAsync(H.tc.xts, 0, xb, s);
+    }
+    if (tc && nrhs > 32 && !H.tc.xts64) {
+      const int64_t xb = H.plan.xt_len * 2 * 64 * 2;
+      if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts64), xb))) return rc;
+      cudaMemsetAsync(H.tc.xts64, 0, xb, s);
     }
     if (!tc && !H.xt_multi) {
       if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es)) ||
           (rc = H.dalloc(&H.p_multi, std::max<int64_t>(H.plan.p_rows, 1) * per * es)))
         return rc;
-      cudaMemset(H.xt_multi, 0, H.plan.xt_len * per * es);
+      cudaMemsetAsync(H.xt_multi, 0, H.plan.xt_len * per * es, s);
       H.grid_du_multi = H.num_sms * hm::occupancy_du_multi(f64);
     }
     for (int64_t k0 = 0; k0 < nrhs; k0 += per) {
@@ -486,7 +495,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
           void *&xw = H.xt_multi_w[w == 8 ? 0 : 1];
           if (!xw) {
             if ((rc = H.dalloc(&xw, H.plan.xt_len * w * es))) return rc;
-            cudaMemset(xw, 0, H.plan.xt_len * w * es);
+            cudaMemsetAsync(xw, 0, H.plan.xt_len * w * es, s);
           }
           xt = xw;
         }

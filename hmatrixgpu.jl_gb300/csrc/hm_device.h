@@ -68,7 +68,8 @@ namespace hm {
 int rhs_per_pass();
 // Width (8, 16 or rhs_per_pass()) of the XT rows of a pass over nr columns.
 int multi_width(int nr);
-// Mixed-precision tensor-core product (hm_tc.cu), 32 right-hand sides per pass.
+// Mixed-precision tensor-core product (hm_tc.cu), 32 or 64 right-hand sides
+// per pass.
 struct TcPack {  // one item's FP32 row-major source -> canonical BF16 chunks
   int64_t src_off, a_off;
   int32_t ld, m, ncols, pad;
@@ -78,14 +79,17 @@ struct DevTc {
   TcItem *v_items = nullptr, *du_items = nullptr;
   int32_t *colmap = nullptr;
   MVReduce *reduce = nullptr;
-  uint16_t *xts = nullptr;  // xt_len rows of 32 BF16 hi + 32 BF16 lo
-  float *prow = nullptr;    // partial rows of split V items
+  uint16_t *xts = nullptr;    // xt_len rows of 32 BF16 hi + 32 BF16 lo (passes of <= 32 columns)
+  uint16_t *xts64 = nullptr;  // xt_len rows of 64 BF16 hi + 64 BF16 lo (passes of 33..64 columns)
+  float *prow = nullptr;      // partial rows of split V items, 64 values per row
   int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;
 };
-size_t tc_smem_bytes();
+constexpr int kTcMaxRhs = 64;  // right-hand sides of the widest pass
+size_t tc_smem_bytes(int nr);
 cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s);
-// permutation + split of X, V pass, reduction of pieces, near/U pass; ev
-// (optional) gets 4 events as launch_matvec_multi.
+// permutation + split of X, V pass, reduction of pieces, near/U pass over
+// nr <= 64 columns (xts64 must exist for nr > 32); ev (optional) gets 4
+// events as launch_matvec_multi.
 cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr,
                              float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches);
 

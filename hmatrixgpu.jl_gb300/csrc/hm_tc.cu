@@ -13,20 +13,24 @@
 // order, so concurrent CTAs work on neighbouring panels and share XTS rows in
 // L2; warp 0 takes the tickets and queues them for the other roles):
 //   warp 0      item tickets (lane 0), queued in shared memory for the others;
-//   warps 1, 3, 8-13  producers (chunk g to producer g mod 8) of an 8-stage
-//               ring of 64-column chunks: 16-byte cp.async copies of the chunk (hi rows to tile
-//               rows 0..63, lo rows to tile rows 64..127) and gathers of the
-//               XTS rows of its columns (whole 128-byte rows) into an N-major
-//               (MN-major) BF16 tile, then a wait, a proxy fence and an
-//               mbarrier arrive;
+//   producers   warps 1, 3 and 8.. (one per stage; chunk g to producer g mod
+//               the stage count) of a ring of 64-column chunks: two bulk
+//               copies of the chunk that complete on the stage's mbarrier (hi
+//               rows to tile rows 0..63, lo rows to tile rows 64..127), and
+//               16-byte cp.async gathers of the XTS rows of its columns (whole
+//               rows) into an N-major (MN-major) BF16 tile, then a wait, a
+//               proxy fence and an mbarrier arrive;
 //   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
-//               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 64 (hi and lo
+//               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 2R (hi and lo
 //               stacked along both M and N; items have at most 64 rows), into
-//               one of two 64-column TMEM accumulators (FP32); commits free the
-//               stage and, at the end of an item, hand the accumulator on;
-//   warps 4-7   epilogue: tcgen05.ld of TMEM lanes 32(w-4).., the sum of the
-//               four hi/lo quadrants, then y rows, t rows of XTS (split again)
-//               or partial rows P.
+//               one of two TMEM accumulators (FP32); commits free the stage
+//               and, at the end of an item, hand the accumulator on;
+//   epilogue    two sets of 4 warps (warps 4-7 and the last four), set e for
+//               accumulator e, that is every other item: tcgen05.ld of the
+//               warp's 32 TMEM lanes, the sum of the four hi/lo quadrants
+//               (the hi-row and lo-row warps of the same rows swap halves of
+//               their sums, so each finishes half of the right-hand sides),
+//               then y rows, t rows of XTS (split again) or partial rows P.
 // Every wait is bounded by the global timer; one that runs out records a code
 // in `status`, raises a CTA-wide abort flag and every role leaves its loop.
 #include <cuda_bf16.h>
@@ -38,34 +42,47 @@ namespace hm {
 
 namespace {
 
-constexpr int kTcWarps = 14;   // roles: see the header comment
-constexpr int kBProducers = 8;  // warps 1, 3, 8..13
-constexpr int kTcThreads = kTcWarps * 32;
-constexpr int kTcRhs = 32;
-constexpr int kKc = 64;             // columns per chunk
-constexpr int kStages = 8;
-constexpr int kABytes = 128 * kKc * 2;    // A tile: 64 hi rows, then 64 lo rows: 16 KB
-constexpr int kBN = 2 * kTcRhs;           // B rows: 32 hi right-hand sides, then 32 lo
-constexpr int kBBytes = kBN * kKc * 2;    // one BF16 B tile: 8 KB
-constexpr uint32_t kTmemCols = 128;       // two 64-column accumulators
-constexpr int kQ = 16;                    // item queue slots
-constexpr int kConsumers = kBProducers + 1 + 4;  // warps that read each queued item
-// One producer per stage: a producer then never waits for a stage more than one
-// release ahead, which a parity wait on the stage's barrier could not tell
-// apart from the release before.
-static_assert(kBProducers == kStages, "one producer warp per stage");
+constexpr int kKc = 64;                // columns per chunk
+constexpr int kABytes = 128 * kKc * 2;  // A tile: 64 hi rows, then 64 lo rows: 16 KB
+constexpr int kQ = 16;                  // item queue slots
+
+// MN-major B: the hi and lo halves of the R right-hand sides are stacked along
+// N, so one XTS row (4R bytes) is one K row of B. Core matrices of 8 N values
+// (16 B) x 8 columns; the N groups are kBGroupN bytes apart, the K groups of 8
+// columns TcShape<R>::kBGroupK bytes apart.
+constexpr uint32_t kBGroupN = 128;
+
+// The shape of a pass over R = 32 or 64 right-hand sides. A 64-wide pass reads
+// every tile once for twice the columns; its B tiles are twice as large, so
+// the ring has 6 stages instead of 8.
+template <int R>
+struct TcShape {
+  static_assert(R == 32 || R == 64, "32 or 64 right-hand sides per pass");
+  static constexpr int kBN = 2 * R;                   // B rows: R hi, then R lo
+  static constexpr int kBBytes = kBN * kKc * 2;       // one BF16 B tile: 8 or 16 KB
+  static constexpr int kStages = R == 32 ? 8 : 6;
+  static constexpr int kBProducers = kStages;         // warps 1, 3, 8 .. 5 + kStages
+  static constexpr int kEpi1 = 6 + kBProducers;       // first warp of the second epilogue set
+  static constexpr int kWarps = kEpi1 + 4;            // roles: see the header comment
+  static constexpr int kThreads = kWarps * 32;
+  static constexpr uint32_t kTmemCols = 2 * kBN;      // two accumulators
+  static constexpr int kConsumers = kBProducers + 1 + 8;  // warps that read each queued item
+  static constexpr uint32_t kBGroupK = (kBN / 8) * kBGroupN;
+  static constexpr int kPieces = R / 4;               // 16-byte pieces of an XTS row
+  static constexpr int kRowsPerCopy = 32 / kPieces;   // XTS rows per warp-wide copy
+  // kind::f16 instruction descriptor: FP32 D, BF16 A (K-major) and B
+  // (MN-major), N = kBN, M = 128.
+  static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) |
+                                     ((static_cast<uint32_t>(kBN) >> 3) << 17) | ((128u >> 4) << 24);
+  // One producer per stage: a producer then never waits for a stage more than
+  // one release ahead, which a parity wait on the stage's barrier could not
+  // tell apart from the release before.
+  static_assert(kBProducers == kStages, "one producer warp per stage");
+};
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr unsigned long long kWaitIters = 1ull << 26;   // backstop if the timer stood still
 constexpr int kSelfTestCode = 90;                        // status of the self-test's wait
 
-// MN-major B with N = 64: the hi and lo halves of the 32 right-hand sides are
-// stacked along N, so one XTS row (128 bytes) is one K row of B. Core
-// matrices of 8 N values (16 B) x 8 columns; the 8 N groups are kBGroupN
-// bytes apart, the K groups of 8 columns kBGroupK bytes apart.
-constexpr uint32_t kBGroupN = 128;
-constexpr uint32_t kBGroupK = 8 * kBGroupN;
-constexpr uint32_t kBLbo = kBGroupK;  // leading byte offset: K direction
-constexpr uint32_t kBSbo = kBGroupN;  // stride byte offset: N direction
 
 __device__ __forceinline__ uint32_t su32(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -80,16 +97,11 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t
   return d;
 }
 
-// kind::f16 instruction descriptor: FP32 D, BF16 A (K-major) and B (MN-major),
-// N = 64, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) |
-                            ((static_cast<uint32_t>(kBN) >> 3) << 17) | ((128u >> 4) << 24);
-
-__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
 __device__ __forceinline__ void commit(uint64_t *bar) {
@@ -122,22 +134,57 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "r"(taddr));
 }
 
+// 16 consecutive accumulator columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+// w[c] = D[.., t1 + c] + D[.., t2 + c] for c < N (N = 16 or 32): the products
+// with B_hi and with B_lo of the same right-hand sides.
+template <int N>
+__device__ __forceinline__ void tmem_sum(uint32_t t1, uint32_t t2, float (&w)[N]) {
+  uint32_t r[N], r2[N];
+  if constexpr (N == 32) {
+    tmem_ld32(t1, r);
+    tmem_ld32(t2, r2);
+  } else {
+    static_assert(N == 16, "16 or 32 columns");
+    tmem_ld16(t1, r);
+    tmem_ld16(t2, r2);
+  }
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int c = 0; c < N; c++) w[c] = __uint_as_float(r[c]) + __uint_as_float(r2[c]);
+}
+
 __device__ __forceinline__ unsigned long long now_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
+template <int R>
 struct TcSmem {
-  unsigned char a[kStages][kABytes];
-  unsigned char b[kStages][kBBytes];
-  float epi[64][kTcRhs + 1];  // lo-row sums handed from epilogue warps 6, 7 to 4, 5
-  uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], epi_ready, epi_free;
+  using Sh = TcShape<R>;
+  unsigned char a[Sh::kStages][kABytes];
+  unsigned char b[Sh::kStages][Sh::kBBytes];
+  // per epilogue set: halves of the row sums handed from the lo-row warps to
+  // the hi-row warps (xa) and back (xb)
+  float xa[2][64][R / 2 + 1], xb[2][64][R / 2 + 1];
+  uint64_t full[Sh::kStages], empty[Sh::kStages], acc_full[2], acc_empty[2];
+  uint64_t xa_ready[2], xa_free[2], xb_ready[2], xb_free[2];
   uint64_t qfull[kQ], qempty[kQ];
-  int32_t qitem[kQ];  // item queue: ticket order, -1 ends it
+  TcItem qdata[kQ];  // item queue: ticket order; kind -1 ends it
   uint32_t tmem;
   volatile int32_t abort;
 };
+// 1024 bytes of alignment slack on top; 232448 bytes is the per-block limit
+static_assert(sizeof(TcSmem<32>) + 1024 <= 232448 && sizeof(TcSmem<64>) + 1024 <= 232448,
+              "tensor-core pass shared memory");
 
 // Waits for the phase of `bar` with parity `parity`; false when the abort flag
 // is up or the time limit ran out (then the flag goes up and `code` is recorded).
@@ -168,26 +215,30 @@ __device__ __forceinline__ bool wait_bar_bounded(uint64_t *bar, uint32_t parity,
   }
 }
 
-__device__ __forceinline__ bool wait_bar(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
+template <class SM>
+__device__ __forceinline__ bool wait_bar(SM &S, uint64_t *bar, uint32_t parity, int32_t *status,
                                          int code) {
   return wait_bar_bounded(bar, parity, &S.abort, status, code, kWaitNs);
 }
 
 // wait_bar by every lane of a warp, with one answer for the whole warp
-__device__ __forceinline__ bool wait_bar_warp(TcSmem &S, uint64_t *bar, uint32_t parity, int32_t *status,
+template <class SM>
+__device__ __forceinline__ bool wait_bar_warp(SM &S, uint64_t *bar, uint32_t parity, int32_t *status,
                                               int code) {
   return __all_sync(0xffffffffu, wait_bar(S, bar, parity, status, code));
 }
 
-// Item n of this CTA from the queue (-1: no more items, or an abort); every
-// consumer warp calls it once per n and releases the slot.
-__device__ __forceinline__ int next_item(TcSmem &S, int n, int32_t *status) {
+// Item n of this CTA from the queue (false: no more items, or an abort); every
+// consumer warp calls it once per n and releases the slot. The item itself
+// travels in the queue, so no consumer waits on a global load per item.
+template <class SM>
+__device__ __forceinline__ bool next_item(SM &S, int n, int32_t *status, TcItem &I) {
   const int q = n % kQ;
-  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((n / kQ) & 1), status, 30)) return -1;
-  const int it = S.qitem[q];
+  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((n / kQ) & 1), status, 30)) return false;
+  I = S.qdata[q];
   __syncwarp();
   if ((threadIdx.x & 31) == 0) arrive(&S.qempty[q]);
-  return it;
+  return I.kind >= 0;
 }
 
 __device__ __forceinline__ int64_t chunk_bytes(int G, int kc) { return static_cast<int64_t>(G) * kc * 16; }
@@ -226,6 +277,7 @@ struct TcArgs {
   const unsigned char *adata;  // tensor-core panels
   const TcItem *items;
   int32_t nitems;
+  int32_t grab;                // items per ticket while many remain (1 or 8)
   int32_t *ticket;             // next item (zeroed by the permutation kernel)
   const int32_t *colmap;
   const uint16_t *xts;         // XTS rows (64 BF16 each)
@@ -240,9 +292,12 @@ struct TcArgs {
   int32_t *status;
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
+template <int R>
+__global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(TcArgs a) {
+  using Sh = TcShape<R>;
+  constexpr int kStages = Sh::kStages;
   extern __shared__ unsigned char smem_raw[];
-  TcSmem &S = *reinterpret_cast<TcSmem *>(
+  TcSmem<R> &S = *reinterpret_cast<TcSmem<R> *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -257,15 +312,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
     }
     for (int q = 0; q < kQ; q++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.qfull[q])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&S.qempty[q])), "r"(kConsumers));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(&S.qempty[q])), "r"(Sh::kConsumers));
     }
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.epi_ready)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.epi_free)));
+    for (int e = 0; e < 2; e++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.xa_ready[e])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.xa_free[e])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.xb_ready[e])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(su32(&S.xb_free[e])));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&S.tmem)),
-                 "r"(kTmemCols));
+                 "r"(Sh::kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -273,36 +332,61 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   if (warp == 0) {
-    // ---- A producer ---------------------------------------------------------
-    // ---- item tickets: lane 0 takes them and queues them for the others ----
-    if (lane == 0) {
-      for (int n = 0; !S.abort; n++) {
+    // ---- item tickets, queued with the items for the other roles -------------
+    // One atomic takes a.grab consecutive items while more than 16 per CTA
+    // remain (one ticket round trip per a.grab short items), single items
+    // after that so that the CTAs finish together. Lanes load the grabbed
+    // items in parallel; lane 0 writes each into its queue slot.
+    int n = 0, last = 0;
+    for (bool more = true; more;) {
+      const int want = last + 16 * static_cast<int>(gridDim.x) < a.nitems ? a.grab : 1;
+      int b = 0;
+      if (lane == 0) b = atomicAdd(a.ticket, want);
+      b = __shfl_sync(0xffffffffu, b, 0);
+      last = b;
+      TcItem mine{};
+      mine.kind = -1;
+      if (lane < want && b + lane < a.nitems) mine = a.items[b + lane];
+      for (int j = 0; j < want; j++, n++) {
+        TcItem t;
+        t.a_off = __shfl_sync(0xffffffffu, mine.a_off, j);
+        t.m = __shfl_sync(0xffffffffu, mine.m, j);
+        t.ncols = __shfl_sync(0xffffffffu, mine.ncols, j);
+        t.map = __shfl_sync(0xffffffffu, mine.map, j);
+        t.out = __shfl_sync(0xffffffffu, mine.out, j);
+        t.kind = __shfl_sync(0xffffffffu, mine.kind, j);
+        t.row0 = __shfl_sync(0xffffffffu, mine.row0, j);
         const int q = n % kQ;
-        if (!wait_bar(S, &S.qempty[q], static_cast<uint32_t>((n / kQ) & 1) ^ 1u, a.status, 29)) break;
-        int it = atomicAdd(a.ticket, 1);
-        if (it >= a.nitems) it = -1;
-        S.qitem[q] = it;
-        arrive(&S.qfull[q]);
-        if (it < 0) break;
+        if (!wait_bar_warp(S, &S.qempty[q], static_cast<uint32_t>((n / kQ) & 1) ^ 1u, a.status, 29)) {
+          more = false;
+          break;
+        }
+        if (lane == 0) {
+          S.qdata[q] = t;
+          arrive(&S.qfull[q]);
+        }
+        if (t.kind < 0) {
+          more = false;
+          break;
+        }
       }
     }
-  } else if (warp == 1 || warp == 3 || warp >= 8) {
-    // ---- producers: chunk g (stage g % 8) goes to producer g % 8 --------------
-    // Column rows are looked up before the stage is free; then each of kKc / 4
-    // instructions copies 4 whole XTS rows (8 lanes x 16 bytes per row), the
-    // warp waits for its copies, fences them for the tensor cores' proxy and
-    // publishes the stage.
-    const int bw = warp == 1 ? 0 : warp == 3 ? 1 : warp - 6;  // 0..7
-    int64_t g = 0;
+  } else if (warp == 1 || warp == 3 || (warp >= 8 && warp < Sh::kEpi1)) {
+    // ---- producers: chunk g (stage g % kStages) goes to producer g % kStages --
+    // Column rows are looked up before the stage is free; then each warp-wide
+    // copy moves kRowsPerCopy whole XTS rows (kPieces lanes x 16 bytes per
+    // row), the warp waits for its copies, fences them for the tensor cores'
+    // proxy and publishes the stage.
+    const int bw = warp == 1 ? 0 : warp == 3 ? 1 : warp - 6;  // 0..kStages-1
+    int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
     bool stop = false;
-    const int piece = lane & 7, sub = lane >> 3;
+    const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
     for (int n = 0; !stop; n++) {
-      const int it = next_item(S, n, a.status);
-      if (it < 0) break;
-      const TcItem I = a.items[it];
+      TcItem I;
+      if (!next_item(S, n, a.status, I)) break;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
-        if ((g & (kBProducers - 1)) != bw) continue;
+        if (g % kStages != bw) continue;
         const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
         int rows[kKc / 32];  // XTS rows of columns c0 + lane + 32 h
 #pragma unroll
@@ -315,31 +399,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
           stop = true;
           break;
         }
-        {  // A: the chunk's hi rows to tile rows 0.., its lo rows to tile rows 64..
-          // (read once: evict-first in L2, so the gathered XTS rows stay resident)
+        if (lane == 0) {
+          // A: the chunk's hi rows to tile rows 0.., its lo rows to tile rows
+          // 64..: two bulk copies that complete on the stage's barrier (read
+          // once: evict-first in L2, so the gathered XTS rows stay resident)
           uint64_t pol;
           asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
           const int G = (I.m + 7) >> 3;
-          const int units = G * kc;  // 16-byte units of each half
+          const uint32_t half = static_cast<uint32_t>(G * kc * 16);
           const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
           const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
-          for (int u = lane; u < units; u += 32) {
-            asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(hi + 16u * u),
-                         "l"(src + 16 * u), "l"(pol)
-                         : "memory");
-            asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(lo + 16u * u),
-                         "l"(src + 16 * (units + u)), "l"(pol)
-                         : "memory");
-          }
+          const uint32_t bar = su32(&S.full[s]);
+          asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2 * half) : "memory");
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(hi),
+              "l"(src), "r"(half), "r"(bar), "l"(pol)
+              : "memory");
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(lo),
+              "l"(src + half), "r"(half), "r"(bar), "l"(pol)
+              : "memory");
         }
+        last_g = g;
         const uint32_t dst0 = su32(S.b[s]) + piece * kBGroupN;
 #pragma unroll
-        for (int i = 0; i < kKc / 4; i++) {
-          const int k = 4 * i + sub;
-          const int r = __shfl_sync(0xffffffffu, rows[i >> 3], k & 31);
+        for (int i = 0; i < kKc / Sh::kRowsPerCopy; i++) {
+          const int k = Sh::kRowsPerCopy * i + sub;
+          const int r = __shfl_sync(0xffffffffu, rows[(i * Sh::kRowsPerCopy) >> 5], k & 31);
           if (k < kc) {
-            const uint16_t *src = a.xts + static_cast<int64_t>(r) * (2 * kTcRhs) + piece * 8;
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst0 + (k >> 3) * kBGroupK + (k & 7) * 16),
+            const uint16_t *src = a.xts + static_cast<int64_t>(r) * (2 * R) + piece * 8;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst0 + (k >> 3) * Sh::kBGroupK + (k & 7) * 16),
                          "l"(src)
                          : "memory");
           }
@@ -351,22 +440,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
         if (lane == 0) arrive(&S.full[s]);
       }
     }
+    // The bulk copies of this warp's last chunk land before the CTA can exit,
+    // aborted or not (one stage per producer: earlier chunks have landed).
+    if (last_g >= 0 && lane == 0) {
+      volatile int32_t none = 0;
+      wait_bar_bounded(&S.full[last_g % kStages], static_cast<uint32_t>((last_g / kStages) & 1), &none, a.status, 31,
+                       kWaitNs);
+    }
+    __syncwarp();
   } else if (warp == 2) {
     // ---- MMA issuer: the warp runs the loop, one elected lane issues --------
-    // Per 16 columns one UMMA: [A_hi; A_lo] (M = 128) x [B_hi B_lo] (N = 64)
+    // Per 16 columns one UMMA: [A_hi; A_lo] (M = 128) x [B_hi B_lo] (N = 2R)
     // into the item's accumulator; the epilogue adds its four quadrants.
     int64_t g = 0;
     int n = 0;
     bool stop = false;
     for (; !stop; n++) {
-      const int it = next_item(S, n, a.status);
-      if (it < 0) break;
-      const TcItem I = a.items[it];
+      TcItem I;
+      if (!next_item(S, n, a.status, I)) break;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       const int ab = n & 1;
       if (!wait_bar_warp(S, &S.acc_empty[ab], static_cast<uint32_t>((n >> 1) & 1) ^ 1u, a.status, 23)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t acc = S.tmem + ab * kBN;
+      const uint32_t acc = S.tmem + ab * Sh::kBN;
       // two chunks per turn where the item has them: one round of waits,
       // descriptors and hand-offs per 128 columns
       for (int c0 = 0; c0 < npad;) {
@@ -386,11 +482,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
         if (elect_one()) {
           for (int h = 0; h < two; h++) {
             const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
-            const uint64_t db = sdesc(su32(S.b[s2[h]]), kBLbo, kBSbo);
+            // leading byte offset: K direction; stride byte offset: N direction
+            const uint64_t db = sdesc(su32(S.b[s2[h]]), Sh::kBGroupK, kBGroupN);
             for (int ks = 0; ks < kc2[h] / 16; ks++) {
               // the start address field counts 16-byte units
-              const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4, ob = static_cast<uint64_t>(ks * 2 * kBGroupK) >> 4;
-              mma(acc, da + oa, db + ob, ((c0 + h * kKc) | ks) ? 1u : 0u);
+              const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
+                             ob = static_cast<uint64_t>(ks * 2 * Sh::kBGroupK) >> 4;
+              mma(acc, da + oa, db + ob, Sh::kIdesc, ((c0 + h * kKc) | ks) ? 1u : 0u);
             }
             commit(&S.empty[s2[h]]);
           }
@@ -406,100 +504,107 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_kernel(TcArgs a) {
     // the last stage release must land before the CTA's shared memory goes away
     if (!stop && g > 0)
       wait_bar_warp(S, &S.empty[(g - 1) % kStages], static_cast<uint32_t>(((g - 1) / kStages) & 1), a.status, 26);
-  } else if (warp >= 4 && warp < 8) {
+  } else if ((warp >= 4 && warp < 8) || warp >= Sh::kEpi1) {
     // ---- epilogue -----------------------------------------------------------
-    // Warp w reads TMEM lanes 32(w-4)..: warps 4, 5 hold the A_hi rows, warps
-    // 6, 7 the A_lo rows of the same panel rows. Warps 6, 7 hand their sums
-    // to 4, 5 through shared memory; 4, 5 add and write the results.
+    // Set e (warps 4-7 or the last four) takes accumulator e, that is items
+    // n = e, e + 2, ... Warp w reads TMEM lanes 32(w mod 4)..: quarters 0, 1
+    // hold the A_hi rows, quarters 2, 3 the A_lo rows of the same panel rows.
+    // The hi-row warp hands the sums of right-hand sides [H, R) to its lo-row
+    // partner and takes those of [0, H) from it (H = R / 2), so that each
+    // finishes and writes half of the row; sum = hi-row part + lo-row part
+    // either way.
+    constexpr int H = R / 2;
+    const int e = warp >= Sh::kEpi1 ? 1 : 0;
     const int quarter = warp & 3, row = (quarter & 1) * 32 + lane;
     const bool lo_part = quarter >= 2;
-    int n = 0;
-    for (;; n++) {
-      const int it = next_item(S, n, a.status);
-      if (it < 0) break;
-      const TcItem I = a.items[it];
-      const int ab = n & 1;
-      if (!wait_bar_warp(S, &S.acc_full[ab], static_cast<uint32_t>((n >> 1) & 1), a.status, 25)) break;
+    const int give = lo_part ? 0 : H, keep = lo_part ? H : 0;
+    float(*xo)[H + 1] = lo_part ? S.xa[e] : S.xb[e];  // written by this warp
+    float(*xi)[H + 1] = lo_part ? S.xb[e] : S.xa[e];  // read by this warp
+    uint64_t *o_ready = lo_part ? &S.xa_ready[e] : &S.xb_ready[e];
+    uint64_t *o_free = lo_part ? &S.xa_free[e] : &S.xb_free[e];
+    uint64_t *i_ready = lo_part ? &S.xb_ready[e] : &S.xa_ready[e];
+    uint64_t *i_free = lo_part ? &S.xb_free[e] : &S.xa_free[e];
+    for (int n = 0;; n++) {
+      TcItem I;
+      if (!next_item(S, n, a.status, I)) break;
+      if ((n & 1) != e) continue;
+      const uint32_t k = static_cast<uint32_t>(n >> 1);  // this set's item count
+      if (!wait_bar_warp(S, &S.acc_full[e], k & 1u, a.status, 25)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      uint32_t r[kTcRhs], r2[kTcRhs];
-      const uint32_t taddr = S.tmem + ab * kBN + (static_cast<uint32_t>(quarter * 32) << 16);
-      tmem_ld32(taddr, r);
-      tmem_ld32(taddr + kTcRhs, r2);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const uint32_t taddr = S.tmem + e * Sh::kBN + (static_cast<uint32_t>(quarter * 32) << 16);
+      float w[H];  // A_part B_hi + A_part B_lo over H right-hand sides
+      tmem_sum<H>(taddr + give, taddr + R + give, w);
+      if (!wait_bar_warp(S, o_free, (k & 1u) ^ 1u, a.status, 27)) break;
+#pragma unroll
+      for (int c = 0; c < H; c++) xo[row][c] = w[c];
+      __syncwarp();
+      if (lane == 0) arrive(o_ready);
+      tmem_sum<H>(taddr + keep, taddr + R + keep, w);
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) arrive(&S.acc_empty[ab]);
-      float v[kTcRhs];  // A_part B_hi + A_part B_lo
+      if (lane == 0) arrive(&S.acc_empty[e]);
+      if (!wait_bar_warp(S, i_ready, k & 1u, a.status, 28)) break;
 #pragma unroll
-      for (int q = 0; q < kTcRhs; q++) v[q] = __uint_as_float(r[q]) + __uint_as_float(r2[q]);
-      if (lo_part) {
-        if (!wait_bar_warp(S, &S.epi_free, static_cast<uint32_t>(n & 1) ^ 1u, a.status, 27)) break;
-#pragma unroll
-        for (int q = 0; q < kTcRhs; q++) S.epi[row][q] = v[q];
-        __syncwarp();
-        if (lane == 0) arrive(&S.epi_ready);
-        continue;
-      }
-      if (!wait_bar_warp(S, &S.epi_ready, static_cast<uint32_t>(n & 1), a.status, 28)) break;
-#pragma unroll
-      for (int q = 0; q < kTcRhs; q++) v[q] += S.epi[row][q];
+      for (int c = 0; c < H; c++) w[c] += xi[row][c];
       __syncwarp();
-      if (lane == 0) arrive(&S.epi_free);
+      if (lane == 0) arrive(i_free);
       if (row >= I.m) continue;
       if (I.kind == 0) {
         float *yr = a.y + a.tmap0[a.tiles[I.out].row0 + I.row0 + row];
 #pragma unroll
-        for (int q = 0; q < kTcRhs; q++)
-          if (q < a.nr) yr[q * a.ldy] = v[q];
+        for (int c = 0; c < H; c++)
+          if (keep + c < a.nr) yr[(keep + c) * a.ldy] = w[c];
       } else if (I.kind == 1) {
-        uint4 *dst = reinterpret_cast<uint4 *>(a.xts_out + static_cast<int64_t>(I.out + row) * (2 * kTcRhs));
+        uint4 *dst = reinterpret_cast<uint4 *>(a.xts_out + static_cast<int64_t>(I.out + row) * (2 * R)) + keep / 8;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < H / 8; q++) {
           uint4 hi, lo;
-          split8(v + 8 * q, hi, lo);
+          split8(w + 8 * q, hi, lo);
           dst[q] = hi;
-          dst[4 + q] = lo;
+          dst[R / 8 + q] = lo;
         }
       } else {
-        float4 *dst = reinterpret_cast<float4 *>(a.prow + static_cast<int64_t>(I.out + row) * kTcRhs);
+        float4 *dst = reinterpret_cast<float4 *>(a.prow + static_cast<int64_t>(I.out + row) * R + keep);
 #pragma unroll
-        for (int q = 0; q < 8; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        for (int q = 0; q < H / 4; q++) dst[q] = make_float4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(kTmemCols));
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(Sh::kTmemCols));
 }
 
-// XTS x rows from X in its own order: the 32 right-hand sides X[j + r ldx]
-// (0 for r >= nr) of source index j, split into BF16 hi (first 64 bytes) and lo
-// (last 64 bytes), go to row sinv[j]. Reads of X are coalesced along j and
+// XTS x rows from X in its own order: the R right-hand sides X[j + r ldx]
+// (0 for r >= nr) of source index j, split into BF16 hi (first 2R bytes) and
+// lo (last 2R bytes), go to row sinv[j]. Reads of X are coalesced along j and
 // every row is written whole; x-region rows that no source index maps to stay
 // zero from the allocation. Also re-arms the two item tickets.
+template <int R>
 __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, int nr,
                                      const int32_t *__restrict__ sinv0, int64_t n_src,
                                      uint16_t *__restrict__ xts, int32_t *__restrict__ tickets) {
-  __shared__ float tile[64][kTcRhs + 1];
+  __shared__ float tile[64][R + 1];
   if (blockIdx.x == 0 && threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
   for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
-    for (int e = threadIdx.x; e < 64 * kTcRhs; e += blockDim.x) {
+    for (int e = threadIdx.x; e < 64 * R; e += blockDim.x) {
       const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
       const int64_t j = j0 + jj;
       tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] : 0.0f;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 64 * 4; e += blockDim.x) {
-      const int jj = e >> 2, q = e & 3;
+    for (int e = threadIdx.x; e < 64 * (R / 8); e += blockDim.x) {
+      const int jj = e / (R / 8), q = e % (R / 8);
       if (j0 + jj < n_src) {
         float v[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) v[i] = tile[jj][8 * q + i];
         uint4 hi, lo;
         split8(v, hi, lo);
-        uint4 *dst = reinterpret_cast<uint4 *>(xts + static_cast<int64_t>(sinv0[j0 + jj]) * (2 * kTcRhs));
+        uint4 *dst = reinterpret_cast<uint4 *>(xts + static_cast<int64_t>(sinv0[j0 + jj]) * (2 * R));
         dst[q] = hi;
-        dst[4 + q] = lo;
+        dst[R / 8 + q] = lo;
       }
     }
     __syncthreads();
@@ -507,21 +612,25 @@ __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, i
 }
 
 // t rows from partial rows, pieces summed in order; one warp per row, lane =
-// right-hand side.
+// right-hand side (and lane + 32 in a 64-wide pass).
+template <int R>
 __global__ void reduce_split_kernel(const MVReduce *__restrict__ red, int32_t nred, const float *__restrict__ P,
                                     uint16_t *__restrict__ xts) {
   const int lane = threadIdx.x & 31;
   for (int32_t e = static_cast<int32_t>(blockIdx.x); e < nred; e += gridDim.x) {
-    const MVReduce R = red[e];
-    for (int row = threadIdx.x >> 5; row < R.nrows; row += blockDim.x >> 5) {
-      float s = 0.0f;
-      for (int j = 0; j < R.npieces; j++)
-        s += P[(static_cast<int64_t>(R.p_row) + static_cast<int64_t>(j) * R.nrows + row) * kTcRhs + lane];
-      const __nv_bfloat16 hb = __float2bfloat16_rn(s);
-      const __nv_bfloat16 lb = __float2bfloat16_rn(s - __bfloat162float(hb));
-      uint16_t *dst = xts + static_cast<int64_t>(R.t_row + row) * (2 * kTcRhs);
-      dst[lane] = *reinterpret_cast<const uint16_t *>(&hb);
-      dst[kTcRhs + lane] = *reinterpret_cast<const uint16_t *>(&lb);
+    const MVReduce D = red[e];
+    for (int row = threadIdx.x >> 5; row < D.nrows; row += blockDim.x >> 5) {
+      uint16_t *dst = xts + static_cast<int64_t>(D.t_row + row) * (2 * R);
+#pragma unroll
+      for (int c = lane; c < R; c += 32) {
+        float s = 0.0f;
+        for (int j = 0; j < D.npieces; j++)
+          s += P[(static_cast<int64_t>(D.p_row) + static_cast<int64_t>(j) * D.nrows + row) * R + c];
+        const __nv_bfloat16 hb = __float2bfloat16_rn(s);
+        const __nv_bfloat16 lb = __float2bfloat16_rn(s - __bfloat162float(hb));
+        dst[c] = *reinterpret_cast<const uint16_t *>(&hb);
+        dst[R + c] = *reinterpret_cast<const uint16_t *>(&lb);
+      }
     }
   }
 }
@@ -557,13 +666,67 @@ __global__ void pack_tc_kernel(const TcPack *__restrict__ jobs, const float *__r
 
 }  // namespace
 
-size_t tc_smem_bytes() { return sizeof(TcSmem) + 1024; }
+template <int R>
+static size_t smem_bytes() {
+  return sizeof(TcSmem<R>) + 1024;
+}
+size_t tc_smem_bytes(int nr) { return nr > 32 ? smem_bytes<64>() : smem_bytes<32>(); }
 
 static void tc_attrs() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(tc_smem_bytes()));
+  cudaFuncSetAttribute(tc_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_bytes<32>()));
+  cudaFuncSetAttribute(tc_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem_bytes<64>()));
   done = true;
+}
+
+template <int R>
+static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr, float *Y, int64_t ldy,
+                  cudaStream_t s, cudaEvent_t *ev) {
+  using Sh = TcShape<R>;
+  uint16_t *xts = R == 64 ? t.xts64 : t.xts;
+  int nl = 0;
+  int gp = static_cast<int>((p.n_src + 63) / 64);
+  if (gp > 2048) gp = 2048;
+  if (ev) cudaEventRecord(ev[0], s);
+  permute_split_kernel<R><<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xts, p.counter + 2);
+  nl++;
+  if (ev) cudaEventRecord(ev[1], s);
+  TcArgs a{};
+  a.adata = static_cast<const unsigned char *>(t.adata);
+  a.colmap = t.colmap;
+  a.xts = xts;
+  a.xts_out = xts;
+  a.prow = t.prow;
+  a.tiles = p.tiles;
+  a.tmap0 = p.tmap0;
+  a.y = Y;
+  a.ldy = ldy;
+  a.nr = nr;
+  a.zero_row = static_cast<int32_t>(p.zero_row);
+  a.status = p.status;
+  const size_t smem = smem_bytes<R>();
+  if (t.n_v > 0) {
+    a.items = t.v_items;
+    a.nitems = t.n_v;
+    a.grab = 8;  // V pieces are short: a few chunks each
+    a.ticket = p.counter + 2;
+    tc_kernel<R><<<t.ctas, Sh::kThreads, smem, s>>>(a);
+    nl++;
+    if (t.n_reduce > 0) {
+      reduce_split_kernel<R><<<t.n_reduce < 4096 ? t.n_reduce : 4096, 256, 0, s>>>(t.reduce, t.n_reduce, t.prow, xts);
+      nl++;
+    }
+  }
+  if (ev) cudaEventRecord(ev[2], s);
+  a.items = t.du_items;
+  a.nitems = t.n_du;
+  a.grab = 1;  // row tiles are long; single tickets keep neighbouring tiles together
+  a.ticket = p.counter + 3;
+  tc_kernel<R><<<t.ctas, Sh::kThreads, smem, s>>>(a);
+  nl++;
+  if (ev) cudaEventRecord(ev[3], s);
+  return nl;
 }
 
 cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s) {
@@ -576,46 +739,9 @@ cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, 
 
 cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr,
                              float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches) {
+  if (nr < 1 || nr > 64 || (nr > 32 && !t.xts64) || !t.xts) return cudaErrorInvalidValue;
   tc_attrs();
-  int nl = 0;
-  int gp = static_cast<int>((p.n_src + 63) / 64);
-  if (gp > 2048) gp = 2048;
-  if (ev) cudaEventRecord(ev[0], s);
-  permute_split_kernel<<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, t.xts, p.counter + 2);
-  nl++;
-  if (ev) cudaEventRecord(ev[1], s);
-  TcArgs a{};
-  a.adata = static_cast<const unsigned char *>(t.adata);
-  a.colmap = t.colmap;
-  a.xts = t.xts;
-  a.xts_out = t.xts;
-  a.prow = t.prow;
-  a.tiles = p.tiles;
-  a.tmap0 = p.tmap0;
-  a.y = Y;
-  a.ldy = ldy;
-  a.nr = nr;
-  a.zero_row = static_cast<int32_t>(p.zero_row);
-  a.status = p.status;
-  const size_t smem = tc_smem_bytes();
-  if (t.n_v > 0) {
-    a.items = t.v_items;
-    a.nitems = t.n_v;
-    a.ticket = p.counter + 2;
-    tc_kernel<<<t.ctas, kTcThreads, smem, s>>>(a);
-    nl++;
-    if (t.n_reduce > 0) {
-      reduce_split_kernel<<<t.n_reduce < 4096 ? t.n_reduce : 4096, 256, 0, s>>>(t.reduce, t.n_reduce, t.prow, t.xts);
-      nl++;
-    }
-  }
-  if (ev) cudaEventRecord(ev[2], s);
-  a.items = t.du_items;
-  a.nitems = t.n_du;
-  a.ticket = p.counter + 3;
-  tc_kernel<<<t.ctas, kTcThreads, smem, s>>>(a);
-  nl++;
-  if (ev) cudaEventRecord(ev[3], s);
+  const int nl = nr > 32 ? run_tc<64>(p, t, X, ldx, nr, Y, ldy, s, ev) : run_tc<32>(p, t, X, ldx, nr, Y, ldy, s, ev);
   if (launches) *launches = nl;
   return cudaGetLastError();
 }

@@ -185,7 +185,8 @@ def test_mixed_tensor_core_many_rhs(case, gpu):
     import torch
     _, _, Ho = case
     H = hmgpu.HMatrix.from_flat(**_flat(Ho), precision="mixed")
-    for nr in (32, 40, 3):
+    # 32: one 32-wide pass; 40, 64: one 64-wide pass; 70: a 64-wide and a 32-wide pass
+    for nr in (32, 40, 64, 70, 3):
         X = np.random.default_rng(nr).standard_normal((Ho.n, nr))
         Xd = torch.tensor(X, dtype=torch.float32, device=gpu).t().contiguous().t()
         Y = (H * Xd).double().cpu().numpy()
