@@ -46,9 +46,9 @@ extern "C" {
 #define HMGPU_MIXED 2 /* FP32 factors with compensated FP32 accumulation for
                          few right-hand sides; for more, a copy of every block
                          as BF16 pairs hi + lo (hi = bf16(a), lo = bf16(a - hi))
-                         multiplied on the tensor cores with FP32 accumulation
-                         (the threshold is hmgpu_hmatrix_autotune's); x, y are
-                         float                                                 */
+                         multiplied on the tensor cores with FP32 accumulation,
+                         one pass per 64 right-hand sides (the threshold is
+                         hmgpu_hmatrix_autotune's); x, y are float             */
 
 /* matrix entry generators for on-device assembly */
 #define HMGPU_KERNEL_EXPLICIT 0  /* entries of a given column-major matrix        */
