@@ -225,6 +225,7 @@ int build_tc(HMatrix &H) {
   t.n_du = static_cast<int32_t>(tp.du_items.size());
   t.n_reduce = H.dp.nmvr;
   t.ctas = H.num_sms;
+  t.xt_rows = H.plan.xt_len;
   std::vector<TcPack> vj, dj;
   for (size_t i = 0; i < tp.v_items.size(); i++) {
     const MVItem &it = H.plan.mv_items[i];
@@ -463,11 +464,13 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
                          std::max<int64_t>(H.plan.p_rows, 1) * hm::kTcMaxRhs * 4)))
         return rc;
       cudaMemsetAsync(H.tc.xts, 0, xb, s);
+      if (cudaError_t e = hm::encode_xts_map(H.tc, 32)) return hm::cuda_fail(e, "tensor map of XTS");
     }
     if (tc && nrhs > 32 && !H.tc.xts64) {
       const int64_t xb = H.plan.xt_len * 2 * 64 * 2;
       if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts64), xb))) return rc;
       cudaMemsetAsync(H.tc.xts64, 0, xb, s);
+      if (cudaError_t e = hm::encode_xts_map(H.tc, 64)) return hm::cuda_fail(e, "tensor map of XTS");
     }
     if (!tc && !H.xt_multi) {
       if ((rc = H.dalloc(&H.xt_multi, H.plan.xt_len * per * es)) ||

@@ -1,5 +1,6 @@
 // Device-side launchers of libhmgpu (implemented in the .cu files).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "hm_internal.h"
@@ -83,9 +84,14 @@ struct DevTc {
   uint16_t *xts64 = nullptr;  // xt_len rows of 64 BF16 hi + 64 BF16 lo (passes of 33..64 columns)
   float *prow = nullptr;      // partial rows of split V items, 64 values per row
   int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;
+  int64_t xt_rows = 0;  // rows of either XTS
+  CUtensorMap xmap[2];  // tile-load maps of xts and xts64 (encode_xts_map)
 };
 constexpr int kTcMaxRhs = 64;  // right-hand sides of the widest pass
 size_t tc_smem_bytes(int nr);
+// The tile-load map of the XTS of width R (32: xts, 64: xts64), after the
+// buffer exists.
+cudaError_t encode_xts_map(DevTc &t, int R);
 cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s);
 // permutation + split of X, V pass, reduction of pieces, near/U pass over
 // nr <= 64 columns (xts64 must exist for nr > 32); ev (optional) gets 4

@@ -33,6 +33,8 @@
 //               then y rows, t rows of XTS (split again) or partial rows P.
 // Every wait is bounded by the global timer; one that runs out records a code
 // in `status`, raises a CTA-wide abort flag and every role leaves its loop.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -274,6 +276,7 @@ __global__ void wait_selftest_kernel(unsigned long long limit_ns, int32_t *statu
 }
 
 struct TcArgs {
+  CUtensorMap xmap;            // XTS as 8 BF16 x rows x N groups: the B tiles of V pieces
   const unsigned char *adata;  // tensor-core panels
   const TcItem *items;
   int32_t nitems;
@@ -293,7 +296,7 @@ struct TcArgs {
 };
 
 template <int R>
-__global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(TcArgs a) {
+__global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __grid_constant__ TcArgs a) {
   using Sh = TcShape<R>;
   constexpr int kStages = Sh::kStages;
   extern __shared__ unsigned char smem_raw[];
@@ -410,7 +413,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(TcArgs a) {
           const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
           const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
           const uint32_t bar = su32(&S.full[s]);
-          asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2 * half) : "memory");
+          const uint32_t btx = I.kind != 0 ? static_cast<uint32_t>(Sh::kBBytes) : 0u;
+          asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2 * half + btx)
+                       : "memory");
           asm volatile(
               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(hi),
               "l"(src), "r"(half), "r"(bar), "l"(pol)
@@ -419,8 +424,24 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(TcArgs a) {
               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(lo),
               "l"(src + half), "r"(half), "r"(bar), "l"(pol)
               : "memory");
+          if (I.kind != 0) {
+            // B of a V piece: its columns are the consecutive XTS rows map + c0
+            // .., so one tile load of 64 rows (rows past the end read as zero)
+            // lands them in the canonical MN-major layout (K groups 128 B
+            // apart, N groups 1024 B apart)
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(su32(S.b[s])),
+                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bar)
+                : "memory");
+            arrive(&S.full[s]);
+          }
         }
         last_g = g;
+        if (I.kind != 0) {  // the copies complete on the stage's barrier
+          __syncwarp();
+          continue;
+        }
         const uint32_t dst0 = su32(S.b[s]) + piece * kBGroupN;
 #pragma unroll
         for (int i = 0; i < kKc / Sh::kRowsPerCopy; i++) {
@@ -482,12 +503,16 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(TcArgs a) {
         if (elect_one()) {
           for (int h = 0; h < two; h++) {
             const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
-            // leading byte offset: K direction; stride byte offset: N direction
-            const uint64_t db = sdesc(su32(S.b[s2[h]]), Sh::kBGroupK, kBGroupN);
+            // leading byte offset: K direction; stride byte offset: N direction.
+            // V pieces' B tiles come from the tile load (K groups 128 B apart,
+            // N groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B).
+            const bool tma_b = I.kind != 0;
+            const uint64_t db = tma_b ? sdesc(su32(S.b[s2[h]]), 128, 1024)
+                                      : sdesc(su32(S.b[s2[h]]), Sh::kBGroupK, kBGroupN);
             for (int ks = 0; ks < kc2[h] / 16; ks++) {
               // the start address field counts 16-byte units
               const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
-                             ob = static_cast<uint64_t>(ks * 2 * Sh::kBGroupK) >> 4;
+                             ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
               mma(acc, da + oa, db + ob, Sh::kIdesc, ((c0 + h * kKc) | ks) ? 1u : 0u);
             }
             commit(&S.empty[s2[h]]);
@@ -680,6 +705,31 @@ static void tc_attrs() {
   done = true;
 }
 
+cudaError_t encode_xts_map(DevTc &t, int R) {
+  // cuTensorMapEncodeTiled through the runtime's driver entry point (no
+  // link-time dependence on the driver library)
+  static PFN_cuTensorMapEncodeTiled_v12000 enc = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  uint16_t *xts = R == 64 ? t.xts64 : t.xts;
+  if (!enc || !xts || t.xt_rows < 1 || (R != 32 && R != 64)) return cudaErrorInvalidValue;
+  // element (e, row, g) = XTS[row][8 g + e]: a box of 8 x 64 x 2R/8 lands as
+  // 2R/8 N groups of 64 rows x 16 bytes
+  cuuint64_t dims[3] = {8, static_cast<cuuint64_t>(t.xt_rows), static_cast<cuuint64_t>(2 * R / 8)};
+  cuuint64_t strides[2] = {static_cast<cuuint64_t>(4 * R), 16};
+  cuuint32_t box[3] = {8, 64, static_cast<cuuint32_t>(2 * R / 8)};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = enc(&t.xmap[R / 64], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, xts, dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 template <int R>
 static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr, float *Y, int64_t ldy,
                   cudaStream_t s, cudaEvent_t *ev) {
@@ -693,6 +743,7 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   nl++;
   if (ev) cudaEventRecord(ev[1], s);
   TcArgs a{};
+  a.xmap = t.xmap[R / 64];
   a.adata = static_cast<const unsigned char *>(t.adata);
   a.colmap = t.colmap;
   a.xts = xts;
