@@ -17,9 +17,11 @@
 //               the stage count) of a ring of 64-column chunks: two bulk
 //               copies of the chunk that complete on the stage's mbarrier (hi
 //               rows to tile rows 0..63, lo rows to tile rows 64..127), and
-//               16-byte cp.async gathers of the XTS rows of its columns (whole
-//               rows) into an N-major (MN-major) BF16 tile, then a wait, a
-//               proxy fence and an mbarrier arrive;
+//               the XTS rows of its columns (whole rows) as an N-major
+//               (MN-major) BF16 tile: for a V piece, whose columns are
+//               consecutive rows, one TMA tile load on the same barrier; for a
+//               row tile, 16-byte cp.async gathers, then a wait, a proxy fence
+//               and an mbarrier arrive;
 //   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
 //               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 2R (hi and lo
 //               stacked along both M and N; items have at most 64 rows), into
