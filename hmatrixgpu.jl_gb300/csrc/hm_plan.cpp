@@ -101,27 +101,26 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   std::vector<int32_t> gorder;  // low-rank blocks, grouped
   std::vector<int32_t> gstart;  // group boundaries in gorder
   {
-    std::vector<int32_t> idx(na);
-    std::iota(idx.begin(), idx.end(), 0);
-    std::vector<int32_t> first(na);
-    {
-      std::vector<std::pair<int64_t, int32_t>> key(na);
-      for (size_t b = 0; b < na; b++)
-        key[b] = {(static_cast<int64_t>(bs.a_cs[b]) << 32) | static_cast<uint32_t>(bs.a_ce[b]),
-                  static_cast<int32_t>(b)};
-      std::vector<std::pair<int64_t, int32_t>> sorted = key;
-      std::sort(sorted.begin(), sorted.end());
-      for (size_t i = 0; i < na;) {  // first appearance of each key
-        size_t j = i;
-        while (j < na && sorted[j].first == sorted[i].first) j++;
-        for (size_t q = i; q < j; q++) first[sorted[q].second] = sorted[i].second;
-        i = j;
-      }
-    }
-    std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return first[a] < first[b]; });
-    gorder = idx;
+    // (source range, block) pairs sorted: each range's blocks form a run in
+    // increasing block order, and the run's first block is the range's first
+    // appearance; the runs are then ordered by that first block
+    std::vector<std::pair<int64_t, int32_t>> sorted(na);
+    for (size_t b = 0; b < na; b++)
+      sorted[b] = {(static_cast<int64_t>(bs.a_cs[b]) << 32) | static_cast<uint32_t>(bs.a_ce[b]),
+                   static_cast<int32_t>(b)};
+    std::sort(sorted.begin(), sorted.end());
+    std::vector<std::pair<int32_t, int32_t>> runs;  // (first block, start in sorted)
     for (size_t i = 0; i < na; i++)
-      if (i == 0 || first[gorder[i]] != first[gorder[i - 1]]) gstart.push_back(static_cast<int32_t>(i));
+      if (i == 0 || sorted[i].first != sorted[i - 1].first)
+        runs.push_back({sorted[i].second, static_cast<int32_t>(i)});
+    std::sort(runs.begin(), runs.end());
+    gorder.reserve(na);
+    gstart.reserve(runs.size() + 1);
+    for (const auto &r : runs) {
+      gstart.push_back(static_cast<int32_t>(gorder.size()));
+      for (size_t i = static_cast<size_t>(r.second); i < na && sorted[i].first == sorted[r.second].first; i++)
+        gorder.push_back(sorted[i].second);
+    }
     gstart.push_back(static_cast<int32_t>(na));
   }
   p.t_off.assign(na, 0);
@@ -134,20 +133,15 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   p.xt_len = round_up(p.x_len + R, vec);
 
   // ---- row tiles --------------------------------------------------------------
-  std::vector<int32_t> cuts;
-  cuts.reserve(2 * (nd + na) + 2);
-  cuts.push_back(0);
-  cuts.push_back(static_cast<int32_t>(m));
-  for (size_t b = 0; b < nd; b++) {
-    cuts.push_back(bs.d_rs[b]);
-    cuts.push_back(bs.d_re[b]);
+  std::vector<int32_t> cuts;  // every block row boundary, ascending, once
+  {
+    std::vector<uint8_t> is_cut(static_cast<size_t>(m) + 1, 0);
+    is_cut[0] = is_cut[m] = 1;
+    for (size_t b = 0; b < nd; b++) is_cut[bs.d_rs[b]] = is_cut[bs.d_re[b]] = 1;
+    for (size_t b = 0; b < na; b++) is_cut[bs.a_rs[b]] = is_cut[bs.a_re[b]] = 1;
+    for (int64_t i = 0; i <= m; i++)
+      if (is_cut[i]) cuts.push_back(static_cast<int32_t>(i));
   }
-  for (size_t b = 0; b < na; b++) {
-    cuts.push_back(bs.a_rs[b]);
-    cuts.push_back(bs.a_re[b]);
-  }
-  std::sort(cuts.begin(), cuts.end());
-  cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
   std::vector<int32_t> trow0, trows;
   for (size_t i = 0; i + 1 < cuts.size(); i++) {
     int32_t a = cuts[i], len = cuts[i + 1] - cuts[i];
@@ -160,8 +154,10 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
     }
   }
   const size_t nt = trow0.size();
-  auto tile_of = [&](int32_t row) {  // tile whose row0 == row (row is a cut)
-    return static_cast<size_t>(std::lower_bound(trow0.begin(), trow0.end(), row) - trow0.begin());
+  std::vector<int32_t> tile_at(static_cast<size_t>(m) + 1, static_cast<int32_t>(nt));
+  for (size_t t = 0; t < nt; t++) tile_at[trow0[t]] = static_cast<int32_t>(t);
+  auto tile_of = [&](int32_t row) {  // tile whose row0 == row (row is a cut; m: past the last tile)
+    return static_cast<size_t>(tile_at[row]);
   };
 
   // ---- contributions per tile (CSR): dense blocks first, then low-rank -------
@@ -187,6 +183,7 @@ void make_plan(const BlockSet &bs, int vec, int nwarps, const std::vector<int64_
   // ---- panels, segments, pack jobs ---------------------------------------------
   p.tiles.resize(nt);
   p.pjobs.reserve(contrib.size());
+  p.segs.reserve(contrib.size());
   int64_t off = 0;
   for (size_t t = 0; t < nt; t++) {
     TileDesc &d = p.tiles[t];
@@ -338,12 +335,21 @@ void make_tc_plan(const Plan &p, TcPlan &tp) {
     tp.v_items.push_back(t);
     tp.v_src.push_back(it.v_off);
   }
+  int64_t ncm = 0, ndu = 0;
+  for (const TileDesc &d : p.tiles) {
+    ncm += d.ncols;
+    ndu += (std::max(d.m, 1) + kTcRows - 1) / kTcRows;
+  }
+  tp.colmap.resize(static_cast<size_t>(ncm));
+  tp.du_items.reserve(static_cast<size_t>(ndu));
+  tp.du_src.reserve(static_cast<size_t>(ndu));
+  int32_t *cm = tp.colmap.data();
   for (size_t ti = 0; ti < p.tiles.size(); ti++) {
     const TileDesc &d = p.tiles[ti];
-    const int32_t map = static_cast<int32_t>(tp.colmap.size());
+    const int32_t map = static_cast<int32_t>(cm - tp.colmap.data());
     for (int32_t q = 0; q < d.nseg; q++) {
       const Seg &sg = p.segs[d.seg0 + q];
-      for (int32_t j = 0; j < sg.ncols; j++) tp.colmap.push_back(sg.vec_off + j);
+      for (int32_t j = 0; j < sg.ncols; j++) *cm++ = sg.vec_off + j;
     }
     for (int32_t r0 = 0; r0 < std::max(d.m, 1); r0 += kTcRows) {
       TcItem t{};
