@@ -13,7 +13,7 @@ product y = H x with x ~ N(0,1) (FP32 storage and arithmetic, 1 right-hand side)
 `e2e` is the same through the public API on pinned host buffers (x copied in,
 y copied out every step).  The reference arm (--impl reference) times the
 reference's CPU product (src/mult.jl:6-32) restated by the oracle, on all host
-cores, over a bounded sample of the same matrix's blocks.
+cores, over the same whole matrix assembled by the oracle.
 """
 import argparse
 import json
@@ -33,7 +33,6 @@ import numpy as np  # noqa: E402
 METRIC = "H-matvec/s at N=2^20, 1 & 32 RHS: mixed vs plain FP32 at equal err; HBM GB/s"
 WORKLOAD = "film-2^20 Laplace leaf64 eta2 tol1e-4, 1 RHS, FP32 storage"
 GRID, LEAF, ETA, TOL = 1024, 64, 2.0, 1e-4
-SAMPLE_STRIDE = 64  # the CPU legs time every 64th dense and admissible block
 # DRAM traffic / algorithmic bytes of the near/U kernel, from an ncu capture on
 # film 512 x 512 (1981.2 MB of dram__bytes_read + write for 1952.3 MB algorithmic)
 TRAFFIC_RATIO = 1981.2 / 1952.3
@@ -174,37 +173,47 @@ def batch_measurement(dev, steps):
             "build_seconds": build}
 
 
-def cpu_sample(threads, target_s=15.0, more_threads=()):
-    """Times the oracle's restatement of the reference CPU mul! (src/mult.jl:6-32)
-    on every SAMPLE_STRIDE-th block of the workload's matrix; returns products/s
-    extrapolated to the whole matrix and a description. `more_threads`: further
-    thread counts timed on the same sample (listed under "more" in the description)."""
+def cpu_product(runs):
+    """The reference's CPU product (src/mult.jl:6-32) on the workload's whole
+    H-matrix. The oracle assembles the matrix (FP64, ACA+ and recompression on
+    all host cores; about 24 GB for the headline film); then, for each
+    (threads, warm-up, steps) in `runs`, whole products y = H x run back to
+    back, each with its own permutation of x, block gemvs and scatter
+    (oracle/cpu_mul.c). Returns ({threads: figures}, description)."""
     from oracle import oracle as O
     P = film_points()
+    t0 = time.time()
     T = O.Tree(P.T, LEAF)
     K = O.Kernel("laplace", P.T, P.T)
-    t0 = time.time()
-    H = O.HMatrix(K, T, T, eta=ETA, eps=TOL, sample_stride=SAMPLE_STRIDE,
-                  nthreads=os.cpu_count() or 1)
+    cores = os.cpu_count() or 1
+    H = O.HMatrix(K, T, T, eta=ETA, eps=TOL, nthreads=cores)
     build_s = time.time() - t0
     x = np.random.default_rng(0).standard_normal(H.n)
+    entries = H.stored_entries()
+    y_check = H.mul(x)  # the checker's sequential product on the same matrix
+    out = {}
+    for th, warm, steps in runs:
+        cp = H.timed_product(th)
+        if warm:
+            cp.run(x, warm)
+        dt, y = cp.run(x, steps)
+        out[th] = {"value": steps / dt, "unit": "matvec/s", "cores": th, "steps": steps, "warmup": warm,
+                   "seconds": dt, "ms_per_step": 1e3 * dt / steps, "gbs": 8.0 * entries * steps / dt / 1e9,
+                   "rel_diff_vs_checker": float(np.linalg.norm(y - y_check) / np.linalg.norm(y_check))}
+        del cp
+    desc = (f"the whole matrix ({H.nD} dense + {H.nA} low-rank blocks, {entries:.3e} FP64 entries, "
+            f"{8 * entries / 1e9:.1f} GB), assembled by the oracle on {cores} cores in {build_s:.0f} s; "
+            f"every step one whole product (x permuted, one gemv per dense block, two per low-rank block, "
+            f"y scattered)")
+    del H
+    return out, desc
 
-    def timed(th):
-        dt1 = H.mul_timed(x, th, 1)
-        reps = max(1, int(target_s / max(dt1, 1e-6)))
-        return H.mul_timed(x, th, reps) / reps, reps
 
-    dt, reps = timed(threads)
-    per_product = dt * SAMPLE_STRIDE
-    more = []
-    for th in more_threads:
-        d2, _ = timed(th)
-        more.append({"value": 1.0 / (d2 * SAMPLE_STRIDE), "unit": "matvec/s", "cores": th})
-    return 1.0 / per_product, {
-        "sample": f"every {SAMPLE_STRIDE}th dense and admissible block of the same partition "
-                  f"({H.nD} dense + {H.nA} low-rank blocks, FP64), {reps} timed repetitions, "
-                  f"time x {SAMPLE_STRIDE}; sample assembled by the oracle in {build_s:.0f}s",
-        "cores": threads, "seconds": dt * reps, "more": more}
+def bench_config(n):
+    """The workload as both arms name it."""
+    return {"workload": WORKLOAD, "N": n, "leaf": LEAF, "eta": ETA, "tol": TOL, "nrhs": 1,
+            "l2": "inputs larger than L2: the factors streamed per step are many times the 129 MB L2",
+            "parallelism": "1 GPU"}
 
 
 def cube_measurement(dev, steps, hbm):
@@ -398,19 +407,29 @@ def learned_measurement(dev):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU product (src/mult.jl:6-32),
+    restated by the oracle (Julia is absent here and on the GPU host), on the
+    whole headline matrix with every host core; `warmup` and `steps` whole
+    products. One more short run on one core is reported beside it."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    v, d = cpu_sample(threads)
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
+    runs = [(threads, args.warmup, args.steps)]
+    if threads > 1:
+        runs.append((1, 1, 2))
+    res, desc = cpu_product(runs)
+    r = res[threads]
+    line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "matvec/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded film points)",
-            "config": {"workload": WORKLOAD, "N": GRID * GRID, "leaf": LEAF, "eta": ETA, "tol": TOL},
-            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": threads, "kind": "port",
-                             "sample": d["sample"]},
-            "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "data": "synthetic (seeded film points, x ~ N(0,1))",
+            "config": bench_config(GRID * GRID),
+            "cpu_baseline": {"value": r["value"], "unit": "matvec/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "host_gbs": r["gbs"], "rel_diff_vs_checker": r["rel_diff_vs_checker"],
+            "one_core": res.get(1),
+            "e2e": {"value": r["value"], "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -570,17 +589,17 @@ def run_gpu(args):
     batch32 = None if args.skip_batch else batch_measurement(dev, args.steps)
     cube18 = None if args.skip_cube else cube_measurement(dev, args.steps, hbm)
     learned = learned_measurement(dev) if args.learned else None
-    cpu_v, cpu_d = cpu_sample(1, target_s=10.0, more_threads=(os.cpu_count() or 1,))
+    cores = os.cpu_count() or 1
+    cpu_runs, cpu_desc = cpu_product([(1, 1, 4)] + ([(cores, 3, 10)] if cores > 1 else []))
     value = job_rate(world, ms * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded film points, x ~ N(0,1))",
-        "config": {"workload": WORKLOAD, "N": n, "leaf": LEAF, "eta": ETA, "tol": TOL,
-                   "precision": "f32", "nrhs": 1, "autotuned": tune,
-                   "l2": f"inputs larger than L2: {inf['matrix_bytes'] / 1e9:.1f} GB of factors streamed per step",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "config": dict(bench_config(n), parallelism=f"replicas x{world}" if world > 1 else "1 GPU"),
+        "precision": "f32", "autotuned": tune,
+        "streamed_gb_per_step": inf["matrix_bytes"] / 1e9,
         "hbm_gbs": alg_bytes / (ms * 1e-3) / 1e9,
         "rel_err_vs_fp64_hmatrix": rel_err,
         "structure": {"dense_blocks": inf["full_leaves"], "lowrank_blocks": inf["admissible_leaves"],
@@ -596,8 +615,9 @@ def run_gpu(args):
                      "traffic_source": "ncu dram__bytes_read+write of du_rows_kernel on film 512x512 "
                                        "(1981.2 MB for 1952.3 MB algorithmic), scaled by algorithmic bytes "
                                        "(profiles/du_rows_v_pass_film512.md)"},
-        "cpu_baseline": {"value": cpu_v, "unit": "matvec/s", "cores": 1, "kind": "port",
-                         "sample": cpu_d["sample"], "all_cores": cpu_d["more"][0]},
+        "cpu_baseline": {"value": cpu_runs[1]["value"], "unit": "matvec/s", "cores": 1, "kind": "port",
+                         "sample": cpu_desc + f"; {cpu_runs[1]['steps']} timed products on one core",
+                         "one_core": cpu_runs[1], "all_cores": cpu_runs.get(cores)},
         "e2e": {"value": job_rate(world, e2e_s), "unit": "matvec/s", "h2d_bytes_per_step": n * es,
                 "d2h_bytes_per_step": n * es},
         "gpu_launches": int(nl.value),

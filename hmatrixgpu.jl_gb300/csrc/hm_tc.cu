@@ -18,10 +18,12 @@
 //               copies of the chunk that complete on the stage's mbarrier (hi
 //               rows to tile rows 0..63, lo rows to tile rows 64..127), and
 //               the XTS rows of its columns (whole rows) as an N-major
-//               (MN-major) BF16 tile: for a V piece, whose columns are
-//               consecutive rows, one TMA tile load on the same barrier; for a
-//               row tile, 16-byte cp.async gathers, then a wait, a proxy fence
-//               and an mbarrier arrive;
+//               (MN-major) BF16 tile: for a whole 64-column chunk of a V
+//               piece, whose columns are consecutive rows, one TMA tile load
+//               on the same barrier; for a row tile or a V piece's last,
+//               partial chunk, 16-byte cp.async gathers (padding columns read
+//               the zero row), then a wait, a proxy fence and an mbarrier
+//               arrive;
 //   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
 //               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 2R (hi and lo
 //               stacked along both M and N; items have at most 64 rows), into
@@ -393,6 +395,11 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         if (g % kStages != bw) continue;
         const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
+        // B by one tile load only where all 64 columns of the chunk are the
+        // item's own: the padding columns of a last, partial chunk must read
+        // the zero row (0 * Inf or 0 * NaN from a neighbour's row would reach
+        // this item's sums)
+        const bool tma_b = I.kind != 0 && c0 + kKc <= I.ncols;
         int rows[kKc / 32];  // XTS rows of columns c0 + lane + 32 h
 #pragma unroll
         for (int h = 0; h < kKc / 32; h++) {
@@ -415,7 +422,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
           const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
           const uint32_t bar = su32(&S.full[s]);
-          const uint32_t btx = I.kind != 0 ? static_cast<uint32_t>(Sh::kBBytes) : 0u;
+          const uint32_t btx = tma_b ? static_cast<uint32_t>(Sh::kBBytes) : 0u;
           asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2 * half + btx)
                        : "memory");
           asm volatile(
@@ -426,11 +433,10 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
               "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(lo),
               "l"(src + half), "r"(half), "r"(bar), "l"(pol)
               : "memory");
-          if (I.kind != 0) {
+          if (tma_b) {
             // B of a V piece: its columns are the consecutive XTS rows map + c0
-            // .., so one tile load of 64 rows (rows past the end read as zero)
-            // lands them in the canonical MN-major layout (K groups 128 B
-            // apart, N groups 1024 B apart)
+            // .., so one tile load of 64 rows lands them in the canonical
+            // MN-major layout (K groups 128 B apart, N groups 1024 B apart)
             asm volatile(
                 "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
                 "%4}], [%5];" ::"r"(su32(S.b[s])),
@@ -440,7 +446,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           }
         }
         last_g = g;
-        if (I.kind != 0) {  // the copies complete on the stage's barrier
+        if (tma_b) {  // the copies complete on the stage's barrier
           __syncwarp();
           continue;
         }
@@ -506,9 +512,10 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           for (int h = 0; h < two; h++) {
             const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
             // leading byte offset: K direction; stride byte offset: N direction.
-            // V pieces' B tiles come from the tile load (K groups 128 B apart,
-            // N groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B).
-            const bool tma_b = I.kind != 0;
+            // Whole chunks of V pieces come from the tile load (K groups 128 B
+            // apart, N groups 1024 B), the rest from the gather (kBGroupK,
+            // 128 B); the producer decides by the same test.
+            const bool tma_b = I.kind != 0 && c0 + h * kKc + kKc <= I.ncols;
             const uint64_t db = tma_b ? sdesc(su32(S.b[s2[h]]), 128, 1024)
                                       : sdesc(su32(S.b[s2[h]]), Sh::kBGroupK, kBGroupN);
             for (int ks = 0; ks < kc2[h] / 16; ks++) {

@@ -188,10 +188,11 @@ int hmgpu_matvec_host(hmgpu_hmatrix *H, const void *x, void *y, int64_t nrhs, in
  * cannot allocate device memory while they run it -- code being captured into
  * a CUDA graph where plain allocation is not allowed, loops that fix their
  * memory up front, hosts whose allocator belongs to another framework. Its
- * scratch (permuted x, t = V x, partial sums, counters) lives in one
- * statically sized device array of HMGPU_NOALLOC_SCRATCH_BYTES that every GPU
- * loading this library holds until the process exits; the call allocates
- * nothing. An H-matrix needing more scratch is rejected with HMGPU_ERR_INVALID.
+ * scratch -- the ticket counter of the near/U pass and XT (the permuted x,
+ * then t = V x) -- lives in one statically sized device array of
+ * HMGPU_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until
+ * the process exits; the call allocates nothing. The status word of the
+ * bounded waits stays in H's own allocation. An H-matrix needing more scratch is rejected with HMGPU_ERR_INVALID.
  * The first call on a device looks up the array's address (make that first
  * call before any stream capture). All calls share the array: calls that
  * overlap on the GPU (other streams, other threads, other H-matrices) race. */

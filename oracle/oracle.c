@@ -7,6 +7,7 @@
  */
 #define _GNU_SOURCE
 #include "oracle.h"
+#include "or_internal.h"
 
 #include <math.h>
 #include <pthread.h>
@@ -49,6 +50,47 @@ static double jl_norm3(double a, double b, double c) {
 }
 
 static int64_t imin(int64_t a, int64_t b) { return a < b ? a : b; }
+
+/* Summation order of the sums inside ACA+ and the recompression.
+ *
+ * Julia reaches these sums through LAPACK (qr, svd: src/aca.jl:125-129) and
+ * through `sum` (src/aca.jl:95-96), whose orders are blocked or SIMD-split and
+ * are not pinned by any reference test. The oracle fixes one order instead,
+ * the one a team of lanes gives when it sums a strided vector: a team of
+ * `nt` lanes (32, or 256 for blocks with m + n >= 4096), lane t adding the
+ * terms t, t + nt, t + 2 nt, ... in that order from 0.0; each group of 32
+ * lanes folded by a butterfly (partners at distance 16, 8, 4, 2, 1); the
+ * groups' sums then added in group order. Every term and every product
+ * inside a term is the reference's. */
+#define OR_TEAM_MIN_MN 4096
+static int team_size(int64_t m, int64_t n) { return m + n >= OR_TEAM_MIN_MN ? 256 : 32; }
+
+/* Folds the lane sums p[0..nt) in the order above. */
+static double team_fold(const double *p, int nt) {
+  double s = 0.0;
+  for (int g = 0; g < nt / 32; g++) {
+    double v[32], nv[32];
+    memcpy(v, p + 32 * g, sizeof v);
+    for (int o = 16; o > 0; o >>= 1) {
+      for (int l = 0; l < 32; l++) nv[l] = v[l] + v[l ^ o];
+      memcpy(v, nv, sizeof v);
+    }
+    s = g == 0 ? v[0] : s + v[0];
+  }
+  return s;
+}
+
+/* sum_{i0 <= i < len} a[i*sa] * b[i*sb], term i on lane (i - i0) mod nt. */
+static double team_dot(const double *a, int64_t sa, const double *b, int64_t sb, int64_t i0,
+                       int64_t len, int nt) {
+  double p[256];
+  for (int t = 0; t < nt; t++) p[t] = 0.0;
+  for (int64_t base = i0; base < len; base += nt) {
+    const int64_t cnt = len - base < nt ? len - base : nt;
+    for (int64_t t = 0; t < cnt; t++) p[t] += a[(base + t) * sa] * b[(base + t) * sb];
+  }
+  return team_fold(p, nt);
+}
 
 /* ------------------------------------------------------------------------ */
 /* cluster tree: src/tree.jl:45-137                                           */
@@ -434,15 +476,23 @@ static int64_t argmax_not_in(const double *a, int64_t n, const char *used) {
   return best;
 }
 
-int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_t *cols,
-                int64_t n, double eps, int64_t max_iter, int64_t cap, double *U, double *V,
-                int64_t *rank) {
+/* ACA+ core. U (m x k, column-major, ld m) and V (k x n, row-major) are
+ * allocated here and doubled as terms are added, so a block of rank k holds
+ * O(k (m + n)) memory whatever its size. */
+static int aca_core(const or_kernel *K, const int64_t *rows, int64_t m, const int64_t *cols,
+                    int64_t n, double eps, int64_t max_iter, double **Up, double **Vp,
+                    int64_t *rank) {
   if (max_iter <= 0) max_iter = m; /* default max_iter = n_rows (:36) */
   max_iter = imin(imin(m, n), max_iter);
-  if (cap < max_iter) return -1;
+  const int nt = team_size(m, n);
+  int64_t cap = imin(max_iter, 16);
+  if (cap < 1) cap = 1;
+  double *U = (double *)malloc((size_t)(m * cap) * sizeof(double));
+  double *V = (double *)malloc((size_t)(cap * n) * sizeof(double));
   double *rrow = (double *)calloc((size_t)n, sizeof(double));
   double *rcol = (double *)calloc((size_t)m, sizeof(double));
   char *used_r = (char *)calloc((size_t)m, 1), *used_c = (char *)calloc((size_t)n, 1);
+  if (!U || !V || !rrow || !rcol || !used_r || !used_c) return -2;
   int64_t k = 0;
   for (int64_t it = 1; it <= max_iter; it++) {
     int64_t rp, cp;
@@ -460,15 +510,17 @@ int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_
     for (int64_t j = 0; j < n; j++) rrow[j] = or_kernel_entry(K, rows[I], cols[j]); \
     for (int64_t q = 0; q < k; q++) {                                         \
       double s = U[(I) + q * m];                                              \
-      for (int64_t j = 0; j < n; j++) rrow[j] -= s * V[q + j * cap];          \
+      const double *vq = V + q * n;                                           \
+      for (int64_t j = 0; j < n; j++) rrow[j] -= s * vq[j];                   \
     }                                                                         \
   } while (0)
 #define RES_COL(J)                                                            \
   do {                                                                        \
     for (int64_t i = 0; i < m; i++) rcol[i] = or_kernel_entry(K, rows[i], cols[J]); \
     for (int64_t q = 0; q < k; q++) {                                         \
-      double s = V[q + (J) * cap];                                            \
-      for (int64_t i = 0; i < m; i++) rcol[i] -= U[i + q * m] * s;            \
+      double s = V[q * n + (J)];                                              \
+      const double *uq = U + q * m;                                           \
+      for (int64_t i = 0; i < m; i++) rcol[i] -= uq[i] * s;                   \
     }                                                                         \
   } while (0)
     if (rval > cval) { /* :79-82 */
@@ -484,16 +536,19 @@ int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_
 #undef RES_COL
     used_r[rp] = 1;
     used_c[cp] = 1;
+    if (k == cap) { /* room for more terms */
+      cap = imin(2 * cap, max_iter);
+      U = (double *)realloc(U, (size_t)(m * cap) * sizeof(double));
+      V = (double *)realloc(V, (size_t)(cap * n) * sizeof(double));
+      if (!U || !V) return -2;
+    }
     double piv = rrow[cp];
-    double su = 0.0, sv = 0.0;
-    for (int64_t j = 0; j < n; j++) {
-      V[k + j * cap] = rrow[j] / piv; /* :92 */
-      sv += V[k + j * cap] * V[k + j * cap];
-    }
-    for (int64_t i = 0; i < m; i++) {
-      U[i + k * m] = rcol[i]; /* :93 */
-      su += rcol[i] * rcol[i];
-    }
+    double *vk = V + k * n, *uk = U + k * m;
+    for (int64_t j = 0; j < n; j++) vk[j] = rrow[j] / piv; /* :92 */
+    for (int64_t i = 0; i < m; i++) uk[i] = rcol[i];       /* :93 */
+    /* sum(v.^2), sum(u.^2) in the team order (top of this file) */
+    double sv = team_dot(vk, 1, vk, 1, 0, n, nt);
+    double su = team_dot(uk, 1, uk, 1, 0, m, nt);
     k++;
     if (sqrt(su * sv) < eps) break; /* :95-99 */
   }
@@ -501,6 +556,26 @@ int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_
   free(rcol);
   free(used_r);
   free(used_c);
+  *Up = U;
+  *Vp = V;
+  *rank = k;
+  return 0;
+}
+
+int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_t *cols,
+                int64_t n, double eps, int64_t max_iter, int64_t cap, double *U, double *V,
+                int64_t *rank) {
+  int64_t mi = max_iter <= 0 ? m : max_iter;
+  if (cap < imin(imin(m, n), mi)) return -1;
+  double *Uc, *Vr;
+  int64_t k;
+  int rc = aca_core(K, rows, m, cols, n, eps, max_iter, &Uc, &Vr, &k);
+  if (rc) return rc;
+  memcpy(U, Uc, (size_t)(m * k) * sizeof(double));
+  for (int64_t q = 0; q < k; q++)
+    for (int64_t j = 0; j < n; j++) V[q + j * cap] = Vr[q * n + j];
+  free(Uc);
+  free(Vr);
   *rank = k;
   return 0;
 }
@@ -510,14 +585,22 @@ int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_
 /* ------------------------------------------------------------------------ */
 
 /* Unblocked Householder QR of A (m x k, col-major, m >= k), LAPACK dgeqr2
- * conventions: reflectors below the diagonal, tau[j], R (k x k, col-major). */
-int or_qr(int64_t m, int64_t k, double *A, double *tau, double *R) {
+ * conventions: reflectors below the diagonal, tau[j], R (k x k, col-major).
+ * The column norms and the reflections' dot products are sums in the team
+ * order of `nt` lanes (top of this file). */
+static void reflect(const double *x, int64_t len, double tau, double *y, int nt) {
+  /* y := (I - tau v v') y with v = [1; x[1..len)] */
+  double w = (team_dot(x, 1, y, 1, 1, len, nt) + y[0]) * tau;
+  y[0] -= w;
+  for (int64_t i = 1; i < len; i++) y[i] -= w * x[i];
+}
+
+int or_qr(int64_t m, int64_t k, double *A, double *tau, double *R, int nt) {
+  if (nt != 32 && nt != 256) return -1;
   for (int64_t j = 0; j < k; j++) {
     double *x = A + j + j * m;
     int64_t len = m - j;
-    double xn = 0.0;
-    for (int64_t i = 1; i < len; i++) xn += x[i] * x[i];
-    xn = sqrt(xn);
+    double xn = sqrt(team_dot(x, 1, x, 1, 1, len, nt));
     double alpha = x[0];
     if (xn == 0.0) {
       tau[j] = 0.0;
@@ -529,14 +612,7 @@ int or_qr(int64_t m, int64_t k, double *A, double *tau, double *R) {
       x[0] = beta;
     }
     /* apply H_j = I - tau v v^T to the trailing columns */
-    for (int64_t c = j + 1; c < k; c++) {
-      double *y = A + j + c * m;
-      double w = y[0];
-      for (int64_t i = 1; i < len; i++) w += x[i] * y[i];
-      w *= tau[j];
-      y[0] -= w;
-      for (int64_t i = 1; i < len; i++) y[i] -= w * x[i];
-    }
+    for (int64_t c = j + 1; c < k; c++) reflect(x, len, tau[j], A + j + c * m, nt);
   }
   if (R) {
     for (int64_t c = 0; c < k; c++)
@@ -548,20 +624,11 @@ int or_qr(int64_t m, int64_t k, double *A, double *tau, double *R) {
 /* B (m x p, col-major) := Q_thin * [C; 0] where C is k x p and Q's reflectors
  * are in QR (m x k) and tau. */
 static void qr_apply_thin(int64_t m, int64_t k, const double *QR, const double *tau,
-                          const double *C, int64_t p, double *B) {
+                          const double *C, int64_t p, double *B, int nt) {
   for (int64_t c = 0; c < p; c++) {
     double *y = B + c * m;
     for (int64_t i = 0; i < m; i++) y[i] = i < k ? C[i + c * k] : 0.0;
-    for (int64_t j = k - 1; j >= 0; j--) {
-      const double *x = QR + j + j * m;
-      int64_t len = m - j;
-      double *yy = y + j;
-      double w = yy[0];
-      for (int64_t i = 1; i < len; i++) w += x[i] * yy[i];
-      w *= tau[j];
-      yy[0] -= w;
-      for (int64_t i = 1; i < len; i++) yy[i] -= w * x[i];
-    }
+    for (int64_t j = k - 1; j >= 0; j--) reflect(QR + j + j * m, m - j, tau[j], y + j, nt);
   }
 }
 
@@ -641,8 +708,9 @@ int or_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const do
   memcpy(QU, U, (size_t)(m * k) * sizeof(double));
   for (int64_t j = 0; j < n; j++) /* V' (n x k) */
     for (int64_t q = 0; q < k; q++) QV[j + q * n] = V[q + j * k];
-  or_qr(m, k, QU, tu, RU); /* :125 */
-  or_qr(n, k, QV, tv, RV); /* :126 */
+  const int nt = team_size(m, n);
+  or_qr(m, k, QU, tu, RU, nt); /* :125 */
+  or_qr(n, k, QV, tv, RV, nt); /* :126 */
   for (int64_t c = 0; c < k; c++) /* RU * RV' (:129) */
     for (int64_t r = 0; r < k; r++) {
       double s = 0.0;
@@ -669,11 +737,11 @@ int or_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const do
   double *C = (double *)malloc((size_t)(k * (r ? r : 1)) * sizeof(double));
   for (int64_t c = 0; c < r; c++)
     for (int64_t i = 0; i < k; i++) C[i + c * k] = M[i + ord[c] * k];
-  qr_apply_thin(m, k, QU, tu, C, r, U_out);
+  qr_apply_thin(m, k, QU, tu, C, r, U_out, nt);
   for (int64_t c = 0; c < r; c++)
     for (int64_t i = 0; i < k; i++) C[i + c * k] = Z[i + ord[c] * k];
   double *B = (double *)malloc((size_t)(n * (r ? r : 1)) * sizeof(double));
-  qr_apply_thin(n, k, QV, tv, C, r, B);
+  qr_apply_thin(n, k, QV, tv, C, r, B, nt);
   for (int64_t c = 0; c < r; c++)
     for (int64_t j = 0; j < n; j++) V_out[c + j * r] = B[j + c * n];
   free(B);
@@ -696,26 +764,6 @@ int or_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const do
 /* assembly: src/hmatrix.jl:72-217                                            */
 /* ------------------------------------------------------------------------ */
 
-typedef struct {
-  int64_t rs, re, cs, ce; /* 1-based inclusive, permuted index space */
-  int64_t r;              /* rank (approx blocks)                    */
-  double *D;              /* dense: m x n row-major                   */
-  double *U;              /* approx: m x r row-major                  */
-  double *V;              /* approx: r x n row-major                  */
-} or_block;
-
-struct or_hmatrix {
-  int64_t m, n;
-  int64_t *tmap, *smap;
-  int64_t tlen, slen;
-  or_block *dense;
-  int64_t nd;
-  or_block *approx;
-  int64_t na;
-  int64_t ncand;       /* admissible leaves that were processed      */
-  int64_t *aca_rank;   /* per candidate: rank before recompression   */
-  int64_t *final_rank; /* per candidate: rank kept, -1 if went dense */
-};
 
 typedef struct {
   const or_kernel *K;
@@ -743,19 +791,17 @@ static void approx_one(build_ctx *c, int64_t p) {
   const or_node *a = &c->X->nodes[c->pairs[2 * p]], *b = &c->Y->nodes[c->pairs[2 * p + 1]];
   int64_t m = a->end - a->start, n = b->end - b->start;
   const int64_t *tid = c->tmap + (a->start - 1), *sid = c->smap + (b->start - 1);
-  int64_t cap = imin(m, n);
-  double *U = (double *)malloc((size_t)(m * cap) * sizeof(double));
-  double *V = (double *)malloc((size_t)(cap * n) * sizeof(double));
+  double *U, *Vr;
   int64_t k;
-  or_aca_plus(c->K, tid, m, sid, n, c->eps / 10.0, m, cap, U, V, &k);
+  aca_core(c->K, tid, m, sid, n, c->eps / 10.0, m, &U, &Vr, &k);
   c->aca_rank[p] = k;
-  double *Uo = U, *Vo = V;
+  double *Uo = U, *Vo;
   int64_t r = k;
-  /* compact V to leading dimension k */
+  /* V as k x n column-major (leading dimension k) */
   double *Vc = (double *)malloc((size_t)((k ? k : 1) * n) * sizeof(double));
   for (int64_t j = 0; j < n; j++)
-    for (int64_t q = 0; q < k; q++) Vc[q + j * k] = V[q + j * cap];
-  free(V);
+    for (int64_t q = 0; q < k; q++) Vc[q + j * k] = Vr[q * n + j];
+  free(Vr);
   if (c->svd) {
     double *U2 = (double *)malloc((size_t)(m * (k ? k : 1)) * sizeof(double));
     double *V2 = (double *)malloc((size_t)((k ? k : 1) * n) * sizeof(double));
@@ -770,6 +816,57 @@ static void approx_one(build_ctx *c, int64_t p) {
   c->rank[p] = r;
   c->U[p] = Uo; /* m x r col-major, ld m */
   c->V[p] = Vo; /* r x n col-major, ld r */
+}
+
+/* Runs fn(ctx, i) for i in [0, n) on nthreads threads (items handed out in
+ * order from a shared counter). */
+typedef struct {
+  void (*fn)(void *, int64_t);
+  void *ctx;
+  int64_t n, next;
+  pthread_mutex_t mu;
+} par_ctx;
+
+static void *par_worker(void *arg) {
+  par_ctx *c = (par_ctx *)arg;
+  for (;;) {
+    pthread_mutex_lock(&c->mu);
+    int64_t i = c->next++;
+    pthread_mutex_unlock(&c->mu);
+    if (i >= c->n) break;
+    c->fn(c->ctx, i);
+  }
+  return NULL;
+}
+
+static void par_for(int nthreads, int64_t n, void (*fn)(void *, int64_t), void *ctx) {
+  par_ctx c;
+  c.fn = fn;
+  c.ctx = ctx;
+  c.n = n;
+  c.next = 0;
+  pthread_mutex_init(&c.mu, NULL);
+  if (nthreads <= 1) {
+    par_worker(&c);
+  } else {
+    pthread_t *th = (pthread_t *)malloc((size_t)nthreads * sizeof(pthread_t));
+    for (int t = 0; t < nthreads; t++) pthread_create(&th[t], NULL, par_worker, &c);
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    free(th);
+  }
+  pthread_mutex_destroy(&c.mu);
+}
+
+typedef struct {
+  const or_kernel *K;
+  const or_hmatrix *h;
+} fill_ctx;
+
+static void fill_one(void *arg, int64_t b) {
+  fill_ctx *c = (fill_ctx *)arg;
+  or_block *B = &c->h->dense[b];
+  int64_t m = B->re - B->rs + 1, n = B->ce - B->cs + 1;
+  fill_dense(c->K, c->h->tmap + (B->rs - 1), m, c->h->smap + (B->cs - 1), n, B->D);
 }
 
 static void *build_worker(void *arg) {
@@ -820,8 +917,9 @@ int or_hmatrix_build(const or_kernel *K, const or_tree *X, const or_tree *Y, dou
     B->ce = b->end - 1;
     int64_t m = a->end - a->start, n = b->end - b->start;
     B->D = (double *)malloc((size_t)(m * n) * sizeof(double));
-    fill_dense(K, h->tmap + (a->start - 1), m, h->smap + (b->start - 1), n, B->D);
   }
+  fill_ctx fc = {K, h};
+  par_for(nthreads, h->nd, fill_one, &fc);
   /* admissible blocks (:189-214), computed in parallel, stored in order */
   build_ctx c;
   memset(&c, 0, sizeof c);

@@ -99,8 +99,9 @@ int or_aca_plus(const or_kernel *K, const int64_t *rows, int64_t m, const int64_
  * Writes U_out (m x r, ld m) and V_out (r x n, ld r); r <= k. */
 int or_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const double *V,
                       double eps, double *U_out, double *V_out, int64_t *r);
-/* Householder QR and one-sided Jacobi SVD, exposed for cross-checks. */
-int or_qr(int64_t m, int64_t k, double *A, double *tau, double *R);
+/* Householder QR and one-sided Jacobi SVD, exposed for cross-checks. The QR's
+ * sums run in the order of a team of nt lanes (32 or 256; see oracle.c). */
+int or_qr(int64_t m, int64_t k, double *A, double *tau, double *R, int nt);
 int or_jacobi_svd(int64_t k, double *A, double *Vj, double *sigma, int64_t *order);
 
 /* ---- assembly + flatten: src/hmatrix.jl:72-217 ------------------------- */
@@ -133,6 +134,19 @@ double or_mul_cpu_timed(const or_hmatrix *h, const double *x, double *y, int nth
                         int reps);
 /* Flattened mul! semantics (src/mult.jl:41-146), sequential order; fills Vx. */
 int or_mul_flat(const or_hmatrix *h, const double *x, double *y, double *Vx);
+
+/* ---- the timed CPU baseline (cpu_mul.c) --------------------------------- */
+/* mul!(result, ::HMatrixCPU, x) (src/mult.jl:6-32) with BLAS-like dot products
+ * (vector accumulators, fused multiply-adds): one permutation of x, one gemv
+ * per dense block, two per low-rank block and one scatter per product. A plan
+ * fixes the thread count, the split of the block list and the buffers. */
+typedef struct or_cpu_mul or_cpu_mul;
+or_cpu_mul *or_cpu_mul_plan(const or_hmatrix *h, int nthreads);
+/* Runs `reps` whole products y = H x; returns their wall time in seconds. */
+double or_cpu_mul_run(or_cpu_mul *p, const double *x, double *y, int reps);
+void or_cpu_mul_free(or_cpu_mul *p);
+/* Stored FP64 entries of all blocks (8 bytes each are read per product). */
+int64_t or_hmatrix_stored_entries(const or_hmatrix *h);
 
 #ifdef __cplusplus
 }

@@ -64,7 +64,7 @@ def lib():
                                   C.c_int64, C.c_int64, F64P, F64P, I64P]
         L.or_svd_recompress.argtypes = [C.c_int64, C.c_int64, C.c_int64, F64P, F64P, C.c_double,
                                         F64P, F64P, I64P]
-        L.or_qr.argtypes = [C.c_int64, C.c_int64, F64P, F64P, F64P]
+        L.or_qr.argtypes = [C.c_int64, C.c_int64, F64P, F64P, F64P, C.c_int]
         L.or_jacobi_svd.argtypes = [C.c_int64, F64P, F64P, F64P, I64P]
         L.or_hmatrix_build.argtypes = [C.POINTER(_Kernel), C.c_void_p, C.c_void_p, C.c_double,
                                        C.c_double, C.c_int, C.c_int64, C.c_int, C.POINTER(C.c_void_p)]
@@ -78,6 +78,13 @@ def lib():
         L.or_mul_cpu_timed.argtypes = [C.c_void_p, F64P, F64P, C.c_int, C.c_int]
         L.or_mul_cpu_timed.restype = C.c_double
         L.or_mul_flat.argtypes = [C.c_void_p, F64P, F64P, F64P]
+        L.or_cpu_mul_plan.argtypes = [C.c_void_p, C.c_int]
+        L.or_cpu_mul_plan.restype = C.c_void_p
+        L.or_cpu_mul_run.argtypes = [C.c_void_p, F64P, F64P, C.c_int]
+        L.or_cpu_mul_run.restype = C.c_double
+        L.or_cpu_mul_free.argtypes = [C.c_void_p]
+        L.or_hmatrix_stored_entries.argtypes = [C.c_void_p]
+        L.or_hmatrix_stored_entries.restype = C.c_int64
         _LIB = L
     return _LIB
 
@@ -282,6 +289,14 @@ class HMatrix:
         y = np.empty(self.m)
         return lib().or_mul_cpu_timed(self._h, _p(x), _p(y), nthreads, reps)
 
+    def stored_entries(self):
+        """FP64 entries stored in all blocks (each read once per product)."""
+        return lib().or_hmatrix_stored_entries(self._h)
+
+    def timed_product(self, nthreads=1):
+        """A CpuProduct: the timed CPU baseline on this matrix (cpu_mul.c)."""
+        return CpuProduct(self, nthreads)
+
     def mul_flat(self, x):
         """Flattened mul! semantics (src/mult.jl:41-146); returns (y, Vx)."""
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -303,3 +318,26 @@ class HMatrix:
                 "max_rank": int(ranks.max()) if len(ranks) else 0,
                 "min_dense_size": int(dsz.min()), "max_dense_size": int(dsz.max()),
                 "compression_ratio": self.m * self.n / comp}
+
+
+class CpuProduct:
+    """The reference's CPU mul! (src/mult.jl:6-32) shaped as Julia runs it, with
+    BLAS-like dot products, on `nthreads` threads (cpu_mul.c). Timing only: the
+    checker is HMatrix.mul."""
+
+    def __init__(self, H, nthreads=1):
+        self.H = H
+        self.nthreads = int(nthreads)
+        self._p = lib().or_cpu_mul_plan(H._h, self.nthreads)
+
+    def run(self, x, reps=1):
+        """(seconds for `reps` whole products, y of the last one)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(self.H.m)
+        dt = lib().or_cpu_mul_run(self._p, _p(x), _p(y), int(reps))
+        return dt, y
+
+    def __del__(self):
+        if getattr(self, "_p", None) and _LIB is not None:
+            _LIB.or_cpu_mul_free(self._p)
+            self._p = None

@@ -58,6 +58,35 @@ def test_batch_equals_members(gpu, precision, nrhs):
     assert B.status() == 0
     del hs  # the batch owns copies: it outlives its members
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("nrhs", [32, 64])
+def test_batch_nonfinite_member_stays_contained(gpu, nrhs):
+    """An Inf or a NaN in one member's x reaches only that member's rows of y:
+    the padding columns of every tensor-core tile read zeros, never a
+    neighbouring member's x or t rows (0 * Inf would be NaN). The other
+    members' rows stay finite and bitwise equal to their own products."""
+    import torch
+    hs = _members("mixed")
+    B = hmgpu.batch(hs)
+    n = sum(H.shape[1] for H in hs)
+    g = torch.Generator(device=gpu).manual_seed(7)
+    x = torch.randn(nrhs, n, device=gpu, generator=g).t()
+    bad = 1  # member whose x gets non-finite entries
+    c0 = sum(H.shape[1] for H in hs[:bad])
+    x[c0 + 3, :] = float("inf")
+    x[c0 + hs[bad].shape[1] - 1, :] = float("nan")
+    y = B * x
+    r0 = c0 = 0
+    for k, H in enumerate(hs):
+        mk, nk = H.shape
+        if k != bad:
+            yk = H * x[c0:c0 + nk].t().contiguous().t()
+            assert torch.isfinite(y[r0:r0 + mk]).all(), k
+            assert torch.equal(y[r0:r0 + mk], yk), k
+        r0 += mk
+        c0 += nk
+    assert B.status() == 0
     assert torch.equal(B * x, y)
 
 

@@ -36,7 +36,8 @@ def test_aca_plus_known_answer_and_oracle(gpu):
     Uso, Vso = O.svd_recompress(U, V, eps / 10)
     assert Us.shape == Uso.shape and U.shape[1] >= Us.shape[1]
     assert np.max(np.abs(Us @ (Vs @ x) - blk @ x)) < eps / 100
-    np.testing.assert_allclose(Us @ Vs, Uso @ Vso, rtol=0, atol=1e-13 * np.abs(blk).max())
+    np.testing.assert_array_equal(Us, Uso)  # QR and Jacobi sums in the same order
+    np.testing.assert_array_equal(Vs, Vso)
 
 
 def test_aca_plus_large_block_cta_team(gpu):
@@ -55,7 +56,8 @@ def test_aca_plus_large_block_cta_team(gpu):
     Us, Vs = hmgpu.SVD_recompress(U, V, eps * 10)
     Uso, Vso = O.svd_recompress(U, V, eps * 10)
     assert Us.shape == Uso.shape
-    np.testing.assert_allclose(Us @ Vs, Uso @ Vso, rtol=0, atol=1e-12 * np.abs(blk).max())
+    np.testing.assert_array_equal(Us, Uso)  # CTA-team QR sums in the oracle's team order
+    np.testing.assert_array_equal(Vs, Vso)
 
 
 def test_svd_recompress_random(gpu):
@@ -66,7 +68,8 @@ def test_svd_recompress_random(gpu):
         Us, Vs = hmgpu.SVD_recompress(U, V, eps)
         Uo, Vo = O.svd_recompress(U, V, eps)
         assert Us.shape[1] == Uo.shape[1], (m, n, k, eps)
-        np.testing.assert_allclose(Us @ Vs, Uo @ Vo, rtol=0, atol=1e-12 * np.abs(U @ V).max())
+        np.testing.assert_array_equal(Us, Uo)
+        np.testing.assert_array_equal(Vs, Vo)
 
 
 def _oracle_h(kind, P, leaf, eta, eps, dims=1):
@@ -99,31 +102,52 @@ def test_circle_log_kernel_reference_checks(gpu):
     assert np.max(np.abs(Ho.mul(x) - y)) < 1e-9              # GPU vs CPU H*x, atol 1e-9
 
 
-def test_partition_and_ranks_match_oracle(gpu):
-    P = geometry.cube(4096, seed=0)
-    K, Ho = _oracle_h("laplace", P, 32, 2.0, 1e-6)
-    H = _dev_h("laplace", P, 32, 2.0, 1e-6, keep_factors=True)
+# Kernels whose entries are IEEE-exact (+, -, *, /, sqrt), so that the device
+# and the oracle start from the same bits. The log and Yukawa kernels call
+# log/exp, whose last bit differs between CUDA and the host C library; their
+# matrices agree to rounding (test_circle_log_kernel_reference_checks,
+# test_kernels_against_dense).
+PARITY_CASES = {
+    # name: (kernel, points, leaf, eta, eps, dims)
+    "circle": ("vector_r", lambda: geometry.circle(1000), 64, 1.5, 1e-6, 3),
+    "cube4096": ("laplace", lambda: geometry.cube(4096, seed=0), 32, 2.0, 1e-6, 1),
+    "sphere": ("laplace", lambda: geometry.sphere(6000, seed=2), 32, 1.5, 1e-5, 1),
+    "film128": ("laplace", lambda: geometry.film(128, 128), 64, 2.0, 1e-4, 1),
+}
+
+
+@pytest.mark.parametrize("case", sorted(PARITY_CASES))
+def test_partition_and_ranks_match_oracle(gpu, case):
+    """Same H-matrix as the oracle's: equal partition, every rank equal, every
+    recompressed factor bitwise equal (ACA+ and the QR/SVD recompression run the
+    same operations in the same order, src/aca.jl:36-143, src/hmatrix.jl:189-213),
+    and the FP64 products agree to 1e-12 (src/mult.jl:6-32 on the same matrix).
+    The film case has blocks with m + n >= 4096, which a whole CTA works on."""
+    import torch
+    kind, pts, leaf, eta, eps, dims = PARITY_CASES[case]
+    P = pts()
+    K, Ho = _oracle_h(kind, P, leaf, eta, eps, dims)
+    H = _dev_h(kind, P, leaf, eta, eps, dims, keep_factors=True)
     d, a = H.blocks()
     # dense list: tree dense leaves, then admissible leaves that did not compress
     np.testing.assert_array_equal(d, Ho.dense_block_indices[:, :4])
     np.testing.assert_array_equal(a[:, :2], Ho.U_block_indices[:, :2])
     ranks_o = Ho.U_block_indices[:, 3] - Ho.U_block_indices[:, 2] + 1
-    assert np.mean(a[:, 4] == ranks_o) > 0.99
-    x = np.random.default_rng(1).standard_normal(4096)
-    import torch
+    np.testing.assert_array_equal(a[:, 4], ranks_o)
+    aca_dev = H.aca_ranks(len(Ho.aca_ranks))
+    np.testing.assert_array_equal(aca_dev[0], Ho.aca_ranks)
+    vrow = Ho.V_block_indices
+    for b in range(len(a)):
+        U, V = H.block_factors(b)
+        uo = Ho.U_block_indices[b, 4]
+        vo = vrow[Ho.U_block_indices[b, 2] - 1, 2] if a[b, 4] else 0
+        np.testing.assert_array_equal(U, Ho.U_matrices[uo:uo + U.size].reshape(U.shape), err_msg=f"U of block {b}")
+        np.testing.assert_array_equal(V, Ho.V_matrices[vo:vo + V.size].reshape(V.shape), err_msg=f"V of block {b}")
+    x = np.random.default_rng(1).standard_normal(Ho.n)
     y = (H * torch.tensor(x, device=gpu)).cpu().numpy()
     yo = Ho.mul(x)
-    yd = K.matvec(x)
-    assert rel(y, yd) < 1e-5 and rel(yo, yd) < 1e-5
-    assert rel(y, yo) < 1e-6
-    # factors of one block against the oracle's
-    U, V = H.block_factors(0)
-    r = a[0, 4]
-    uo = Ho.U_block_indices[0, 4]
-    Uo = Ho.U_matrices[uo:uo + U.size].reshape(U.shape)
-    vo = Ho.V_block_indices[Ho.U_block_indices[0, 2] - 1, 2]
-    Vo = Ho.V_matrices[vo:vo + V.size].reshape(V.shape)
-    np.testing.assert_allclose(U @ V, Uo @ Vo, rtol=0, atol=1e-12 * np.abs(Uo @ Vo).max())
+    assert rel(y, yo) <= 1e-12
+    assert rel(yo, K.matvec(x)) < 50 * eps
 
 
 @pytest.mark.parametrize("kind,geom,leaf,eta,eps,dims", [

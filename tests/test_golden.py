@@ -56,7 +56,10 @@ def test_circle_golden_device(gpu, name, kind, dims):
     d, a = H.blocks()
     np.testing.assert_array_equal(d, g["dense_block_indices"][:, :4])
     ranks = g["U_block_indices"][:, 3] - g["U_block_indices"][:, 2] + 1
-    assert np.mean(a[:, 4] == ranks) >= 0.99
+    if kind == "vector_r":  # IEEE-exact entries: the same H-matrix as the oracle's
+        np.testing.assert_array_equal(a[:, 4], ranks)
+    else:  # CUDA's log and the host's differ in the last bit of some entries
+        assert np.mean(a[:, 4] == ranks) >= 0.99
     y = (H * torch.tensor(g["x"], device=gpu)).cpu().numpy()
     assert np.max(np.abs(y - g["y"])) < 1e-9             # test/test_hmatrix.jl:164 (GPU vs CPU)
     assert np.max(np.abs(y - g["y_dense"])) < 1e-5       # test/test_hmatrix.jl:199

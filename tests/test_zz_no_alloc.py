@@ -2,7 +2,8 @@
 memory while it runs (graph capture without allocation, fixed-footprint loops,
 hosts whose allocator belongs to another framework). Its scratch is a static
 device array of HMGPU_NOALLOC_SCRATCH_BYTES shared by every call, so this file
-is collected last and checks two calls in a row against hmgpu_matvec."""
+is collected last and checks two calls in a row against hmgpu_matvec and
+against the oracle's CPU product."""
 import ctypes as C
 
 import numpy as np
@@ -39,6 +40,29 @@ def test_noalloc_matches_matvec_twice(gpu, precision, tol):
         torch.cuda.synchronize()
         err = float(torch.linalg.norm((y - y_ref).double()) / torch.linalg.norm(y_ref.double()))
         assert err <= tol
+
+
+def test_noalloc_matches_oracle_mul(gpu):
+    """The oracle's own H-matrix (imported through the reference's flattened
+    layout) multiplied by hmgpu_matvec_noalloc, twice, against the oracle's CPU
+    mul! (src/mult.jl:6-32) on the same matrix: 1e-12 in FP64."""
+    import torch
+    P = geometry.cube(4096, seed=0)
+    Ho = O.HMatrix(O.Kernel("laplace", P.T, P.T), O.Tree(P.T, 32), O.Tree(P.T, 32), eta=2.0, eps=1e-6,
+                   nthreads=8)
+    H = hmgpu.HMatrix.from_flat(Ho.m, Ho.n, Ho.target_index_map, Ho.source_index_map,
+                                Ho.dense_block_indices, Ho.dense_blocks, Ho.U_block_indices, Ho.U_matrices,
+                                Ho.V_block_indices, Ho.V_matrices, precision="f64")
+    stream = torch.cuda.current_stream(gpu).cuda_stream
+    rng = np.random.default_rng(17)
+    for _ in range(2):
+        x = rng.standard_normal(Ho.n)
+        xd = torch.tensor(x, device=gpu)
+        y = torch.full((Ho.m,), float("nan"), dtype=torch.float64, device=gpu)
+        assert _noalloc(H, xd, y, stream) == 0, _lib.lib().hmgpu_last_error()
+        torch.cuda.synchronize()
+        yo = Ho.mul(x)
+        assert np.linalg.norm(y.cpu().numpy() - yo) / np.linalg.norm(yo) <= 1e-12
 
 
 def test_noalloc_rejects_oversized_matrix(gpu):
