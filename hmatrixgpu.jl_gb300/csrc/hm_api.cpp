@@ -203,8 +203,10 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   return HMGPU_OK;
 }
 
-// Tensor-core copy of a FP32 layout: canonical BF16 (hi, lo) chunks of every
-// multi-RHS V item and every row tile (hm_tc.cu), packed from the FP32 panels.
+// Tensor-core copy of a FP32 layout: canonical FP16 (hi, lo) chunks of every
+// multi-RHS V item and every row tile (hm_tc.cu), packed from the FP32 panels
+// and V rows with power-of-two scales: per rank row from its V row (max and
+// 1-norm), then per panel row.
 int build_tc(HMatrix &H) {
   TcPlan tp;
   make_tc_plan(H.plan, tp);
@@ -226,26 +228,47 @@ int build_tc(HMatrix &H) {
   t.n_reduce = H.dp.nmvr;
   t.ctas = H.num_sms;
   t.xt_rows = H.plan.xt_len;
+  // XT row of every P row (the rows of V items cut into column pieces)
+  std::vector<int32_t> p2t(static_cast<size_t>(std::max<int64_t>(H.plan.p_rows, 1)), 0);
+  for (const MVReduce &D : H.plan.mv_reduce)
+    for (int32_t j = 0; j < D.npieces; j++)
+      for (int32_t r = 0; r < D.nrows; r++)
+        p2t[static_cast<size_t>(D.p_row) + static_cast<size_t>(j) * D.nrows + r] = D.t_row + r;
   std::vector<TcPack> vj, dj;
   for (size_t i = 0; i < tp.v_items.size(); i++) {
     const MVItem &it = H.plan.mv_items[i];
-    vj.push_back(TcPack{tp.v_src[i], tp.v_items[i].a_off, it.stride, it.nrows, it.ncols, 0});
+    const int32_t trow = it.kind == 0 ? it.out : p2t[static_cast<size_t>(it.out)];
+    vj.push_back(TcPack{tp.v_src[i], tp.v_items[i].a_off, it.stride, it.nrows, it.ncols, 1, 0, trow});
   }
   for (size_t i = 0; i < tp.du_items.size(); i++) {
-    const TcItem &t = tp.du_items[i];
-    dj.push_back(TcPack{tp.du_src[i], t.a_off, H.plan.tiles[t.out].ld, t.m, t.ncols, 0});
+    const TcItem &ti = tp.du_items[i];
+    dj.push_back(TcPack{tp.du_src[i], ti.a_off, H.plan.tiles[ti.out].ld, ti.m, ti.ncols, 0, ti.map, 0});
   }
   TcPack *dvj = nullptr, *ddj = nullptr;
-  if ((rc = upload(H, &dvj, vj)) || (rc = upload(H, &ddj, dj))) return rc;
-  cudaError_t e = launch_pack_tc(dvj, static_cast<int64_t>(vj.size()), static_cast<const float *>(H.vdata),
-                                 t.adata, 0);
+  VGroup *dg = nullptr;
+  float *sc = nullptr;  // nu | gam | colsc, xt_len each
+  const int64_t xr = H.plan.xt_len;
+  if ((rc = upload(H, &dvj, vj)) || (rc = upload(H, &ddj, dj)) || (rc = upload(H, &dg, H.plan.vgroups)) ||
+      (rc = H.dalloc(reinterpret_cast<void **>(&sc), 3 * xr * sizeof(float))))
+    return rc;
+  cudaError_t e = cudaMemset(sc, 0, 3 * xr * sizeof(float));
   if (e == cudaSuccess)
-    e = launch_pack_tc(ddj, static_cast<int64_t>(dj.size()), static_cast<const float *>(H.panels), t.adata, 0);
+    e = launch_tc_scales(dg, static_cast<int64_t>(H.plan.vgroups.size()), static_cast<const float *>(H.vdata), xr,
+                         sc, sc + xr, sc + 2 * xr, 0);
+  if (e == cudaSuccess)
+    e = launch_pack_tc(dvj, static_cast<int64_t>(vj.size()), static_cast<const float *>(H.vdata), t.adata,
+                       t.colmap, sc + 2 * xr, sc, sc + xr, 0);
+  if (e == cudaSuccess)
+    e = launch_pack_tc(ddj, static_cast<int64_t>(dj.size()), static_cast<const float *>(H.panels), t.adata,
+                       t.colmap, sc + 2 * xr, sc, sc + xr, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "tensor-core packing");
   H.dfree(dvj);
   H.dfree(ddj);
-  H.device_bytes -= static_cast<int64_t>((vj.size() + dj.size()) * sizeof(TcPack));
+  H.dfree(dg);
+  H.dfree(sc);
+  H.device_bytes -= static_cast<int64_t>((vj.size() + dj.size()) * sizeof(TcPack) +
+                                         H.plan.vgroups.size() * sizeof(VGroup) + 3 * xr * sizeof(float));
   return HMGPU_OK;
 }
 
@@ -461,7 +484,8 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
       const int64_t xb = H.plan.xt_len * 2 * 32 * 2;
       if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts), xb)) ||
           (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.prow),
-                         std::max<int64_t>(H.plan.p_rows, 1) * hm::kTcMaxRhs * 4)))
+                         std::max<int64_t>(H.plan.p_rows, 1) * hm::kTcMaxRhs * 4)) ||
+          (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xscale), 2 * hm::kTcMaxRhs * sizeof(float))))
         return rc;
       cudaMemsetAsync(H.tc.xts, 0, xb, s);
       if (cudaError_t e = hm::encode_xts_map(H.tc, 32)) return hm::cuda_fail(e, "tensor map of XTS");
@@ -485,7 +509,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
       const int nr = static_cast<int>(std::min<int64_t>(per, nrhs - k0));
       int nl = 0;
       cudaError_t e;
-      if (tc)  // BF16 (hi, lo) splits on the tensor cores
+      if (tc)  // scaled FP16 (hi, lo) splits on the tensor cores
         e = hm::launch_matvec_tc(H.dp, H.tc, reinterpret_cast<const float *>(static_cast<const char *>(x) + k0 * ldx * es),
                                  ldx, nr, reinterpret_cast<float *>(static_cast<char *>(y) + k0 * ldy * es), ldy,
                                  s, ev, &nl);

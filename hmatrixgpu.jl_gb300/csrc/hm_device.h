@@ -71,18 +71,22 @@ int rhs_per_pass();
 int multi_width(int nr);
 // Mixed-precision tensor-core product (hm_tc.cu), 32 or 64 right-hand sides
 // per pass.
-struct TcPack {  // one item's FP32 row-major source -> canonical BF16 chunks
+struct TcPack {  // one item's FP32 row-major source -> canonical FP16 chunks and row factors
   int64_t src_off, a_off;
-  int32_t ld, m, ncols, pad;
+  int32_t ld, m, ncols;
+  int32_t kind;  // 0: near/U rows (columns scaled through colmap[map + c]), 1: V rows
+  int32_t map;   // kind 0: colmap offset of column 0
+  int32_t trow;  // kind 1: XT row (rank row) of row 0; rows are consecutive
 };
 struct DevTc {
-  void *adata = nullptr;  // canonical BF16 (hi, lo) chunks of every item
+  void *adata = nullptr;  // canonical FP16 (hi, lo) chunks of every item, each with its row factors
   TcItem *v_items = nullptr, *du_items = nullptr;
   int32_t *colmap = nullptr;
   MVReduce *reduce = nullptr;
-  uint16_t *xts = nullptr;    // xt_len rows of 32 BF16 hi + 32 BF16 lo (passes of <= 32 columns)
-  uint16_t *xts64 = nullptr;  // xt_len rows of 64 BF16 hi + 64 BF16 lo (passes of 33..64 columns)
+  uint16_t *xts = nullptr;    // xt_len rows of 32 FP16 hi + 32 FP16 lo (passes of <= 32 columns)
+  uint16_t *xts64 = nullptr;  // xt_len rows of 64 FP16 hi + 64 FP16 lo (passes of 33..64 columns)
   float *prow = nullptr;      // partial rows of split V items, 64 values per row
+  float *xscale = nullptr;    // per pass: max |x_r| bits (64 words), then 1 / sigma_r (64 floats)
   int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;
   int64_t xt_rows = 0;  // rows of either XTS
   CUtensorMap xmap[2];  // tile-load maps of xts and xts64 (encode_xts_map)
@@ -92,7 +96,13 @@ size_t tc_smem_bytes(int nr);
 // The tile-load map of the XTS of width R (32: xts, 64: xts64), after the
 // buffer exists.
 cudaError_t encode_xts_map(DevTc &t, int R);
-cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s);
+// Scales of the rank rows from the FP32 V rows of every source group: nu
+// (max magnitude into [2^14, 2^15)), gam (2^-ceil(log2 of the row's 1-norm))
+// at each row's XT row, and colsc (1 / gam on t rows, 1 on x rows; xt_rows).
+cudaError_t launch_tc_scales(const VGroup *groups, int64_t ngroups, const float *vdata, int64_t xt_rows,
+                             float *nu, float *gam, float *colsc, cudaStream_t s);
+cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, const int32_t *colmap,
+                           const float *colsc, const float *nu, const float *gam, cudaStream_t s);
 // permutation + split of X, V pass, reduction of pieces, near/U pass over
 // nr <= 64 columns (xts64 must exist for nr > 32); ev (optional) gets 4
 // events as launch_matvec_multi.

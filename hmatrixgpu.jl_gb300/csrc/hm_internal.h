@@ -129,10 +129,11 @@ struct MVReduce {
 };
 
 // A work item of the tensor-core product: a panel of m <= 64 rows and
-// ncols columns stored as BF16 (hi, lo) pairs in the UMMA canonical K-major
-// layout, 64 columns per chunk (the last chunk rounded up to 16 columns):
-// chunk c holds hi then lo, each ceil(m / 8) groups of 8 rows x kc columns
-// (kc * 16 bytes per group). Column j of the panel meets XT row
+// ncols columns stored as scaled FP16 (hi, lo) pairs in the UMMA canonical
+// K-major layout, 64 columns per chunk (the last chunk rounded up to 16
+// columns): chunk c holds hi then lo, each ceil(m / 8) groups of 8 rows x kc
+// columns (kc * 16 bytes per group); after the last chunk, 64 FP32 row
+// factors that undo the rows' scales. Column j of the panel meets XT row
 // map + j (V items) or colmap[map + j] (near/U items). Row tiles of more
 // than 64 rows become several items.
 struct TcItem {

@@ -1,13 +1,25 @@
 // Mixed-precision multi-right-hand-side product on the 5th-generation tensor
-// cores (tcgen05, sm_103a): Y = H X for up to 32 right-hand sides per pass.
+// cores (tcgen05, sm_103a): Y = H X for up to 64 right-hand sides per pass.
 //
 // Storage. Every panel of the product (a row tile of the near/U pass, or a
-// column piece of at most 128 V rows of a source group) is stored once more as
-// BF16 pairs a = hi + lo (hi = bf16(a), lo = bf16(a - hi); relative residual
-// about 2^-17; all four products of the hi/lo pairs are formed), already in
-// the UMMA canonical K-major layout, 64 columns per
-// chunk, so a chunk is two contiguous byte ranges copied as they are. The right-hand sides live in XTS, one 128-byte
-// row per entry of XT = [x permuted | t]: 32 BF16 hi values, then 32 lo values.
+// column piece of at most 64 V rows of a source group) is stored once more as
+// FP16 pairs a = hi + lo (hi = fp16(a), lo = fp16(a - hi): 22 significant
+// bits, relative residual about 2^-23), already in the UMMA canonical K-major
+// layout, 64 columns per chunk, so a chunk is two contiguous byte ranges
+// copied as they are. FP16 has FP32's precision to within two bits but a
+// narrow exponent range, so every operand carries power-of-two scales that
+// put its largest magnitude in [2^14, 2^15) (exact, and undone exactly):
+//   panel rows   one scale per row (rho_i), undone in the epilogue; its
+//                inverse trails the item's chunks (64 floats);
+//   V rows       nu_k per rank row, and a second per-rank-row scale gamma_k =
+//                2^-ceil(log2 ||V_k||_1) that bounds the t entries it makes:
+//                the V pass writes t~_k = t_k sigma gamma_k (below 2^15 for
+//                any x), and the U columns that read t~_k are stored times
+//                1/gamma_k;
+//   x            sigma_r per right-hand side, from max |x_r| at run time,
+//                undone on y.
+// The right-hand sides live in XTS, one row per entry of XT = [x permuted |
+// t]: R FP16 hi values, then R lo values (4R bytes).
 //
 // Pipeline (one persistent CTA per SM; items from a ticket counter, in list
 // order, so concurrent CTAs work on neighbouring panels and share XTS rows in
@@ -18,12 +30,13 @@
 //               copies of the chunk that complete on the stage's mbarrier (hi
 //               rows to tile rows 0..63, lo rows to tile rows 64..127), and
 //               the XTS rows of its columns (whole rows) as an N-major
-//               (MN-major) BF16 tile: for a whole 64-column chunk of a V
-//               piece, whose columns are consecutive rows, one TMA tile load
-//               on the same barrier; for a row tile or a V piece's last,
-//               partial chunk, 16-byte cp.async gathers (padding columns read
-//               the zero row), then a wait, a proxy fence and an mbarrier
-//               arrive;
+//               (MN-major) FP16 tile: for a V piece, whose columns are
+//               consecutive rows, one TMA tile load on the same barrier (in a
+//               last chunk with padding columns, on the warp's own barrier,
+//               after which the warp zeroes the padding rows and publishes);
+//               for a row tile, 16-byte cp.async gathers (padding columns
+//               read the zero row), then a wait, a proxy fence and an
+//               mbarrier arrive;
 //   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
 //               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 2R (hi and lo
 //               stacked along both M and N; items have at most 64 rows), into
@@ -34,12 +47,13 @@
 //               warp's 32 TMEM lanes, the sum of the four hi/lo quadrants
 //               (the hi-row and lo-row warps of the same rows swap halves of
 //               their sums, so each finishes half of the right-hand sides),
-//               then y rows, t rows of XTS (split again) or partial rows P.
+//               the scales undone, then y rows, t rows of XTS (split again)
+//               or partial rows P.
 // Every wait is bounded by the global timer; one that runs out records a code
 // in `status`, raises a CTA-wide abort flag and every role leaves its loop.
 #include <cuda.h>
 #include <cudaTypedefs.h>
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "hm_device.h"
@@ -65,7 +79,7 @@ template <int R>
 struct TcShape {
   static_assert(R == 32 || R == 64, "32 or 64 right-hand sides per pass");
   static constexpr int kBN = 2 * R;                   // B rows: R hi, then R lo
-  static constexpr int kBBytes = kBN * kKc * 2;       // one BF16 B tile: 8 or 16 KB
+  static constexpr int kBBytes = kBN * kKc * 2;       // one FP16 B tile: 8 or 16 KB
   static constexpr int kStages = R == 32 ? 8 : 6;
   static constexpr int kBProducers = kStages;         // warps 1, 3, 8 .. 5 + kStages
   static constexpr int kEpi1 = 6 + kBProducers;       // first warp of the second epilogue set
@@ -76,10 +90,10 @@ struct TcShape {
   static constexpr uint32_t kBGroupK = (kBN / 8) * kBGroupN;
   static constexpr int kPieces = R / 4;               // 16-byte pieces of an XTS row
   static constexpr int kRowsPerCopy = 32 / kPieces;   // XTS rows per warp-wide copy
-  // kind::f16 instruction descriptor: FP32 D, BF16 A (K-major) and B
+  // kind::f16 instruction descriptor: FP32 D, FP16 A (K-major) and B
   // (MN-major), N = kBN, M = 128.
-  static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) |
-                                     ((static_cast<uint32_t>(kBN) >> 3) << 17) | ((128u >> 4) << 24);
+  static constexpr uint32_t kIdesc = (1u << 4) | (1u << 16) | ((static_cast<uint32_t>(kBN) >> 3) << 17) |
+                                     ((128u >> 4) << 24);
   // One producer per stage: a producer then never waits for a stage more than
   // one release ahead, which a parity wait on the stage's barrier could not
   // tell apart from the release before.
@@ -181,7 +195,7 @@ struct TcSmem {
   // per epilogue set: halves of the row sums handed from the lo-row warps to
   // the hi-row warps (xa) and back (xb)
   float xa[2][64][R / 2 + 1], xb[2][64][R / 2 + 1];
-  uint64_t full[Sh::kStages], empty[Sh::kStages], acc_full[2], acc_empty[2];
+  uint64_t full[Sh::kStages], empty[Sh::kStages], bfull[Sh::kStages], acc_full[2], acc_empty[2];
   uint64_t xa_ready[2], xa_free[2], xb_ready[2], xb_free[2];
   uint64_t qfull[kQ], qempty[kQ];
   TcItem qdata[kQ];  // item queue: ticket order; kind -1 ends it
@@ -250,18 +264,36 @@ __device__ __forceinline__ bool next_item(SM &S, int n, int32_t *status, TcItem 
 __device__ __forceinline__ int64_t chunk_bytes(int G, int kc) { return static_cast<int64_t>(G) * kc * 16; }
 
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  __half2 v = __floats2half2_rn(a, b);
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
-// hi/lo split of 8 values into two 16-byte words
+// hi/lo split of 8 values (|v| < 2^16) into two 16-byte words of FP16:
+// hi = fp16(v), lo = fp16(v - hi), v - hi exact in FP32
 __device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo) {
   float h[8];
 #pragma unroll
-  for (int i = 0; i < 8; i++) h[i] = __bfloat162float(__float2bfloat16_rn(v[i]));
+  for (int i = 0; i < 8; i++) h[i] = __half2float(__float2half_rn(v[i]));
   hi = make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
   lo = make_uint4(pack2(v[0] - h[0], v[1] - h[1]), pack2(v[2] - h[2], v[3] - h[3]),
                   pack2(v[4] - h[4], v[5] - h[5]), pack2(v[6] - h[6], v[7] - h[7]));
+}
+
+// 2^e for the scale that puts a largest magnitude `mx` in [2^14, 2^15); 1 for
+// a zero, infinite or NaN `mx` (the values then pass unscaled and a non-finite
+// input stays non-finite). Exponents are clamped so that the scale and its
+// inverse are normal FP32 numbers.
+__device__ __forceinline__ float pow2_scale(float mx) {
+  if (!(mx > 0.0f) || !isfinite(mx)) return 1.0f;
+  int e = 14 - ilogbf(mx);
+  e = max(-120, min(120, e));
+  return __int_as_float((e + 127) << 23);
+}
+
+// Offset of the row factors (64 floats) that trail an item's chunks.
+__device__ __host__ __forceinline__ int64_t trailer_off(int m, int ncols) {
+  const int64_t npad = ncols > 0 ? (ncols + 15) & ~15 : 16;
+  return int64_t(32) * ((m + 7) / 8) * npad;
 }
 
 // Self-test of the bounded wait: a barrier nobody arrives at, waited on with
@@ -280,14 +312,15 @@ __global__ void wait_selftest_kernel(unsigned long long limit_ns, int32_t *statu
 }
 
 struct TcArgs {
-  CUtensorMap xmap;            // XTS as 8 BF16 x rows x N groups: the B tiles of V pieces
+  CUtensorMap xmap;            // XTS as 8 FP16 x rows x N groups: the B tiles of V pieces
   const unsigned char *adata;  // tensor-core panels
   const TcItem *items;
   int32_t nitems;
   int32_t grab;                // items per ticket while many remain (1 or 8)
   int32_t *ticket;             // next item (zeroed by the permutation kernel)
   const int32_t *colmap;
-  const uint16_t *xts;         // XTS rows (64 BF16 each)
+  const uint16_t *xts;         // XTS rows (2R FP16 each)
+  const float *xs_inv;         // 1 / sigma_r per right-hand side (64)
   uint16_t *xts_out;           // t rows (kind 1)
   float *prow;                 // P rows (kind 2)
   const TileDesc *tiles;
@@ -312,6 +345,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     for (int s = 0; s < kStages; s++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.full[s])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.empty[s])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.bfull[s])));
     }
     for (int b = 0; b < 2; b++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.acc_full[b])));
@@ -386,6 +420,8 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // proxy and publishes the stage.
     const int bw = warp == 1 ? 0 : warp == 3 ? 1 : warp - 6;  // 0..kStages-1
     int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
+    uint32_t tails = 0;          // tile loads completed on this warp's bfull barrier
+    bool tail_pending = false;   // a tile load on bfull not yet seen complete
     bool stop = false;
     const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
     for (int n = 0; !stop; n++) {
@@ -395,11 +431,14 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         if (g % kStages != bw) continue;
         const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
-        // B by one tile load only where all 64 columns of the chunk are the
-        // item's own: the padding columns of a last, partial chunk must read
-        // the zero row (0 * Inf or 0 * NaN from a neighbour's row would reach
-        // this item's sums)
-        const bool tma_b = I.kind != 0 && c0 + kKc <= I.ncols;
+        // B of a V piece by one tile load of 64 XTS rows. In a last chunk
+        // whose columns [ncols, kc) are padding, those rows belong to other
+        // blocks (or are t rows being rewritten) and must not reach the MMA
+        // (0 * Inf or 0 * NaN): the load completes on the warp's own bfull
+        // barrier, the warp zeroes the padding rows and only then publishes
+        // the stage.
+        const bool tma_b = I.kind != 0;
+        const bool pad = tma_b && I.ncols - c0 < kc;
         int rows[kKc / 32];  // XTS rows of columns c0 + lane + 32 h
 #pragma unroll
         for (int h = 0; h < kKc / 32; h++) {
@@ -422,7 +461,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
           const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
           const uint32_t bar = su32(&S.full[s]);
-          const uint32_t btx = tma_b ? static_cast<uint32_t>(Sh::kBBytes) : 0u;
+          const uint32_t btx = tma_b && !pad ? static_cast<uint32_t>(Sh::kBBytes) : 0u;
           asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2 * half + btx)
                        : "memory");
           asm volatile(
@@ -437,17 +476,43 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
             // B of a V piece: its columns are the consecutive XTS rows map + c0
             // .., so one tile load of 64 rows lands them in the canonical
             // MN-major layout (K groups 128 B apart, N groups 1024 B apart)
+            const uint32_t bb = pad ? su32(&S.bfull[s]) : bar;
+            if (pad)
+              asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb),
+                           "r"(static_cast<uint32_t>(Sh::kBBytes))
+                           : "memory");
             asm volatile(
                 "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
                 "%4}], [%5];" ::"r"(su32(S.b[s])),
-                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bar)
+                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bb)
                 : "memory");
-            arrive(&S.full[s]);
+            if (!pad) arrive(&S.full[s]);
           }
         }
         last_g = g;
-        if (tma_b) {  // the copies complete on the stage's barrier
+        if (tma_b && !pad) {  // the copies complete on the stage's barrier
           __syncwarp();
+          continue;
+        }
+        if (pad) {
+          tail_pending = true;
+          if (!wait_bar_warp(S, &S.bfull[s], tails & 1u, a.status, 32)) {
+            stop = true;
+            break;
+          }
+          tail_pending = false;
+          tails++;
+          // rows [valid, kc) of every N group (16 bytes per row and group) to zero
+          const int valid = I.ncols - c0, nz = kc - valid;
+          for (int e = lane; e < nz * (Sh::kBN / 8); e += 32) {
+            const int k = valid + e % nz, gq = e / nz;
+            asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(su32(S.b[s]) + gq * 1024u + k * 16u),
+                         "r"(0u)
+                         : "memory");
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) arrive(&S.full[s]);
           continue;
         }
         const uint32_t dst0 = su32(S.b[s]) + piece * kBGroupN;
@@ -473,6 +538,8 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // aborted or not (one stage per producer: earlier chunks have landed).
     if (last_g >= 0 && lane == 0) {
       volatile int32_t none = 0;
+      if (tail_pending)  // a tile load on bfull that the abort left unwaited
+        wait_bar_bounded(&S.bfull[bw], tails & 1u, &none, a.status, 33, kWaitNs);
       wait_bar_bounded(&S.full[last_g % kStages], static_cast<uint32_t>((last_g / kStages) & 1), &none, a.status, 31,
                        kWaitNs);
     }
@@ -512,10 +579,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           for (int h = 0; h < two; h++) {
             const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
             // leading byte offset: K direction; stride byte offset: N direction.
-            // Whole chunks of V pieces come from the tile load (K groups 128 B
-            // apart, N groups 1024 B), the rest from the gather (kBGroupK,
-            // 128 B); the producer decides by the same test.
-            const bool tma_b = I.kind != 0 && c0 + h * kKc + kKc <= I.ncols;
+            // V pieces' B tiles come from the tile load (K groups 128 B apart,
+            // N groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B).
+            const bool tma_b = I.kind != 0;
             const uint64_t db = tma_b ? sdesc(su32(S.b[s2[h]]), 128, 1024)
                                       : sdesc(su32(S.b[s2[h]]), Sh::kBGroupK, kBGroupN);
             for (int ks = 0; ks < kc2[h] / 16; ks++) {
@@ -583,11 +649,15 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       __syncwarp();
       if (lane == 0) arrive(i_free);
       if (row >= I.m) continue;
+      // the row's factor: 1 / rho_i (kind 0), or gamma_k / nu_k (V rows)
+      const float f = __ldg(reinterpret_cast<const float *>(a.adata + I.a_off + trailer_off(I.m, I.ncols)) + row);
+#pragma unroll
+      for (int c = 0; c < H; c++) w[c] *= f;
       if (I.kind == 0) {
         float *yr = a.y + a.tmap0[a.tiles[I.out].row0 + I.row0 + row];
 #pragma unroll
         for (int c = 0; c < H; c++)
-          if (keep + c < a.nr) yr[(keep + c) * a.ldy] = w[c];
+          if (keep + c < a.nr) yr[(keep + c) * a.ldy] = w[c] * __ldg(a.xs_inv + keep + c);
       } else if (I.kind == 1) {
         uint4 *dst = reinterpret_cast<uint4 *>(a.xts_out + static_cast<int64_t>(I.out + row) * (2 * R)) + keep / 8;
 #pragma unroll
@@ -610,22 +680,58 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(Sh::kTmemCols));
 }
 
+// max |X[., r]| per right-hand side r < nr, as FP32 bits (non-negative
+// floats order as unsigned integers) into xmax[r], which starts at zero.
+__global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, int64_t n_src,
+                            unsigned *__restrict__ xmax) {
+  __shared__ unsigned smax[kTcMaxRhs];
+  for (int r = threadIdx.x; r < kTcMaxRhs; r += blockDim.x) smax[r] = 0u;
+  __syncthreads();
+  for (int r = 0; r < nr; r++) {
+    unsigned m = 0u;
+    for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < n_src;
+         j += static_cast<int64_t>(gridDim.x) * blockDim.x)
+      m = max(m, __float_as_uint(fabsf(X[j + r * ldx])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&smax[r], m);
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < nr; r += blockDim.x) atomicMax(&xmax[r], smax[r]);
+}
+
+// sigma_r = pow2_scale(max |x_r|) for r < R (1 beyond nr); block 0 also
+// stores 1 / sigma_r for the epilogue.
+template <int R>
+__device__ __forceinline__ void load_sigma(const unsigned *xmax, int nr, float *sg, float *xs_inv) {
+  for (int r = threadIdx.x; r < R; r += blockDim.x) {
+    const float s = r < nr ? pow2_scale(__uint_as_float(xmax[r])) : 1.0f;
+    sg[r] = s;
+    if (blockIdx.x == 0) xs_inv[r] = 1.0f / s;
+  }
+  __syncthreads();
+}
+
 // XTS x rows from X in its own order: the R right-hand sides X[j + r ldx]
-// (0 for r >= nr) of source index j, split into BF16 hi (first 2R bytes) and
-// lo (last 2R bytes), go to row sinv[j]. Reads of X are coalesced along j and
-// every row is written whole; x-region rows that no source index maps to stay
-// zero from the allocation. Also re-arms the two item tickets.
+// (0 for r >= nr) of source index j, times sigma_r, split into FP16 hi
+// (first 2R bytes) and lo (last 2R bytes), go to row sinv[j]. Reads of X are
+// coalesced along j and every row is written whole; x-region rows that no
+// source index maps to stay zero from the allocation. Also re-arms the two
+// item tickets.
 template <int R>
 __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, int nr,
                                      const int32_t *__restrict__ sinv0, int64_t n_src,
-                                     uint16_t *__restrict__ xts, int32_t *__restrict__ tickets) {
+                                     uint16_t *__restrict__ xts, int32_t *__restrict__ tickets,
+                                     const unsigned *__restrict__ xmax, float *__restrict__ xs_inv) {
   __shared__ float tile[64][R + 1];
+  __shared__ float sg[R];
   if (blockIdx.x == 0 && threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
+  load_sigma<R>(xmax, nr, sg, xs_inv);
   for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
     for (int e = threadIdx.x; e < 64 * R; e += blockDim.x) {
       const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
       const int64_t j = j0 + jj;
-      tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] : 0.0f;
+      tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] * sg[r] : 0.0f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * (R / 8); e += blockDim.x) {
@@ -645,8 +751,9 @@ __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, i
   }
 }
 
-// t rows from partial rows, pieces summed in order; one warp per row, lane =
-// right-hand side (and lane + 32 in a 64-wide pass).
+// t rows from partial rows (already scaled by their rows' factors), pieces
+// summed in order; one warp per row, lane = right-hand side (and lane + 32 in
+// a 64-wide pass).
 template <int R>
 __global__ void reduce_split_kernel(const MVReduce *__restrict__ red, int32_t nred, const float *__restrict__ P,
                                     uint16_t *__restrict__ xts) {
@@ -660,8 +767,8 @@ __global__ void reduce_split_kernel(const MVReduce *__restrict__ red, int32_t nr
         float s = 0.0f;
         for (int j = 0; j < D.npieces; j++)
           s += P[(static_cast<int64_t>(D.p_row) + static_cast<int64_t>(j) * D.nrows + row) * R + c];
-        const __nv_bfloat16 hb = __float2bfloat16_rn(s);
-        const __nv_bfloat16 lb = __float2bfloat16_rn(s - __bfloat162float(hb));
+        const __half hb = __float2half_rn(s);
+        const __half lb = __float2half_rn(s - __half2float(hb));
         dst[c] = *reinterpret_cast<const uint16_t *>(&hb);
         dst[R + c] = *reinterpret_cast<const uint16_t *>(&lb);
       }
@@ -669,10 +776,84 @@ __global__ void reduce_split_kernel(const MVReduce *__restrict__ red, int32_t nr
   }
 }
 
-// Canonical BF16 (hi, lo) chunks of one item from its FP32 row-major source.
+// Scales of the rank rows, from the FP32 V rows of each source group (one
+// block per group, a warp per row): nu[t] = pow2_scale(max |V_t|) and
+// gam[t] = 2^-ceil(log2 ||V_t||_1) (1 for a zero row), at the row's XT row t;
+// colsc[t] = 1 / gam[t] (colsc is 1 on the x rows).
+__global__ void tscale_kernel(const VGroup *__restrict__ groups, const float *__restrict__ vdata,
+                              float *__restrict__ nu, float *__restrict__ gam, float *__restrict__ colsc) {
+  const VGroup g = groups[blockIdx.x];
+  const int lane = threadIdx.x & 31;
+  for (int r = threadIdx.x >> 5; r < g.rows; r += blockDim.x >> 5) {
+    const float *v = vdata + g.v_off + static_cast<int64_t>(r) * g.stride;
+    float mx = 0.0f, l1 = 0.0f;
+    for (int j = lane; j < g.stride; j += 32) {
+      const float a = fabsf(v[j]);
+      mx = fmaxf(mx, a);
+      l1 += a;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      l1 += __shfl_xor_sync(0xffffffffu, l1, o);
+    }
+    if (lane == 0) {
+      float gm = 1.0f;
+      if (l1 > 0.0f && isfinite(l1)) {
+        // the smallest power of two >= l1, with a margin for the rounding of l1
+        int e = ilogbf(l1 * 1.0001f) + 1;
+        e = max(-120, min(120, e));
+        gm = __int_as_float((127 - e) << 23);
+      }
+      const int64_t t = static_cast<int64_t>(g.t_off) + r;
+      nu[t] = pow2_scale(mx);
+      gam[t] = gm;
+      colsc[t] = 1.0f / gm;
+    }
+  }
+}
+
+__global__ void fill_kernel(float *__restrict__ p, int64_t n, float v) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[i] = v;
+}
+
+// Canonical FP16 (hi, lo) chunks of one item from its FP32 row-major source,
+// with the item's row factors after them. Near/U rows (kind 0): every column
+// times colsc of its XT row, the row scaled by rho_i = pow2_scale(its largest
+// magnitude), factor 1 / rho_i. V rows (kind 1): scaled by nu of their rank
+// row, factor gam / nu.
 __global__ void pack_tc_kernel(const TcPack *__restrict__ jobs, const float *__restrict__ src,
-                               unsigned char *__restrict__ adata) {
+                               unsigned char *__restrict__ adata, const int32_t *__restrict__ colmap,
+                               const float *__restrict__ colsc, const float *__restrict__ nu,
+                               const float *__restrict__ gam) {
   const TcPack J = jobs[blockIdx.x];
+  __shared__ float rs[64], fac[64];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  auto csc = [&](int c) { return J.kind == 0 ? colsc[colmap[J.map + c]] : 1.0f; };
+  for (int r = warp; r < 64; r += blockDim.x >> 5) {
+    float sc = 1.0f, f = 0.0f;
+    if (r < J.m) {
+      if (J.kind == 0) {
+        float mx = 0.0f;
+        for (int c = lane; c < J.ncols; c += 32)
+          mx = fmaxf(mx, fabsf(src[J.src_off + static_cast<int64_t>(r) * J.ld + c] * csc(c)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sc = pow2_scale(mx);
+        f = 1.0f / sc;
+      } else {
+        sc = nu[J.trow + r];
+        f = gam[J.trow + r] / sc;
+      }
+    }
+    if (lane == 0) {
+      rs[r] = sc;
+      fac[r] = f;
+    }
+  }
+  __syncthreads();
   const int G = (J.m + 7) >> 3;
   const int npad = J.ncols > 0 ? (J.ncols + 15) & ~15 : 16;
   unsigned char *base = adata + J.a_off;
@@ -686,7 +867,8 @@ __global__ void pack_tc_kernel(const TcPack *__restrict__ jobs, const float *__r
 #pragma unroll
       for (int i = 0; i < 8; i++) {
         const int c = c0 + k8 + i;
-        v[i] = (r < J.m && c < J.ncols) ? src[J.src_off + static_cast<int64_t>(r) * J.ld + c] : 0.0f;
+        v[i] = (r < J.m && c < J.ncols) ? src[J.src_off + static_cast<int64_t>(r) * J.ld + c] * csc(c) * rs[r]
+                                        : 0.0f;
       }
       uint4 hi, lo;
       split8(v, hi, lo);
@@ -696,6 +878,8 @@ __global__ void pack_tc_kernel(const TcPack *__restrict__ jobs, const float *__r
     }
     base += 2 * half;
   }
+  float *tr = reinterpret_cast<float *>(adata + J.a_off + trailer_off(J.m, J.ncols));
+  for (int r = threadIdx.x; r < 64; r += blockDim.x) tr[r] = fac[r];
 }
 
 }  // namespace
@@ -733,7 +917,7 @@ cudaError_t encode_xts_map(DevTc &t, int R) {
   cuuint64_t strides[2] = {static_cast<cuuint64_t>(4 * R), 16};
   cuuint32_t box[3] = {8, 64, static_cast<cuuint32_t>(2 * R / 8)};
   cuuint32_t es[3] = {1, 1, 1};
-  const CUresult r = enc(&t.xmap[R / 64], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, xts, dims, strides, box, es,
+  const CUresult r = enc(&t.xmap[R / 64], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, xts, dims, strides, box, es,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
@@ -748,14 +932,19 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   int gp = static_cast<int>((p.n_src + 63) / 64);
   if (gp > 2048) gp = 2048;
   if (ev) cudaEventRecord(ev[0], s);
-  permute_split_kernel<R><<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xts, p.counter + 2);
-  nl++;
+  unsigned *xmax = reinterpret_cast<unsigned *>(t.xscale);
+  float *xs_inv = t.xscale + kTcMaxRhs;
+  cudaMemsetAsync(xmax, 0, kTcMaxRhs * sizeof(unsigned), s);
+  xmax_kernel<<<gp < 512 ? gp : 512, 256, 0, s>>>(X, ldx, nr, p.n_src, xmax);
+  permute_split_kernel<R><<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xts, p.counter + 2, xmax, xs_inv);
+  nl += 2;
   if (ev) cudaEventRecord(ev[1], s);
   TcArgs a{};
   a.xmap = t.xmap[R / 64];
   a.adata = static_cast<const unsigned char *>(t.adata);
   a.colmap = t.colmap;
   a.xts = xts;
+  a.xs_inv = xs_inv;
   a.xts_out = xts;
   a.prow = t.prow;
   a.tiles = p.tiles;
@@ -789,17 +978,28 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   return nl;
 }
 
-cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, cudaStream_t s) {
+cudaError_t launch_tc_scales(const VGroup *groups, int64_t ngroups, const float *vdata, int64_t xt_rows,
+                             float *nu, float *gam, float *colsc, cudaStream_t s) {
+  fill_kernel<<<1024, 256, 0, s>>>(colsc, xt_rows, 1.0f);
+  for (int64_t g0 = 0; g0 < ngroups; g0 += 65535) {
+    const int nb = static_cast<int>(ngroups - g0 < 65535 ? ngroups - g0 : 65535);
+    tscale_kernel<<<nb, 256, 0, s>>>(groups + g0, vdata, nu, gam, colsc);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, void *adata, const int32_t *colmap,
+                           const float *colsc, const float *nu, const float *gam, cudaStream_t s) {
   for (int64_t j0 = 0; j0 < njobs; j0 += 65535) {
     const int nb = static_cast<int>(njobs - j0 < 65535 ? njobs - j0 : 65535);
-    pack_tc_kernel<<<nb, 256, 0, s>>>(jobs + j0, src, static_cast<unsigned char *>(adata));
+    pack_tc_kernel<<<nb, 256, 0, s>>>(jobs + j0, src, static_cast<unsigned char *>(adata), colmap, colsc, nu, gam);
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr,
                              float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches) {
-  if (nr < 1 || nr > 64 || (nr > 32 && !t.xts64) || !t.xts) return cudaErrorInvalidValue;
+  if (nr < 1 || nr > 64 || (nr > 32 && !t.xts64) || !t.xts || !t.xscale) return cudaErrorInvalidValue;
   tc_attrs();
   const int nl = nr > 32 ? run_tc<64>(p, t, X, ldx, nr, Y, ldy, s, ev) : run_tc<32>(p, t, X, ldx, nr, Y, ldy, s, ev);
   if (launches) *launches = nl;
