@@ -234,15 +234,24 @@ int build_tc(HMatrix &H) {
     for (int32_t j = 0; j < D.npieces; j++)
       for (int32_t r = 0; r < D.nrows; r++)
         p2t[static_cast<size_t>(D.p_row) + static_cast<size_t>(j) * D.nrows + r] = D.t_row + r;
+  // batch members: contiguous source ranges (right-hand-side scales are per
+  // member, so a batch's products equal its members' own) and row ranges
+  std::vector<int64_t> mcol = H.member_cols, mrow = H.member_rows;
+  if (mcol.size() < 2) mcol = {0, H.bs.n}, mrow = {0, H.bs.m};
+  t.nmem = static_cast<int32_t>(mcol.size() - 1);
+  if ((rc = upload(H, &t.mcol0, mcol))) return rc;
   std::vector<TcPack> vj, dj;
   for (size_t i = 0; i < tp.v_items.size(); i++) {
     const MVItem &it = H.plan.mv_items[i];
     const int32_t trow = it.kind == 0 ? it.out : p2t[static_cast<size_t>(it.out)];
-    vj.push_back(TcPack{tp.v_src[i], tp.v_items[i].a_off, it.stride, it.nrows, it.ncols, 1, 0, trow});
+    vj.push_back(TcPack{tp.v_src[i], tp.v_items[i].a_off, it.stride, it.nrows, it.ncols, 1, 0, trow, 0, 0});
   }
   for (size_t i = 0; i < tp.du_items.size(); i++) {
     const TcItem &ti = tp.du_items[i];
-    dj.push_back(TcPack{tp.du_src[i], ti.a_off, H.plan.tiles[ti.out].ld, ti.m, ti.ncols, 0, ti.map, 0});
+    const int64_t row = H.plan.tiles[ti.out].row0;
+    const int32_t mem = static_cast<int32_t>(std::upper_bound(mrow.begin(), mrow.end(), row) - mrow.begin()) - 1;
+    dj.push_back(TcPack{tp.du_src[i], ti.a_off, H.plan.tiles[ti.out].ld, ti.m, ti.ncols, 0, ti.map, 0,
+                        std::max(0, std::min(mem, t.nmem - 1)), 0});
   }
   TcPack *dvj = nullptr, *ddj = nullptr;
   VGroup *dg = nullptr;
@@ -452,6 +461,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
                             int64_t ldy, void *stream) {
   if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
   HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard multiplies through hmgpu_matvec_shard only");
   if (nrhs < 0) return hm::fail(HMGPU_ERR_INVALID, "nrhs < 0");
   if (nrhs == 0) return HMGPU_OK;
   if (!x || !y) return hm::fail(HMGPU_ERR_INVALID, "x or y is NULL");
@@ -485,7 +495,8 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
       if ((rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xts), xb)) ||
           (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.prow),
                          std::max<int64_t>(H.plan.p_rows, 1) * hm::kTcMaxRhs * 4)) ||
-          (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xscale), 2 * hm::kTcMaxRhs * sizeof(float))))
+          (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xscale),
+                         2 * static_cast<size_t>(H.tc.nmem) * hm::kTcMaxRhs * sizeof(float))))
         return rc;
       cudaMemsetAsync(H.tc.xts, 0, xb, s);
       if (cudaError_t e = hm::encode_xts_map(H.tc, 32)) return hm::cuda_fail(e, "tensor map of XTS");

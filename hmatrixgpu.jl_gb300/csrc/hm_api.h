@@ -53,6 +53,13 @@ struct HMatrix {
   int64_t aca_batches = 0, aca_reruns = 0, aca_ws_bytes = 0;
   int64_t device_bytes = 0;
   std::vector<void *> dev_allocs;
+  // batches: first row and first column of every member, then m and n (empty
+  // outside batches)
+  std::vector<int64_t> member_rows, member_cols;
+  // a row shard (hmgpu_hmatrix_shard): owns permuted rows [shard_row0, shard_row1)
+  bool is_shard = false;
+  int32_t shard_rank = 0, shard_world = 1;
+  int64_t shard_row0 = 0, shard_row1 = 0;
 
   ~HMatrix();
   void release();

@@ -31,6 +31,7 @@ extern "C" int hmgpu_hmatrix_batch(hmgpu_hmatrix *const *members, int32_t count,
   for (int32_t k = 0; k < count; k++) {
     if (!members[k]) return hm::fail(HMGPU_ERR_INVALID, "member " + std::to_string(k) + " is NULL");
     M[k] = reinterpret_cast<const HMatrix *>(members[k]);
+    if (M[k]->is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard cannot be a batch member");
   }
   int dev = 0;
   cudaGetDevice(&dev);
@@ -66,6 +67,12 @@ extern "C" int hmgpu_hmatrix_batch(hmgpu_hmatrix *const *members, int32_t count,
                               panel_base, v_base)))
     return rc;
   B->multi_from = M[0]->multi_from;
+  B->member_rows.assign(1, 0);
+  B->member_cols.assign(1, 0);
+  for (int32_t k = 0; k < count; k++) {
+    B->member_rows.push_back(B->member_rows.back() + M[k]->bs.m);
+    B->member_cols.push_back(B->member_cols.back() + M[k]->bs.n);
+  }
 
   // device data: the members' panels and V rows, copied in order
   if ((rc = B->dalloc(&B->panels, P.panel_len * es))) return rc;
@@ -246,6 +253,7 @@ int time_products(hmgpu_hmatrix *h, const void *x, void *y, int64_t nrhs, int64_
 extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, int32_t *result) {
   if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
   HMatrix &H = *reinterpret_cast<HMatrix *>(h);
+  if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard multiplies through hmgpu_matvec_shard only");
   const uint64_t key = structure_hash(H);
   int32_t best[4];
   if (cache_lookup(cache_path, key, best)) {

@@ -77,6 +77,8 @@ struct TcPack {  // one item's FP32 row-major source -> canonical FP16 chunks an
   int32_t kind;  // 0: near/U rows (columns scaled through colmap[map + c]), 1: V rows
   int32_t map;   // kind 0: colmap offset of column 0
   int32_t trow;  // kind 1: XT row (rank row) of row 0; rows are consecutive
+  int32_t member;  // batch member of the rows (0 outside batches)
+  int32_t pad;
 };
 struct DevTc {
   void *adata = nullptr;  // canonical FP16 (hi, lo) chunks of every item, each with its row factors
@@ -86,7 +88,9 @@ struct DevTc {
   uint16_t *xts = nullptr;    // xt_len rows of 32 FP16 hi + 32 FP16 lo (passes of <= 32 columns)
   uint16_t *xts64 = nullptr;  // xt_len rows of 64 FP16 hi + 64 FP16 lo (passes of 33..64 columns)
   float *prow = nullptr;      // partial rows of split V items, 64 values per row
-  float *xscale = nullptr;    // per pass: max |x_r| bits (64 words), then 1 / sigma_r (64 floats)
+  float *xscale = nullptr;    // per pass: max |x_r| bits (64 words per member), then 1 / sigma (64 floats per member)
+  int64_t *mcol0 = nullptr;   // first source index of each batch member, nmem + 1 entries
+  int32_t nmem = 1;           // batch members (1 outside batches)
   int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;
   int64_t xt_rows = 0;  // rows of either XTS
   CUtensorMap xmap[2];  // tile-load maps of xts and xts64 (encode_xts_map)

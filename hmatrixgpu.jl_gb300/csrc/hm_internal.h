@@ -145,6 +145,7 @@ struct TcItem {
   int32_t row0;     // kind 0: first row of the item within its tile
 };
 static_assert(sizeof(TcItem) == 32, "TcItem layout");
+constexpr int kTcTrailer = 68 * 4;  // bytes after an item's chunks: 64 row factors, its batch member, padding
 
 // The V rows of one source group: rows [0, rows) of `stride` stored elements
 // at v_off, dotted with XT[x_off, x_off + stride), outputs at XT rows t_off...

@@ -47,6 +47,7 @@ extern "C" int hmgpu_matvec_noalloc(hmgpu_hmatrix *h, const void *x, void *y, vo
   if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
   if (!x || !y) return hm::fail(HMGPU_ERR_INVALID, "x or y is NULL");
   hm::HMatrix &H = *reinterpret_cast<hm::HMatrix *>(h);
+  if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard multiplies through hmgpu_matvec_shard only");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return hm::cuda_fail(e, "cudaGetDevice");

@@ -317,10 +317,10 @@ void make_tc_plan(const Plan &p, TcPlan &tp) {
   constexpr int32_t kTcRows = 64;  // rows per item: hi and lo stack to the 128 UMMA rows
   tp = TcPlan();
   // bytes of an item: hi and lo, ceil(m / 8) row groups x padded columns x 16 B,
-  // then the 64 FP32 row factors
+  // then the trailer (64 FP32 row factors and the item's batch member)
   auto item_bytes = [](int32_t m, int32_t ncols) {
     const int64_t npad = ncols > 0 ? round_up(ncols, 16) : 16;
-    return int64_t(32) * ((m + 7) / 8) * npad + 64 * 4;
+    return int64_t(32) * ((m + 7) / 8) * npad + kTcTrailer;
   };
   int64_t off = 0;
   for (const MVItem &it : p.mv_items) {

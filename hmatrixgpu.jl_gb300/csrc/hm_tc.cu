@@ -85,7 +85,11 @@ struct TcShape {
   static constexpr int kEpi1 = 6 + kBProducers;       // first warp of the second epilogue set
   static constexpr int kWarps = kEpi1 + 4;            // roles: see the header comment
   static constexpr int kThreads = kWarps * 32;
-  static constexpr uint32_t kTmemCols = 2 * kBN;      // two accumulators
+  // TMEM: every column of the SM's 512, cut into accumulator buffers of kBN
+  // columns, half of them for each epilogue set
+  static constexpr uint32_t kTmemCols = 512;
+  static constexpr int kBufs = static_cast<int>(kTmemCols) / kBN;  // 8 or 4
+  static constexpr int kSetBufs = kBufs / 2;
   static constexpr int kConsumers = kBProducers + 1 + 8;  // warps that read each queued item
   static constexpr uint32_t kBGroupK = (kBN / 8) * kBGroupN;
   static constexpr int kPieces = R / 4;               // 16-byte pieces of an XTS row
@@ -141,19 +145,6 @@ __device__ __forceinline__ bool elect_one() {
   return pred != 0;
 }
 
-// 32 consecutive accumulator columns of this warp's 32 TMEM lanes.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
-        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
-        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-
 // 16 consecutive accumulator columns of this warp's 32 TMEM lanes.
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
@@ -163,22 +154,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "r"(taddr));
 }
 
-// w[c] = D[.., t1 + c] + D[.., t2 + c] for c < N (N = 16 or 32): the products
-// with B_hi and with B_lo of the same right-hand sides.
-template <int N>
-__device__ __forceinline__ void tmem_sum(uint32_t t1, uint32_t t2, float (&w)[N]) {
-  uint32_t r[N], r2[N];
-  if constexpr (N == 32) {
-    tmem_ld32(t1, r);
-    tmem_ld32(t2, r2);
-  } else {
-    static_assert(N == 16, "16 or 32 columns");
-    tmem_ld16(t1, r);
-    tmem_ld16(t2, r2);
-  }
+// w[c] = D[.., t1 + c] + D[.., t2 + c] for c < 16: the products with B_hi
+// and with B_lo of the same right-hand sides.
+__device__ __forceinline__ void tmem_sum16(uint32_t t1, uint32_t t2, float (&w)[16]) {
+  uint32_t r[16], r2[16];
+  tmem_ld16(t1, r);
+  tmem_ld16(t2, r2);
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int c = 0; c < N; c++) w[c] = __uint_as_float(r[c]) + __uint_as_float(r2[c]);
+  for (int c = 0; c < 16; c++) w[c] = __uint_as_float(r[c]) + __uint_as_float(r2[c]);
 }
 
 __device__ __forceinline__ unsigned long long now_ns() {
@@ -195,15 +179,19 @@ struct TcSmem {
   // per epilogue set: halves of the row sums handed from the lo-row warps to
   // the hi-row warps (xa) and back (xb)
   float xa[2][64][R / 2 + 1], xb[2][64][R / 2 + 1];
-  uint64_t full[Sh::kStages], empty[Sh::kStages], bfull[Sh::kStages], acc_full[2], acc_empty[2];
+  uint64_t full[Sh::kStages], empty[Sh::kStages], bfull[Sh::kStages];
+  uint64_t seg_full[Sh::kBufs], seg_empty[Sh::kBufs];  // per accumulator buffer
   uint64_t xa_ready[2], xa_free[2], xb_ready[2], xb_free[2];
   uint64_t qfull[kQ], qempty[kQ];
   TcItem qdata[kQ];  // item queue: ticket order; kind -1 ends it
   uint32_t tmem;
   volatile int32_t abort;
 };
-// 1024 bytes of alignment slack on top; 232448 bytes is the per-block limit
-static_assert(sizeof(TcSmem<32>) + 1024 <= 232448 && sizeof(TcSmem<64>) + 1024 <= 232448,
+// 128 bytes of alignment slack on top (the tile loads and the no-swizzle
+// operand layouts need 128-byte alignment at most); 232448 bytes is the
+// per-block limit
+constexpr size_t kSmemAlign = 128;
+static_assert(sizeof(TcSmem<32>) + kSmemAlign <= 232448 && sizeof(TcSmem<64>) + kSmemAlign <= 232448,
               "tensor-core pass shared memory");
 
 // Waits for the phase of `bar` with parity `parity`; false when the abort flag
@@ -290,7 +278,8 @@ __device__ __forceinline__ float pow2_scale(float mx) {
   return __int_as_float((e + 127) << 23);
 }
 
-// Offset of the row factors (64 floats) that trail an item's chunks.
+// Offset of the row factors (64 floats, then the item's batch member as an
+// int32 and padding: kTrailer bytes) that trail an item's chunks.
 __device__ __host__ __forceinline__ int64_t trailer_off(int m, int ncols) {
   const int64_t npad = ncols > 0 ? (ncols + 15) & ~15 : 16;
   return int64_t(32) * ((m + 7) / 8) * npad;
@@ -320,7 +309,7 @@ struct TcArgs {
   int32_t *ticket;             // next item (zeroed by the permutation kernel)
   const int32_t *colmap;
   const uint16_t *xts;         // XTS rows (2R FP16 each)
-  const float *xs_inv;         // 1 / sigma_r per right-hand side (64)
+  const float *xs_inv;         // 1 / sigma per batch member and right-hand side (64 per member)
   uint16_t *xts_out;           // t rows (kind 1)
   float *prow;                 // P rows (kind 2)
   const TileDesc *tiles;
@@ -338,7 +327,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
   constexpr int kStages = Sh::kStages;
   extern __shared__ unsigned char smem_raw[];
   TcSmem<R> &S = *reinterpret_cast<TcSmem<R> *>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+      (reinterpret_cast<uintptr_t>(smem_raw) + kSmemAlign - 1) & ~static_cast<uintptr_t>(kSmemAlign - 1));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     S.abort = 0;
@@ -347,9 +336,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.empty[s])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.bfull[s])));
     }
-    for (int b = 0; b < 2; b++) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.acc_full[b])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(su32(&S.acc_empty[b])));
+    for (int b = 0; b < Sh::kBufs; b++) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.seg_full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(su32(&S.seg_empty[b])));
     }
     for (int q = 0; q < kQ; q++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.qfull[q])));
@@ -551,55 +540,44 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     int64_t g = 0;
     int n = 0;
     bool stop = false;
+    // Every 64-column chunk goes to a fresh accumulator buffer of the item's
+    // epilogue set (set n & 1, buffers used in turn), whose warps add the
+    // chunks' sums in FP32 registers: the tensor cores' own accumulation then
+    // spans only the 4 UMMAs of one chunk, whatever the item's length.
+    uint32_t kseg[2] = {0u, 0u};  // chunks handed to each epilogue set so far
     for (; !stop; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
-      const int ab = n & 1;
-      if (!wait_bar_warp(S, &S.acc_empty[ab], static_cast<uint32_t>((n >> 1) & 1) ^ 1u, a.status, 23)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t acc = S.tmem + ab * Sh::kBN;
-      // two chunks per turn where the item has them: one round of waits,
-      // descriptors and hand-offs per 128 columns
-      for (int c0 = 0; c0 < npad;) {
-        const int two = c0 + kKc < npad ? 2 : 1;
-        int s2[2], kc2[2];
-        bool ok = true;
-        for (int h = 0; h < two; h++) {
-          kc2[h] = min(kKc, npad - c0 - h * kKc);
-          s2[h] = static_cast<int>((g + h) % kStages);
-          ok = ok && wait_bar_warp(S, &S.full[s2[h]], static_cast<uint32_t>(((g + h) / kStages) & 1), a.status, 24);
-        }
-        if (!ok) {
+      const int e = n & 1;
+      // V pieces' B tiles come from the tile load (K groups 128 B apart, N
+      // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
+      const bool tma_b = I.kind != 0;
+      for (int c0 = 0; c0 < npad; c0 += kKc, g++, kseg[e]++) {
+        const int kc = min(kKc, npad - c0), st = static_cast<int>(g % kStages);
+        const int buf = e * Sh::kSetBufs + static_cast<int>(kseg[e] % Sh::kSetBufs);
+        if (!wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23) ||
+            !wait_bar_warp(S, &S.full[st], static_cast<uint32_t>((g / kStages) & 1), a.status, 24)) {
           stop = true;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (elect_one()) {
-          for (int h = 0; h < two; h++) {
-            const uint64_t da = sdesc(su32(S.a[s2[h]]), 128, static_cast<uint32_t>(kc2[h]) * 16);
-            // leading byte offset: K direction; stride byte offset: N direction.
-            // V pieces' B tiles come from the tile load (K groups 128 B apart,
-            // N groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B).
-            const bool tma_b = I.kind != 0;
-            const uint64_t db = tma_b ? sdesc(su32(S.b[s2[h]]), 128, 1024)
-                                      : sdesc(su32(S.b[s2[h]]), Sh::kBGroupK, kBGroupN);
-            for (int ks = 0; ks < kc2[h] / 16; ks++) {
-              // the start address field counts 16-byte units
-              const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
-                             ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
-              mma(acc, da + oa, db + ob, Sh::kIdesc, ((c0 + h * kKc) | ks) ? 1u : 0u);
-            }
-            commit(&S.empty[s2[h]]);
+          const uint32_t acc = S.tmem + static_cast<uint32_t>(buf * Sh::kBN);
+          // leading byte offset: K direction; stride byte offset: N direction
+          const uint64_t da = sdesc(su32(S.a[st]), 128, static_cast<uint32_t>(kc) * 16);
+          const uint64_t db = tma_b ? sdesc(su32(S.b[st]), 128, 1024) : sdesc(su32(S.b[st]), Sh::kBGroupK, kBGroupN);
+          for (int ks = 0; ks < kc / 16; ks++) {
+            // the start address field counts 16-byte units
+            const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
+                           ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
+            mma(acc, da + oa, db + ob, Sh::kIdesc, ks ? 1u : 0u);
           }
+          commit(&S.empty[st]);
+          commit(&S.seg_full[buf]);
         }
         __syncwarp();
-        g += two;
-        c0 += two * kKc;
       }
-      if (stop) break;
-      if (elect_one()) commit(&S.acc_full[ab]);
-      __syncwarp();
     }
     // the last stage release must land before the CTA's shared memory goes away
     if (!stop && g > 0)
@@ -617,60 +595,83 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     const int e = warp >= Sh::kEpi1 ? 1 : 0;
     const int quarter = warp & 3, row = (quarter & 1) * 32 + lane;
     const bool lo_part = quarter >= 2;
-    const int give = lo_part ? 0 : H, keep = lo_part ? H : 0;
+    const int keep = lo_part ? H : 0;
     float(*xo)[H + 1] = lo_part ? S.xa[e] : S.xb[e];  // written by this warp
     float(*xi)[H + 1] = lo_part ? S.xb[e] : S.xa[e];  // read by this warp
     uint64_t *o_ready = lo_part ? &S.xa_ready[e] : &S.xb_ready[e];
     uint64_t *o_free = lo_part ? &S.xa_free[e] : &S.xb_free[e];
     uint64_t *i_ready = lo_part ? &S.xb_ready[e] : &S.xa_ready[e];
     uint64_t *i_free = lo_part ? &S.xb_free[e] : &S.xa_free[e];
+    uint32_t kseg = 0;  // chunks of this set's items consumed so far
     for (int n = 0;; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
       if ((n & 1) != e) continue;
       const uint32_t k = static_cast<uint32_t>(n >> 1);  // this set's item count
-      if (!wait_bar_warp(S, &S.acc_full[e], k & 1u, a.status, 25)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t taddr = S.tmem + e * Sh::kBN + (static_cast<uint32_t>(quarter * 32) << 16);
-      float w[H];  // A_part B_hi + A_part B_lo over H right-hand sides
-      tmem_sum<H>(taddr + give, taddr + R + give, w);
+      const int nch = ((I.ncols > 0 ? (I.ncols + 15) & ~15 : 16) + kKc - 1) / kKc;
+      // w[c]: A_part B_hi + A_part B_lo of right-hand side c, chunk by chunk
+      float w[R];
+#pragma unroll
+      for (int c = 0; c < R; c++) w[c] = 0.0f;
+      bool ok = true;
+      for (int ch = 0; ch < nch; ch++, kseg++) {
+        const int buf = e * Sh::kSetBufs + static_cast<int>(kseg % Sh::kSetBufs);
+        if (!wait_bar_warp(S, &S.seg_full[buf], (kseg / Sh::kSetBufs) & 1u, a.status, 25)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t taddr = S.tmem + static_cast<uint32_t>(buf * Sh::kBN) + (static_cast<uint32_t>(quarter * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < R; c0 += 16) {
+          float d[16];
+          tmem_sum16(taddr + c0, taddr + R + c0, d);
+#pragma unroll
+          for (int c = 0; c < 16; c++) w[c0 + c] += d[c];
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) arrive(&S.seg_empty[buf]);
+      }
+      if (!ok) break;
+      // the hi-row warp keeps right-hand sides [0, H), the lo-row warp [H, R)
+      // (selects, not a runtime index: w stays in registers)
       if (!wait_bar_warp(S, o_free, (k & 1u) ^ 1u, a.status, 27)) break;
 #pragma unroll
-      for (int c = 0; c < H; c++) xo[row][c] = w[c];
+      for (int c = 0; c < H; c++) xo[row][c] = lo_part ? w[c] : w[H + c];
       __syncwarp();
       if (lane == 0) arrive(o_ready);
-      tmem_sum<H>(taddr + keep, taddr + R + keep, w);
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) arrive(&S.acc_empty[e]);
       if (!wait_bar_warp(S, i_ready, k & 1u, a.status, 28)) break;
+      float v[H];
 #pragma unroll
-      for (int c = 0; c < H; c++) w[c] += xi[row][c];
+      for (int c = 0; c < H; c++) v[c] = (lo_part ? w[H + c] : w[c]) + xi[row][c];
       __syncwarp();
       if (lane == 0) arrive(i_free);
       if (row >= I.m) continue;
       // the row's factor: 1 / rho_i (kind 0), or gamma_k / nu_k (V rows)
-      const float f = __ldg(reinterpret_cast<const float *>(a.adata + I.a_off + trailer_off(I.m, I.ncols)) + row);
+      const float *trailer = reinterpret_cast<const float *>(a.adata + I.a_off + trailer_off(I.m, I.ncols));
+      const float f = __ldg(trailer + row);
 #pragma unroll
-      for (int c = 0; c < H; c++) w[c] *= f;
+      for (int c = 0; c < H; c++) v[c] *= f;
       if (I.kind == 0) {
         float *yr = a.y + a.tmap0[a.tiles[I.out].row0 + I.row0 + row];
+        const float *xs = a.xs_inv + __float_as_int(__ldg(trailer + 64)) * kTcMaxRhs + keep;  // its member's
 #pragma unroll
         for (int c = 0; c < H; c++)
-          if (keep + c < a.nr) yr[(keep + c) * a.ldy] = w[c] * __ldg(a.xs_inv + keep + c);
+          if (keep + c < a.nr) yr[(keep + c) * a.ldy] = v[c] * __ldg(xs + c);
       } else if (I.kind == 1) {
         uint4 *dst = reinterpret_cast<uint4 *>(a.xts_out + static_cast<int64_t>(I.out + row) * (2 * R)) + keep / 8;
 #pragma unroll
         for (int q = 0; q < H / 8; q++) {
           uint4 hi, lo;
-          split8(w + 8 * q, hi, lo);
+          split8(v + 8 * q, hi, lo);
           dst[q] = hi;
           dst[R / 8 + q] = lo;
         }
       } else {
         float4 *dst = reinterpret_cast<float4 *>(a.prow + static_cast<int64_t>(I.out + row) * R + keep);
 #pragma unroll
-        for (int q = 0; q < H / 4; q++) dst[q] = make_float4(w[4 * q], w[4 * q + 1], w[4 * q + 2], w[4 * q + 3]);
+        for (int q = 0; q < H / 4; q++) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
       }
     }
   }
@@ -680,58 +681,96 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem), "r"(Sh::kTmemCols));
 }
 
-// max |X[., r]| per right-hand side r < nr, as FP32 bits (non-negative
-// floats order as unsigned integers) into xmax[r], which starts at zero.
-__global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, int64_t n_src,
-                            unsigned *__restrict__ xmax) {
-  __shared__ unsigned smax[kTcMaxRhs];
-  for (int r = threadIdx.x; r < kTcMaxRhs; r += blockDim.x) smax[r] = 0u;
-  __syncthreads();
-  for (int r = 0; r < nr; r++) {
-    unsigned m = 0u;
-    for (int64_t j = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; j < n_src;
-         j += static_cast<int64_t>(gridDim.x) * blockDim.x)
-      m = max(m, __float_as_uint(fabsf(X[j + r * ldx])));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(&smax[r], m);
+// Batch member of source index j: the largest k with col0[k] <= j.
+__device__ __forceinline__ int member_of(const int64_t *col0, int nmem, int64_t j) {
+  int lo = 0, hi = nmem - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (col0[mid] <= j)
+      lo = mid;
+    else
+      hi = mid - 1;
   }
-  __syncthreads();
-  for (int r = threadIdx.x; r < nr; r += blockDim.x) atomicMax(&xmax[r], smax[r]);
+  return lo;
 }
 
-// sigma_r = pow2_scale(max |x_r|) for r < R (1 beyond nr); block 0 also
-// stores 1 / sigma_r for the epilogue.
-template <int R>
-__device__ __forceinline__ void load_sigma(const unsigned *xmax, int nr, float *sg, float *xs_inv) {
-  for (int r = threadIdx.x; r < R; r += blockDim.x) {
-    const float s = r < nr ? pow2_scale(__uint_as_float(xmax[r])) : 1.0f;
-    sg[r] = s;
-    if (blockIdx.x == 0) xs_inv[r] = 1.0f / s;
-  }
+// max |X[., r]| per batch member and right-hand side r < nr, as FP32 bits
+// (non-negative floats order as unsigned integers) into xmax[member * 64 + r],
+// which starts at zero. Members own the contiguous source ranges [col0[k],
+// col0[k + 1]); each block takes a contiguous range of source indices and
+// keeps the maxima of its current member in shared memory.
+__global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, int64_t n_src,
+                            const int64_t *__restrict__ col0, int nmem, unsigned *__restrict__ xmax) {
+  __shared__ unsigned smax[kTcMaxRhs];
+  __shared__ int cur, mlo, mhi;
+  const int64_t per = (n_src + gridDim.x - 1) / gridDim.x;
+  const int64_t jb = blockIdx.x * per, je = min(n_src, jb + per);
+  for (int r = threadIdx.x; r < kTcMaxRhs; r += blockDim.x) smax[r] = 0u;
+  if (threadIdx.x == 0) cur = -1;
   __syncthreads();
+  for (int64_t j0 = jb; j0 < je; j0 += blockDim.x) {
+    if (threadIdx.x == 0) {
+      mlo = member_of(col0, nmem, j0);
+      mhi = member_of(col0, nmem, min(je, j0 + static_cast<int64_t>(blockDim.x)) - 1);
+    }
+    __syncthreads();
+    if (mlo != cur) {  // the block's range enters another member: flush, restart
+      if (cur >= 0)
+        for (int r = threadIdx.x; r < nr; r += blockDim.x) atomicMax(&xmax[cur * kTcMaxRhs + r], smax[r]);
+      __syncthreads();
+      for (int r = threadIdx.x; r < kTcMaxRhs; r += blockDim.x) smax[r] = 0u;
+      if (threadIdx.x == 0) cur = mlo;
+      __syncthreads();
+    }
+    const int64_t j = j0 + threadIdx.x;
+    if (mlo == mhi) {
+      for (int r = 0; r < nr; r++) {
+        unsigned m = j < je ? __float_as_uint(fabsf(X[j + r * ldx])) : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(&smax[r], m);
+      }
+    } else if (j < je) {  // a member boundary inside this step: straight to global
+      const int mj = member_of(col0, nmem, j);
+      for (int r = 0; r < nr; r++) atomicMax(&xmax[mj * kTcMaxRhs + r], __float_as_uint(fabsf(X[j + r * ldx])));
+    }
+    __syncthreads();
+  }
+  if (cur >= 0)
+    for (int r = threadIdx.x; r < nr; r += blockDim.x) atomicMax(&xmax[cur * kTcMaxRhs + r], smax[r]);
 }
 
 // XTS x rows from X in its own order: the R right-hand sides X[j + r ldx]
-// (0 for r >= nr) of source index j, times sigma_r, split into FP16 hi
-// (first 2R bytes) and lo (last 2R bytes), go to row sinv[j]. Reads of X are
-// coalesced along j and every row is written whole; x-region rows that no
-// source index maps to stay zero from the allocation. Also re-arms the two
-// item tickets.
+// (0 for r >= nr) of source index j, times sigma of (j's batch member, r),
+// split into FP16 hi (first 2R bytes) and lo (last 2R bytes), go to row
+// sinv[j]. Reads of X are coalesced along j and every row is written whole;
+// x-region rows that no source index maps to stay zero from the allocation.
+// Block 0 also stores 1 / sigma per member and right-hand side for the
+// epilogue, and re-arms the two item tickets.
 template <int R>
 __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, int nr,
                                      const int32_t *__restrict__ sinv0, int64_t n_src,
                                      uint16_t *__restrict__ xts, int32_t *__restrict__ tickets,
+                                     const int64_t *__restrict__ col0, int nmem,
                                      const unsigned *__restrict__ xmax, float *__restrict__ xs_inv) {
   __shared__ float tile[64][R + 1];
-  __shared__ float sg[R];
-  if (blockIdx.x == 0 && threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
-  load_sigma<R>(xmax, nr, sg, xs_inv);
+  __shared__ int mem[64];
+  if (blockIdx.x == 0) {
+    if (threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
+    for (int e = threadIdx.x; e < nmem * R; e += blockDim.x) {
+      const int k = e / R, r = e % R;
+      xs_inv[k * kTcMaxRhs + r] = r < nr ? 1.0f / pow2_scale(__uint_as_float(xmax[k * kTcMaxRhs + r])) : 1.0f;
+    }
+  }
   for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
+    if (threadIdx.x < 64) mem[threadIdx.x] = member_of(col0, nmem, min(j0 + threadIdx.x, n_src - 1));
+    __syncthreads();
     for (int e = threadIdx.x; e < 64 * R; e += blockDim.x) {
       const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
       const int64_t j = j0 + jj;
-      tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] * sg[r] : 0.0f;
+      tile[jj][r] = (j < n_src && r < nr)
+                        ? X[j + r * ldx] * pow2_scale(__uint_as_float(xmax[mem[jj] * kTcMaxRhs + r]))
+                        : 0.0f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * (R / 8); e += blockDim.x) {
@@ -879,14 +918,14 @@ __global__ void pack_tc_kernel(const TcPack *__restrict__ jobs, const float *__r
     base += 2 * half;
   }
   float *tr = reinterpret_cast<float *>(adata + J.a_off + trailer_off(J.m, J.ncols));
-  for (int r = threadIdx.x; r < 64; r += blockDim.x) tr[r] = fac[r];
+  for (int r = threadIdx.x; r < 68; r += blockDim.x) tr[r] = r < 64 ? fac[r] : __int_as_float(r == 64 ? J.member : 0);
 }
 
 }  // namespace
 
 template <int R>
 static size_t smem_bytes() {
-  return sizeof(TcSmem<R>) + 1024;
+  return sizeof(TcSmem<R>) + kSmemAlign;
 }
 size_t tc_smem_bytes(int nr) { return nr > 32 ? smem_bytes<64>() : smem_bytes<32>(); }
 
@@ -933,10 +972,11 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   if (gp > 2048) gp = 2048;
   if (ev) cudaEventRecord(ev[0], s);
   unsigned *xmax = reinterpret_cast<unsigned *>(t.xscale);
-  float *xs_inv = t.xscale + kTcMaxRhs;
-  cudaMemsetAsync(xmax, 0, kTcMaxRhs * sizeof(unsigned), s);
-  xmax_kernel<<<gp < 512 ? gp : 512, 256, 0, s>>>(X, ldx, nr, p.n_src, xmax);
-  permute_split_kernel<R><<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xts, p.counter + 2, xmax, xs_inv);
+  float *xs_inv = t.xscale + static_cast<int64_t>(t.nmem) * kTcMaxRhs;
+  cudaMemsetAsync(xmax, 0, static_cast<size_t>(t.nmem) * kTcMaxRhs * sizeof(unsigned), s);
+  xmax_kernel<<<gp < 512 ? gp : 512, 256, 0, s>>>(X, ldx, nr, p.n_src, t.mcol0, t.nmem, xmax);
+  permute_split_kernel<R><<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xts, p.counter + 2, t.mcol0, t.nmem,
+                                              xmax, xs_inv);
   nl += 2;
   if (ev) cudaEventRecord(ev[1], s);
   TcArgs a{};
@@ -999,7 +1039,8 @@ cudaError_t launch_pack_tc(const TcPack *jobs, int64_t njobs, const float *src, 
 
 cudaError_t launch_matvec_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx, int nr,
                              float *Y, int64_t ldy, cudaStream_t s, cudaEvent_t *ev, int *launches) {
-  if (nr < 1 || nr > 64 || (nr > 32 && !t.xts64) || !t.xts || !t.xscale) return cudaErrorInvalidValue;
+  if (nr < 1 || nr > 64 || (nr > 32 && !t.xts64) || !t.xts || !t.xscale || !t.mcol0 || t.nmem < 1)
+    return cudaErrorInvalidValue;
   tc_attrs();
   const int nl = nr > 32 ? run_tc<64>(p, t, X, ldx, nr, Y, ldy, s, ev) : run_tc<32>(p, t, X, ldx, nr, Y, ldy, s, ev);
   if (launches) *launches = nl;

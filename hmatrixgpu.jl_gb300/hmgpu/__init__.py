@@ -465,6 +465,13 @@ class HMatrix:
             check(rc)
         return st.value
 
+    def shard(self, rank, world):
+        """Row shard `rank` of `world` (hmgpu_hmatrix_shard): the H-matrix's
+        contiguous range of permuted rows, for products split over GPUs."""
+        h = C.c_void_p()
+        check(lib().hmgpu_hmatrix_shard(self._h, int(rank), int(world), C.byref(h)))
+        return Shard(h, self.shape, self.dtype)
+
     # ---- products ------------------------------------------------------------------
     def mul(self, y, x, stream=None):
         """mul!(y, H, x): y and x are torch CUDA tensors (stream-ordered on the
@@ -496,6 +503,45 @@ class HMatrix:
 
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
+
+
+class Shard:
+    """Rows [row_begin, row_end) of an H-matrix in the permuted target order
+    (hmgpu_hmatrix_shard). Each owned row of its product is bitwise the row
+    the whole H-matrix computes; it reads x in the permuted source order."""
+
+    def __init__(self, handle, shape, dtype):
+        self._h = handle
+        self.shape = shape
+        self.dtype = dtype
+        b, e = C.c_int64(), C.c_int64()
+        check(lib().hmgpu_shard_rows(self._h, C.byref(b), C.byref(e)))
+        self.rows = (b.value, e.value)
+
+    def mul_permuted(self, y_rows, x_perm, stream=None):
+        """y_rows[i] = (H x)[target_map[row_begin + i] - 1] for the owned rows,
+        from x_perm (all n entries, permuted source order). CUDA tensors of
+        the H-matrix's dtype, stream-ordered."""
+        import torch
+        want = torch.float64 if self.dtype == np.float64 else torch.float32
+        if x_perm.dtype != want or y_rows.dtype != want or not (x_perm.is_cuda and y_rows.is_cuda):
+            raise TypeError(f"x and y must be CUDA {want} tensors")
+        if x_perm.numel() != self.shape[1] or y_rows.numel() != self.rows[1] - self.rows[0]:
+            raise ValueError("dimension mismatch")
+        if not (x_perm.is_contiguous() and y_rows.is_contiguous()):
+            raise ValueError("x and y must be contiguous")
+        if stream is None:
+            stream = torch.cuda.current_stream(x_perm.device).cuda_stream
+        with torch.cuda.device(x_perm.device):
+            check(lib().hmgpu_matvec_shard(self._h, C.c_void_p(x_perm.data_ptr()), C.c_void_p(y_rows.data_ptr()),
+                                           C.c_void_p(stream)))
+        return y_rows
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().hmgpu_hmatrix_free(h)
+            self._h = None
 
 
 def sparsify_hmatrix(K, X, Y, eta=1.5, triplets=False):

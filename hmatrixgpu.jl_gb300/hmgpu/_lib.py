@@ -74,6 +74,9 @@ SIGNATURES = {
     "hmgpu_matvec": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64, VP]),
     "hmgpu_matvec_host": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64]),
     "hmgpu_matvec_noalloc": (C.c_int, [VP, VP, VP, VP]),
+    "hmgpu_hmatrix_shard": (C.c_int, [VP, C.c_int32, C.c_int32, C.POINTER(VP)]),
+    "hmgpu_shard_rows": (C.c_int, [VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "hmgpu_matvec_shard": (C.c_int, [VP, VP, VP, VP]),
     "hmgpu_hmatrix_info": (C.c_int, [VP, C.POINTER(Info)]),
     "hmgpu_hmatrix_build_profile": (C.c_int, [VP, C.POINTER(C.c_double), C.c_int32]),
     "hmgpu_hmatrix_status": (C.c_int, [VP, C.POINTER(C.c_int)]),

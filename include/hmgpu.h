@@ -45,7 +45,9 @@ extern "C" {
 #define HMGPU_F32 1   /* all factors FP32, FP32 arithmetic; x, y are float         */
 #define HMGPU_MIXED 2 /* FP32 factors with compensated FP32 accumulation for
                          few right-hand sides; for more, a copy of every block
-                         as BF16 pairs hi + lo (hi = bf16(a), lo = bf16(a - hi))
+                         as FP16 pairs hi + lo (hi = fp16(s a), lo = fp16(s a -
+                         hi), 22 significant bits) under power-of-two scales s
+                         per panel row, per rank row and per right-hand side,
                          multiplied on the tensor cores with FP32 accumulation,
                          one pass per 64 right-hand sides (the threshold is
                          hmgpu_hmatrix_autotune's); x, y are float             */
@@ -296,6 +298,27 @@ int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const double *U, const
  * memory, V in host or device memory). */
 int hmgpu_sparsify(const hmgpu_kernel *K, const hmgpu_tree *X, const hmgpu_tree *Y, double eta,
                    int64_t *I, int64_t *J, double *V, int64_t *nnz);
+
+/* ---- row shards for products over several GPUs --------------------------- */
+/* Row ownership follows the reference's product, which writes every row of the
+ * permuted output exactly once (DU_mult_vec_kernel!, src/mult.jl:80-146; the
+ * store at :144), so the rows split over GPUs with no reduction.
+ * hmgpu_hmatrix_shard gives shard `rank` of `world`: a handle on the current
+ * device (H's) holding a contiguous range of H's row tiles, balanced by stored
+ * entries, and the V rows of every source group those tiles read. Its rows are
+ * the permuted rows [row_begin, row_end) of hmgpu_shard_rows (0-based; the
+ * shards of one H cover 0..m once, in rank order). H may be freed afterwards.
+ * hmgpu_matvec_shard computes those rows of y = H x for one right-hand side:
+ * x_perm holds all n entries of x in the permuted source order (x_perm[j] =
+ * x[source_map[j] - 1]; the caller gathers it from the ranks first), y_rows
+ * receives row_end - row_begin values, y_rows[i] = (H x)[target_map[row_begin
+ * + i] - 1]. Device pointers of the mode's element type; stream-ordered. Each
+ * owned row is bitwise the row hmgpu_matvec computes on H. A shard serves only
+ * this entry point (the other product, batch, autotune and save calls refuse
+ * it). */
+int hmgpu_hmatrix_shard(const hmgpu_hmatrix *H, int32_t rank, int32_t world, hmgpu_hmatrix **out);
+int hmgpu_shard_rows(const hmgpu_hmatrix *S, int64_t *row_begin, int64_t *row_end);
+int hmgpu_matvec_shard(hmgpu_hmatrix *S, const void *x_perm, void *y_rows, void *stream);
 
 /* ---- batches, CUDA graphs, autotuning (no counterpart in the reference) -- */
 /* One H-matrix made of `count` members: the block-diagonal operator
