@@ -65,6 +65,13 @@ namespace {
 constexpr int kKc = 64;                // columns per chunk
 constexpr int kABytes = 128 * kKc * 2;  // A tile: 64 hi rows, then 64 lo rows: 16 KB
 constexpr int kQ = 16;                  // item queue slots
+#ifndef HM_TC_SEG_CHUNKS
+#define HM_TC_SEG_CHUNKS 1
+#endif
+// chunks per accumulator buffer: the tensor cores' own accumulation spans at
+// most this many chunks (4 UMMAs each) before the epilogue takes the partial
+// sums into FP32 registers
+constexpr int kSegChunks = HM_TC_SEG_CHUNKS;
 
 // MN-major B: the hi and lo halves of the R right-hand sides are stacked along
 // N, so one XTS row (4R bytes) is one K row of B. Core matrices of 8 N values
@@ -540,11 +547,12 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     int64_t g = 0;
     int n = 0;
     bool stop = false;
-    // Every 64-column chunk goes to a fresh accumulator buffer of the item's
-    // epilogue set (set n & 1, buffers used in turn), whose warps add the
-    // chunks' sums in FP32 registers: the tensor cores' own accumulation then
-    // spans only the 4 UMMAs of one chunk, whatever the item's length.
-    uint32_t kseg[2] = {0u, 0u};  // chunks handed to each epilogue set so far
+    // Every kSegChunks chunks of an item go to a fresh accumulator buffer of
+    // the item's epilogue set (set n & 1, buffers used in turn), whose warps
+    // add the buffers' sums in FP32 registers: the tensor cores' own
+    // accumulation then spans at most 4 kSegChunks UMMAs, whatever the item's
+    // length.
+    uint32_t kseg[2] = {0u, 0u};  // buffers handed to each epilogue set so far
     for (; !stop; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
@@ -553,10 +561,12 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       // V pieces' B tiles come from the tile load (K groups 128 B apart, N
       // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
       const bool tma_b = I.kind != 0;
-      for (int c0 = 0; c0 < npad; c0 += kKc, g++, kseg[e]++) {
+      for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         const int kc = min(kKc, npad - c0), st = static_cast<int>(g % kStages);
+        const int ci = c0 / kKc;  // chunk of the item
+        const bool first = ci % kSegChunks == 0, last = ci % kSegChunks == kSegChunks - 1 || c0 + kKc >= npad;
         const int buf = e * Sh::kSetBufs + static_cast<int>(kseg[e] % Sh::kSetBufs);
-        if (!wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23) ||
+        if ((first && !wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23)) ||
             !wait_bar_warp(S, &S.full[st], static_cast<uint32_t>((g / kStages) & 1), a.status, 24)) {
           stop = true;
           break;
@@ -571,12 +581,13 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
             // the start address field counts 16-byte units
             const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
                            ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
-            mma(acc, da + oa, db + ob, Sh::kIdesc, ks ? 1u : 0u);
+            mma(acc, da + oa, db + ob, Sh::kIdesc, (first && ks == 0) ? 0u : 1u);
           }
           commit(&S.empty[st]);
-          commit(&S.seg_full[buf]);
+          if (last) commit(&S.seg_full[buf]);
         }
         __syncwarp();
+        if (last) kseg[e]++;
       }
     }
     // the last stage release must land before the CTA's shared memory goes away
@@ -602,19 +613,20 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     uint64_t *o_free = lo_part ? &S.xa_free[e] : &S.xb_free[e];
     uint64_t *i_ready = lo_part ? &S.xb_ready[e] : &S.xa_ready[e];
     uint64_t *i_free = lo_part ? &S.xb_free[e] : &S.xa_free[e];
-    uint32_t kseg = 0;  // chunks of this set's items consumed so far
+    uint32_t kseg = 0;  // accumulator buffers of this set consumed so far
     for (int n = 0;; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
       if ((n & 1) != e) continue;
       const uint32_t k = static_cast<uint32_t>(n >> 1);  // this set's item count
       const int nch = ((I.ncols > 0 ? (I.ncols + 15) & ~15 : 16) + kKc - 1) / kKc;
+      const int nbuf = (nch + kSegChunks - 1) / kSegChunks;  // accumulator buffers of the item
       // w[c]: A_part B_hi + A_part B_lo of right-hand side c, chunk by chunk
       float w[R];
 #pragma unroll
       for (int c = 0; c < R; c++) w[c] = 0.0f;
       bool ok = true;
-      for (int ch = 0; ch < nch; ch++, kseg++) {
+      for (int ch = 0; ch < nbuf; ch++, kseg++) {
         const int buf = e * Sh::kSetBufs + static_cast<int>(kseg % Sh::kSetBufs);
         if (!wait_bar_warp(S, &S.seg_full[buf], (kseg / Sh::kSetBufs) & 1u, a.status, 25)) {
           ok = false;
