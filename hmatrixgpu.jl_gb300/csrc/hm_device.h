@@ -93,7 +93,7 @@ struct DevTc {
   int32_t nmem = 1;           // batch members (1 outside batches)
   int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;
   int64_t xt_rows = 0;  // rows of either XTS
-  CUtensorMap xmap[2];  // tile-load maps of xts and xts64 (encode_xts_map)
+  CUtensorMap xmap[4];  // tile-load maps of xts and xts64: 64-row boxes, then 8-row boxes (encode_xts_map)
 };
 constexpr int kTcMaxRhs = 64;  // right-hand sides of the widest pass
 size_t tc_smem_bytes(int nr);

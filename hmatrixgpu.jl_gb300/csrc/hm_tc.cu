@@ -31,24 +31,28 @@
 //               rows to tile rows 0..63, lo rows to tile rows 64..127), and
 //               the XTS rows of its columns (whole rows) as an N-major
 //               (MN-major) FP16 tile: for a V piece, whose columns are
-//               consecutive rows, one TMA tile load on the same barrier (in a
-//               last chunk with padding columns, on the warp's own barrier,
-//               after which the warp zeroes the padding rows and publishes);
-//               for a row tile, 16-byte cp.async gathers (padding columns
-//               read the zero row), then a wait, a proxy fence and an
-//               mbarrier arrive;
+//               consecutive rows, one TMA tile load of 64 rows on the same
+//               barrier; for a row tile, one 8-row TMA tile load per K group
+//               of 8 columns that are 8 consecutive rows (the runs of whole
+//               source clusters and rank ranges), 16-byte cp.async gathers
+//               for the other groups (padding columns read the zero row),
+//               then a wait, a proxy fence and an mbarrier arrive;
 //   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
 //               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 2R (hi and lo
 //               stacked along both M and N; items have at most 64 rows), into
-//               one of two TMEM accumulators (FP32); commits free the stage
-//               and, at the end of an item, hand the accumulator on;
+//               a fresh TMEM accumulator buffer (FP32) every kSegChunks
+//               chunks; commits free the stage and hand each buffer to the
+//               item's epilogue set. In a V piece's last chunk it first zeroes
+//               the B rows of padding columns (other blocks' XTS rows, which
+//               the 64-row tile load brought in: 0 * Inf must not reach a sum);
 //   epilogue    two sets of 4 warps (warps 4-7 and the last four), set e for
-//               accumulator e, that is every other item: tcgen05.ld of the
-//               warp's 32 TMEM lanes, the sum of the four hi/lo quadrants
-//               (the hi-row and lo-row warps of the same rows swap halves of
-//               their sums, so each finishes half of the right-hand sides),
-//               the scales undone, then y rows, t rows of XTS (split again)
-//               or partial rows P.
+//               every other item: per accumulator buffer, tcgen05.ld of the
+//               warp's 32 TMEM lanes added to FP32 registers; at the item's
+//               end the sum of the four hi/lo quadrants (the hi-row and
+//               lo-row warps of the same rows swap halves of their sums, so
+//               each finishes half of the right-hand sides), the scales
+//               undone, then y rows, t rows of XTS (split again) or partial
+//               rows P.
 // Every wait is bounded by the global timer; one that runs out records a code
 // in `status`, raises a CTA-wide abort flag and every role leaves its loop.
 #include <cuda.h>
@@ -186,7 +190,7 @@ struct TcSmem {
   // per epilogue set: halves of the row sums handed from the lo-row warps to
   // the hi-row warps (xa) and back (xb)
   float xa[2][64][R / 2 + 1], xb[2][64][R / 2 + 1];
-  uint64_t full[Sh::kStages], empty[Sh::kStages], bfull[Sh::kStages];
+  uint64_t full[Sh::kStages], empty[Sh::kStages];
   uint64_t seg_full[Sh::kBufs], seg_empty[Sh::kBufs];  // per accumulator buffer
   uint64_t xa_ready[2], xa_free[2], xb_ready[2], xb_free[2];
   uint64_t qfull[kQ], qempty[kQ];
@@ -308,7 +312,8 @@ __global__ void wait_selftest_kernel(unsigned long long limit_ns, int32_t *statu
 }
 
 struct TcArgs {
-  CUtensorMap xmap;            // XTS as 8 FP16 x rows x N groups: the B tiles of V pieces
+  CUtensorMap xmap;            // XTS as 8 FP16 x rows x N groups, 64-row boxes: the B tiles of V pieces
+  CUtensorMap xmap8;           // the same view, 8-row boxes: K groups of near/U B tiles
   const unsigned char *adata;  // tensor-core panels
   const TcItem *items;
   int32_t nitems;
@@ -341,7 +346,6 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     for (int s = 0; s < kStages; s++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.full[s])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.empty[s])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.bfull[s])));
     }
     for (int b = 0; b < Sh::kBufs; b++) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(&S.seg_full[b])));
@@ -416,8 +420,6 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // proxy and publishes the stage.
     const int bw = warp == 1 ? 0 : warp == 3 ? 1 : warp - 6;  // 0..kStages-1
     int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
-    uint32_t tails = 0;          // tile loads completed on this warp's bfull barrier
-    bool tail_pending = false;   // a tile load on bfull not yet seen complete
     bool stop = false;
     const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
     for (int n = 0; !stop; n++) {
@@ -427,20 +429,35 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         if (g % kStages != bw) continue;
         const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
-        // B of a V piece by one tile load of 64 XTS rows. In a last chunk
-        // whose columns [ncols, kc) are padding, those rows belong to other
-        // blocks (or are t rows being rewritten) and must not reach the MMA
-        // (0 * Inf or 0 * NaN): the load completes on the warp's own bfull
-        // barrier, the warp zeroes the padding rows and only then publishes
-        // the stage.
+        // B of a V piece by one tile load of 64 XTS rows (in a last chunk the
+        // MMA warp zeroes the rows of padding columns before it multiplies)
         const bool tma_b = I.kind != 0;
-        const bool pad = tma_b && I.ncols - c0 < kc;
         int rows[kKc / 32];  // XTS rows of columns c0 + lane + 32 h
 #pragma unroll
         for (int h = 0; h < kKc / 32; h++) {
           const int c = c0 + lane + 32 * h;
           rows[h] = a.zero_row;
           if (c < I.ncols) rows[h] = I.kind == 0 ? __ldg(a.colmap + I.map + c) : I.map + c;
+        }
+        // near/U tiles: a K group of 8 columns that are 8 consecutive XTS rows
+        // (most are: a tile's columns come in runs of whole source clusters
+        // and rank ranges) arrives by one 8-row tile load straight into its
+        // place in the B tile; the other groups are gathered row by row
+        uint32_t gmask = 0;  // bit q: K group q by tile load
+        int grow[kKc / 8];   // first XTS row of each K group
+        if (!tma_b) {
+#pragma unroll
+          for (int h = 0; h < kKc / 32; h++) {
+            const int prev = __shfl_up_sync(0xffffffffu, rows[h], 1);
+            const bool ok = c0 + lane + 32 * h < I.ncols && ((lane & 7) == 0 || rows[h] == prev + 1);
+            const uint32_t b = __ballot_sync(0xffffffffu, ok);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              if (((b >> (8 * j)) & 0xffu) == 0xffu) gmask |= 1u << (4 * h + j);
+              grow[4 * h + j] = __shfl_sync(0xffffffffu, rows[h], 8 * j);
+            }
+          }
+          gmask &= (1u << (kc / 8)) - 1u;
         }
         if (!wait_bar_warp(S, &S.empty[s], static_cast<uint32_t>((g / kStages) & 1) ^ 1u, a.status, 22)) {
           stop = true;
@@ -457,7 +474,8 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           const unsigned char *src = a.adata + I.a_off + static_cast<int64_t>(c0 / kKc) * 2 * chunk_bytes(G, kKc);
           const uint32_t hi = su32(S.a[s]), lo = hi + 128u * kc;
           const uint32_t bar = su32(&S.full[s]);
-          const uint32_t btx = tma_b && !pad ? static_cast<uint32_t>(Sh::kBBytes) : 0u;
+          const uint32_t btx = tma_b ? static_cast<uint32_t>(Sh::kBBytes)
+                                     : static_cast<uint32_t>(__popc(gmask)) * Sh::kBGroupK;
           asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2 * half + btx)
                        : "memory");
           asm volatile(
@@ -472,51 +490,34 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
             // B of a V piece: its columns are the consecutive XTS rows map + c0
             // .., so one tile load of 64 rows lands them in the canonical
             // MN-major layout (K groups 128 B apart, N groups 1024 B apart)
-            const uint32_t bb = pad ? su32(&S.bfull[s]) : bar;
-            if (pad)
-              asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb),
-                           "r"(static_cast<uint32_t>(Sh::kBBytes))
-                           : "memory");
             asm volatile(
                 "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
                 "%4}], [%5];" ::"r"(su32(S.b[s])),
-                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bb)
+                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bar)
                 : "memory");
-            if (!pad) arrive(&S.full[s]);
+            arrive(&S.full[s]);
           }
         }
         last_g = g;
-        if (tma_b && !pad) {  // the copies complete on the stage's barrier
+        if (tma_b) {  // the copies complete on the stage's barrier
           __syncwarp();
           continue;
         }
-        if (pad) {
-          tail_pending = true;
-          if (!wait_bar_warp(S, &S.bfull[s], tails & 1u, a.status, 32)) {
-            stop = true;
-            break;
-          }
-          tail_pending = false;
-          tails++;
-          // rows [valid, kc) of every N group (16 bytes per row and group) to zero
-          const int valid = I.ncols - c0, nz = kc - valid;
-          for (int e = lane; e < nz * (Sh::kBN / 8); e += 32) {
-            const int k = valid + e % nz, gq = e / nz;
-            asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(su32(S.b[s]) + gq * 1024u + k * 16u),
-                         "r"(0u)
-                         : "memory");
-          }
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncwarp();
-          if (lane == 0) arrive(&S.full[s]);
-          continue;
-        }
+        __syncwarp();  // the stage's expected bytes are set before any tile load lands
+#pragma unroll
+        for (int q = 0; q < kKc / 8; q++)
+          if (lane == q && ((gmask >> q) & 1u))
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(su32(S.b[s]) + static_cast<uint32_t>(q) * Sh::kBGroupK),
+                "l"(reinterpret_cast<uint64_t>(&a.xmap8)), "r"(0), "r"(grow[q]), "r"(0), "r"(su32(&S.full[s]))
+                : "memory");
         const uint32_t dst0 = su32(S.b[s]) + piece * kBGroupN;
 #pragma unroll
         for (int i = 0; i < kKc / Sh::kRowsPerCopy; i++) {
           const int k = Sh::kRowsPerCopy * i + sub;
           const int r = __shfl_sync(0xffffffffu, rows[(i * Sh::kRowsPerCopy) >> 5], k & 31);
-          if (k < kc) {
+          if (k < kc && !((gmask >> (k >> 3)) & 1u)) {
             const uint16_t *src = a.xts + static_cast<int64_t>(r) * (2 * R) + piece * 8;
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst0 + (k >> 3) * Sh::kBGroupK + (k & 7) * 16),
                          "l"(src)
@@ -534,8 +535,6 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // aborted or not (one stage per producer: earlier chunks have landed).
     if (last_g >= 0 && lane == 0) {
       volatile int32_t none = 0;
-      if (tail_pending)  // a tile load on bfull that the abort left unwaited
-        wait_bar_bounded(&S.bfull[bw], tails & 1u, &none, a.status, 33, kWaitNs);
       wait_bar_bounded(&S.full[last_g % kStages], static_cast<uint32_t>((last_g / kStages) & 1), &none, a.status, 31,
                        kWaitNs);
     }
@@ -570,6 +569,22 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
             !wait_bar_warp(S, &S.full[st], static_cast<uint32_t>((g / kStages) & 1), a.status, 24)) {
           stop = true;
           break;
+        }
+        if (tma_b && I.ncols - c0 < kc) {
+          // the last chunk of a V piece: the tile load brought 64 consecutive
+          // XTS rows, and those of the padding columns [ncols, kc) belong to
+          // other blocks (or are t rows being rewritten). The A tile is zero
+          // there, but 0 * Inf and 0 * NaN are not, so the rows are zeroed
+          // (16 bytes per row and N group) before the UMMAs read them.
+          const int valid = I.ncols - c0, nz = kc - valid;
+          for (int z = lane; z < nz * (Sh::kBN / 8); z += 32) {
+            const int k = valid + z % nz, gq = z / nz;
+            asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(su32(S.b[st]) + gq * 1024u + k * 16u),
+                         "r"(0u)
+                         : "memory");
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (elect_one()) {
@@ -961,17 +976,20 @@ cudaError_t encode_xts_map(DevTc &t, int R) {
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
   }();
   uint16_t *xts = R == 64 ? t.xts64 : t.xts;
-  if (!enc || !xts || t.xt_rows < 1 || (R != 32 && R != 64)) return cudaErrorInvalidValue;
+  if (!enc || !xts || t.xt_rows < 8 || (R != 32 && R != 64)) return cudaErrorInvalidValue;
   // element (e, row, g) = XTS[row][8 g + e]: a box of 8 x 64 x 2R/8 lands as
   // 2R/8 N groups of 64 rows x 16 bytes
   cuuint64_t dims[3] = {8, static_cast<cuuint64_t>(t.xt_rows), static_cast<cuuint64_t>(2 * R / 8)};
   cuuint64_t strides[2] = {static_cast<cuuint64_t>(4 * R), 16};
-  cuuint32_t box[3] = {8, 64, static_cast<cuuint32_t>(2 * R / 8)};
-  cuuint32_t es[3] = {1, 1, 1};
-  const CUresult r = enc(&t.xmap[R / 64], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, xts, dims, strides, box, es,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+  for (int b = 0; b < 2; b++) {  // boxes of 64 rows (V pieces) and of 8 rows (K groups of near/U tiles)
+    cuuint32_t box[3] = {8, b == 0 ? 64u : 8u, static_cast<cuuint32_t>(2 * R / 8)};
+    cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = enc(&t.xmap[2 * b + R / 64], CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, xts, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
 }
 
 template <int R>
@@ -993,6 +1011,7 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   if (ev) cudaEventRecord(ev[1], s);
   TcArgs a{};
   a.xmap = t.xmap[R / 64];
+  a.xmap8 = t.xmap[2 + R / 64];
   a.adata = static_cast<const unsigned char *>(t.adata);
   a.colmap = t.colmap;
   a.xts = xts;
