@@ -135,6 +135,7 @@ def batch_measurement(dev, steps):
         members.append(hmgpu.HMatrix(hmgpu.Kernel("yukawa", P), T, T, eta=1.5, eps=1e-5, precision="f32"))
     B = hmgpu.batch(members)
     build = time.time() - t0
+    tune = B.autotune()  # the batch's own unit sizes and V schedule
     m, n = B.shape
     x = torch.randn(n, device=dev, generator=torch.Generator(dev).manual_seed(5))
     y = torch.empty(m, device=dev)
@@ -162,6 +163,16 @@ def batch_measurement(dev, steps):
     same = bool(torch.equal(y, y_each))
     G = hmgpu.Graph(B, x, y)
     t_graph = timed(lambda: G.launch(), reps)
+    import ctypes as C
+    L = hmgpu._lib.lib()
+    hmgpu.check(L.hmgpu_hmatrix_set_profiling(B._h, 1))
+    for _ in range(reps):
+        hmgpu.mul_(y, B, x)
+    ph = np.zeros(3)
+    nl, npd = C.c_int64(), C.c_int64()
+    hmgpu.check(L.hmgpu_hmatrix_phase_times(B._h, hmgpu.ptr(ph), C.byref(nl), C.byref(npd)))
+    hmgpu.check(L.hmgpu_hmatrix_set_profiling(B._h, 0))
+    ph = ph / max(npd.value, 1)
     inf = B.info()
     byts = 4 * (inf["dense_entries"] + inf["far_entries"]) + 4 * (2 * n + 2 * inf["total_rank"])
     return {"workload": "32 sphere H-matrices, N log-uniform in [8192, 131072] (total %d), Yukawa, "
@@ -170,6 +181,7 @@ def batch_measurement(dev, steps):
             "products_per_s_batch_graph": 32e3 / t_graph,
             "speedup_batch_graph_vs_one_by_one": t_each / t_graph,
             "batch_equals_members_bitwise": same, "algorithmic_gbs_batch_graph": byts / (t_graph * 1e-3) / 1e9,
+            "phases_ms": {"permute": ph[0], "v_pass": ph[1], "near_u_pass": ph[2]}, "autotuned": tune,
             "build_seconds": build}
 
 

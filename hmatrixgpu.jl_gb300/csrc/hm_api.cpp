@@ -496,7 +496,7 @@ extern "C" int hmgpu_matvec(hmgpu_hmatrix *h, const void *x, void *y, int64_t nr
           (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.prow),
                          std::max<int64_t>(H.plan.p_rows, 1) * hm::kTcMaxRhs * 4)) ||
           (rc = H.dalloc(reinterpret_cast<void **>(&H.tc.xscale),
-                         2 * static_cast<size_t>(H.tc.nmem) * hm::kTcMaxRhs * sizeof(float))))
+                         3 * static_cast<size_t>(H.tc.nmem) * hm::kTcMaxRhs * sizeof(float))))
         return rc;
       cudaMemsetAsync(H.tc.xts, 0, xb, s);
       if (cudaError_t e = hm::encode_xts_map(H.tc, 32)) return hm::cuda_fail(e, "tensor map of XTS");

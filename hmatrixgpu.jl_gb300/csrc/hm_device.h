@@ -88,7 +88,7 @@ struct DevTc {
   uint16_t *xts = nullptr;    // xt_len rows of 32 FP16 hi + 32 FP16 lo (passes of <= 32 columns)
   uint16_t *xts64 = nullptr;  // xt_len rows of 64 FP16 hi + 64 FP16 lo (passes of 33..64 columns)
   float *prow = nullptr;      // partial rows of split V items, 64 values per row
-  float *xscale = nullptr;    // per pass: max |x_r| bits (64 words per member), then 1 / sigma (64 floats per member)
+  float *xscale = nullptr;    // per pass and member: max |x_r| bits, sigma_r, 1 / sigma_r (64 words each)
   int64_t *mcol0 = nullptr;   // first source index of each batch member, nmem + 1 entries
   int32_t nmem = 1;           // batch members (1 outside batches)
   int32_t n_v = 0, n_du = 0, n_reduce = 0, ctas = 0;

@@ -72,10 +72,14 @@ constexpr int kQ = 16;                  // item queue slots
 #ifndef HM_TC_SEG_CHUNKS
 #define HM_TC_SEG_CHUNKS 1
 #endif
-// chunks per accumulator buffer: the tensor cores' own accumulation spans at
-// most this many chunks (4 UMMAs each) before the epilogue takes the partial
-// sums into FP32 registers
-constexpr int kSegChunks = HM_TC_SEG_CHUNKS;
+#ifndef HM_TC_SEG_CHUNKS_V
+#define HM_TC_SEG_CHUNKS_V HM_TC_SEG_CHUNKS
+#endif
+// chunks per accumulator buffer, for near/U tiles and for V pieces: the
+// tensor cores' own accumulation spans at most this many chunks (4 UMMAs
+// each) before the epilogue takes the partial sums into FP32 registers
+constexpr int kSegChunksDU = HM_TC_SEG_CHUNKS;
+constexpr int kSegChunksV = HM_TC_SEG_CHUNKS_V;
 
 // MN-major B: the hi and lo halves of the R right-hand sides are stacked along
 // N, so one XTS row (4R bytes) is one K row of B. Core matrices of 8 N values
@@ -560,6 +564,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       // V pieces' B tiles come from the tile load (K groups 128 B apart, N
       // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
       const bool tma_b = I.kind != 0;
+      const int kSegChunks = tma_b ? kSegChunksV : kSegChunksDU;
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         const int kc = min(kKc, npad - c0), st = static_cast<int>(g % kStages);
         const int ci = c0 / kKc;  // chunk of the item
@@ -635,7 +640,8 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       if ((n & 1) != e) continue;
       const uint32_t k = static_cast<uint32_t>(n >> 1);  // this set's item count
       const int nch = ((I.ncols > 0 ? (I.ncols + 15) & ~15 : 16) + kKc - 1) / kKc;
-      const int nbuf = (nch + kSegChunks - 1) / kSegChunks;  // accumulator buffers of the item
+      const int span = I.kind != 0 ? kSegChunksV : kSegChunksDU;
+      const int nbuf = (nch + span - 1) / span;  // accumulator buffers of the item
       // w[c]: A_part B_hi + A_part B_lo of right-hand side c, chunk by chunk
       float w[R];
 #pragma unroll
@@ -724,47 +730,43 @@ __device__ __forceinline__ int member_of(const int64_t *col0, int nmem, int64_t 
 // max |X[., r]| per batch member and right-hand side r < nr, as FP32 bits
 // (non-negative floats order as unsigned integers) into xmax[member * 64 + r],
 // which starts at zero. Members own the contiguous source ranges [col0[k],
-// col0[k + 1]); each block takes a contiguous range of source indices and
-// keeps the maxima of its current member in shared memory.
+// col0[k + 1]). Block x takes source indices [x kXmaxSpan, (x + 1)
+// kXmaxSpan), its warp w right-hand side 8 y + w: coalesced loads along the
+// indices, four in flight per lane, one atomic per member met.
+constexpr int kXmaxSpan = 8192;
 __global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, int64_t n_src,
                             const int64_t *__restrict__ col0, int nmem, unsigned *__restrict__ xmax) {
-  __shared__ unsigned smax[kTcMaxRhs];
-  __shared__ int cur, mlo, mhi;
-  const int64_t per = (n_src + gridDim.x - 1) / gridDim.x;
-  const int64_t jb = blockIdx.x * per, je = min(n_src, jb + per);
-  for (int r = threadIdx.x; r < kTcMaxRhs; r += blockDim.x) smax[r] = 0u;
-  if (threadIdx.x == 0) cur = -1;
-  __syncthreads();
-  for (int64_t j0 = jb; j0 < je; j0 += blockDim.x) {
-    if (threadIdx.x == 0) {
-      mlo = member_of(col0, nmem, j0);
-      mhi = member_of(col0, nmem, min(je, j0 + static_cast<int64_t>(blockDim.x)) - 1);
+  const int lane = threadIdx.x & 31;
+  const int r = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= nr) return;
+  const int64_t j0 = blockIdx.x * static_cast<int64_t>(kXmaxSpan), j1 = min(n_src, j0 + kXmaxSpan);
+  const float *xr = X + r * ldx;
+  for (int k = member_of(col0, nmem, j0); k < nmem && col0[k] < j1; k++) {
+    const int64_t a0 = max(j0, col0[k]), a1 = min(j1, col0[k + 1]);
+    unsigned m = 0u;
+    int64_t j = a0 + lane;
+    for (; j + 96 < a1; j += 128) {
+      const float v0 = xr[j], v1 = xr[j + 32], v2 = xr[j + 64], v3 = xr[j + 96];
+      m = max(m, max(__float_as_uint(fabsf(v0)), __float_as_uint(fabsf(v1))));
+      m = max(m, max(__float_as_uint(fabsf(v2)), __float_as_uint(fabsf(v3))));
     }
-    __syncthreads();
-    if (mlo != cur) {  // the block's range enters another member: flush, restart
-      if (cur >= 0)
-        for (int r = threadIdx.x; r < nr; r += blockDim.x) atomicMax(&xmax[cur * kTcMaxRhs + r], smax[r]);
-      __syncthreads();
-      for (int r = threadIdx.x; r < kTcMaxRhs; r += blockDim.x) smax[r] = 0u;
-      if (threadIdx.x == 0) cur = mlo;
-      __syncthreads();
-    }
-    const int64_t j = j0 + threadIdx.x;
-    if (mlo == mhi) {
-      for (int r = 0; r < nr; r++) {
-        unsigned m = j < je ? __float_as_uint(fabsf(X[j + r * ldx])) : 0u;
+    for (; j < a1; j += 32) m = max(m, __float_as_uint(fabsf(xr[j])));
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((threadIdx.x & 31) == 0) atomicMax(&smax[r], m);
-      }
-    } else if (j < je) {  // a member boundary inside this step: straight to global
-      const int mj = member_of(col0, nmem, j);
-      for (int r = 0; r < nr; r++) atomicMax(&xmax[mj * kTcMaxRhs + r], __float_as_uint(fabsf(X[j + r * ldx])));
-    }
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && a1 > a0) atomicMax(&xmax[k * kTcMaxRhs + r], m);
   }
-  if (cur >= 0)
-    for (int r = threadIdx.x; r < nr; r += blockDim.x) atomicMax(&xmax[cur * kTcMaxRhs + r], smax[r]);
+}
+
+// sigma per member and right-hand side (sig) and its inverse (xs_inv), from
+// the maxima; right-hand sides past nr get 1.
+__global__ void sigma_kernel(const unsigned *__restrict__ xmax, int nmem, int nr, float *__restrict__ sig,
+                             float *__restrict__ xs_inv) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nmem * kTcMaxRhs; e += gridDim.x * blockDim.x) {
+    const int r = e % kTcMaxRhs;
+    const float s = r < nr ? pow2_scale(__uint_as_float(xmax[e])) : 1.0f;
+    sig[e] = s;
+    xs_inv[e] = 1.0f / s;
+  }
 }
 
 // XTS x rows from X in its own order: the R right-hand sides X[j + r ldx]
@@ -772,32 +774,22 @@ __global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, in
 // split into FP16 hi (first 2R bytes) and lo (last 2R bytes), go to row
 // sinv[j]. Reads of X are coalesced along j and every row is written whole;
 // x-region rows that no source index maps to stay zero from the allocation.
-// Block 0 also stores 1 / sigma per member and right-hand side for the
-// epilogue, and re-arms the two item tickets.
+// Also re-arms the two item tickets.
 template <int R>
 __global__ void permute_split_kernel(const float *__restrict__ X, int64_t ldx, int nr,
                                      const int32_t *__restrict__ sinv0, int64_t n_src,
                                      uint16_t *__restrict__ xts, int32_t *__restrict__ tickets,
-                                     const int64_t *__restrict__ col0, int nmem,
-                                     const unsigned *__restrict__ xmax, float *__restrict__ xs_inv) {
+                                     const int64_t *__restrict__ col0, int nmem, const float *__restrict__ sig) {
   __shared__ float tile[64][R + 1];
   __shared__ int mem[64];
-  if (blockIdx.x == 0) {
-    if (threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
-    for (int e = threadIdx.x; e < nmem * R; e += blockDim.x) {
-      const int k = e / R, r = e % R;
-      xs_inv[k * kTcMaxRhs + r] = r < nr ? 1.0f / pow2_scale(__uint_as_float(xmax[k * kTcMaxRhs + r])) : 1.0f;
-    }
-  }
+  if (blockIdx.x == 0 && threadIdx.x < 2) tickets[threadIdx.x] = 0;  // V and near/U item tickets
   for (int64_t j0 = blockIdx.x * 64ll; j0 < n_src; j0 += gridDim.x * 64ll) {
     if (threadIdx.x < 64) mem[threadIdx.x] = member_of(col0, nmem, min(j0 + threadIdx.x, n_src - 1));
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * R; e += blockDim.x) {
       const int r = e / 64, jj = e % 64;  // consecutive threads: consecutive j
       const int64_t j = j0 + jj;
-      tile[jj][r] = (j < n_src && r < nr)
-                        ? X[j + r * ldx] * pow2_scale(__uint_as_float(xmax[mem[jj] * kTcMaxRhs + r]))
-                        : 0.0f;
+      tile[jj][r] = (j < n_src && r < nr) ? X[j + r * ldx] * __ldg(sig + mem[jj] * kTcMaxRhs + r) : 0.0f;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * (R / 8); e += blockDim.x) {
@@ -1001,13 +993,17 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   int gp = static_cast<int>((p.n_src + 63) / 64);
   if (gp > 2048) gp = 2048;
   if (ev) cudaEventRecord(ev[0], s);
+  // per member and right-hand side: max |x| bits, sigma, 1 / sigma
+  const int64_t nm64 = static_cast<int64_t>(t.nmem) * kTcMaxRhs;
   unsigned *xmax = reinterpret_cast<unsigned *>(t.xscale);
-  float *xs_inv = t.xscale + static_cast<int64_t>(t.nmem) * kTcMaxRhs;
-  cudaMemsetAsync(xmax, 0, static_cast<size_t>(t.nmem) * kTcMaxRhs * sizeof(unsigned), s);
-  xmax_kernel<<<gp < 512 ? gp : 512, 256, 0, s>>>(X, ldx, nr, p.n_src, t.mcol0, t.nmem, xmax);
+  float *sig = t.xscale + nm64, *xs_inv = t.xscale + 2 * nm64;
+  cudaMemsetAsync(xmax, 0, nm64 * sizeof(unsigned), s);
+  const dim3 gx(static_cast<unsigned>((p.n_src + kXmaxSpan - 1) / kXmaxSpan), static_cast<unsigned>((nr + 7) / 8));
+  xmax_kernel<<<gx, 256, 0, s>>>(X, ldx, nr, p.n_src, t.mcol0, t.nmem, xmax);
+  sigma_kernel<<<static_cast<unsigned>((nm64 + 255) / 256), 256, 0, s>>>(xmax, t.nmem, nr, sig, xs_inv);
   permute_split_kernel<R><<<gp, 256, 0, s>>>(X, ldx, nr, p.sinv0, p.n_src, xts, p.counter + 2, t.mcol0, t.nmem,
-                                              xmax, xs_inv);
-  nl += 2;
+                                              sig);
+  nl += 3;
   if (ev) cudaEventRecord(ev[1], s);
   TcArgs a{};
   a.xmap = t.xmap[R / 64];
