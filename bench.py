@@ -322,6 +322,35 @@ def cube_measurement(dev, steps, hbm):
     rhs64["mixed_speedup_vs_plain_f32"] = rhs64["plain_f32"]["ms_per_64rhs_product"] / \
         rhs64["mixed_tensor_cores"]["ms_per_64rhs_product"]
     del Hm
+
+    # the same matrix stored in FP64 (the drop-in's FP64 mode), one RHS
+    H64 = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=2.0, eps=1e-6, precision="f64")
+    H64.autotune()
+    x64, y64 = x.double(), torch.empty(n, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        hmgpu.mul_(y64, H64, x64)
+    hmgpu.check(lib.hmgpu_hmatrix_set_profiling(H64._h, 1))
+    torch.cuda.synchronize()
+    s.record(stream)
+    for _ in range(reps):
+        hmgpu.mul_(y64, H64, x64)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms64 = s.elapsed_time(e) / reps
+    ph64 = np.zeros(3)
+    hmgpu.check(lib.hmgpu_hmatrix_phase_times(H64._h, hmgpu.ptr(ph64), C.byref(nl), C.byref(npd)))
+    hmgpu.check(lib.hmgpu_hmatrix_set_profiling(H64._h, 0))
+    ph64 = ph64 / max(npd.value, 1)
+    b64 = 2 * alg  # every stored entry and vector entry in 8 bytes
+    y64h = y64.cpu().numpy()
+    f64 = {"ms_per_product": ms64, "matvec_per_s": 1e3 / ms64, "hbm_gbs": b64 / (ms64 * 1e-3) / 1e9,
+           "frac_of_measured": b64 / (ms64 * 1e-3) / 1e9 / hbm,
+           "phases_ms": {"permute": ph64[0], "v_pass": ph64[1], "near_u_pass": ph64[2]},
+           "near_u_gbs": 2 * du_b / (ph64[2] * 1e-3) / 1e9, "v_pass_gbs": 2 * v_b / (ph64[1] * 1e-3) / 1e9,
+           "stored_gb": H64.info()["matrix_bytes"] / 1e9,
+           "rel_err_256_exact_rows": float(np.linalg.norm(y64h[rows] - exact) / np.linalg.norm(exact)),
+           "rel_diff_vs_f32": float(np.linalg.norm(y64h - ys) / np.linalg.norm(y64h))}
+    del H64
     return {"workload": "cube-2^18 Laplace leaf64 eta2 tol1e-6, 1 RHS, FP32 storage",
             "build_seconds": build, "build": H.build_profile(), "autotuned": tune,
             "dense_entries": inf["dense_entries"], "far_entries": inf["far_entries"],
@@ -332,7 +361,7 @@ def cube_measurement(dev, steps, hbm):
             "v_pass_gbs": v_b / (ph[1] * 1e-3) / 1e9, "near_u_gbs": du_b / (ph[2] * 1e-3) / 1e9,
             "near_u_frac_of_measured": du_b / (ph[2] * 1e-3) / 1e9 / hbm,
             "v_pass_frac_of_measured": v_b / (ph[1] * 1e-3) / 1e9 / hbm,
-            "rel_err_256_exact_rows": err, "rhs64": rhs64}
+            "rel_err_256_exact_rows": err, "rhs64": rhs64, "f64_storage": f64}
 
 
 def learned_measurement(dev):
