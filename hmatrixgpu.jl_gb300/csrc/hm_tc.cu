@@ -79,13 +79,7 @@ constexpr int kQ = 16;                  // item queue slots
 // tensor cores' own accumulation spans at most this many chunks (4 UMMAs
 // each) before the epilogue takes the partial sums into FP32 registers
 constexpr int kSegChunksDU = HM_TC_SEG_CHUNKS;
-#ifndef HM_TC_XTS_EVICT_LAST
-#define HM_TC_XTS_EVICT_LAST 1
-#endif
-// XTS rows are read by every tile whose blocks touch their cluster: loads of
-// them ask L2 to keep them (evict-last) while the tile chunks, read once,
-// go first (evict-first)
-constexpr bool kXtsEvictLast = HM_TC_XTS_EVICT_LAST != 0;
+
 constexpr int kSegChunksV = HM_TC_SEG_CHUNKS_V;
 
 // MN-major B: the hi and lo halves of the R right-hand sides are stacked along
@@ -433,11 +427,6 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
     bool stop = false;
     const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
-    uint64_t xpol;  // L2 policy of the XTS loads
-    if (kXtsEvictLast)
-      asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(xpol));
-    else
-      asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(xpol));
     for (int n = 0; !stop; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
@@ -507,9 +496,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
             // .., so one tile load of 64 rows lands them in the canonical
             // MN-major layout (K groups 128 B apart, N groups 1024 B apart)
             asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], "
-                "[%1, {%2, %3, %4}], [%5], %6;" ::"r"(su32(S.b[s])),
-                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bar), "l"(xpol)
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(su32(S.b[s])),
+                "l"(reinterpret_cast<uint64_t>(&a.xmap)), "r"(0), "r"(I.map + c0), "r"(0), "r"(bar)
                 : "memory");
             arrive(&S.full[s]);
           }
@@ -524,10 +513,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
         for (int q = 0; q < kKc / 8; q++)
           if (lane == q && ((gmask >> q) & 1u))
             asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], "
-                "[%1, {%2, %3, %4}], [%5], %6;" ::"r"(su32(S.b[s]) + static_cast<uint32_t>(q) * Sh::kBGroupK),
-                "l"(reinterpret_cast<uint64_t>(&a.xmap8)), "r"(0), "r"(grow[q]), "r"(0), "r"(su32(&S.full[s])),
-                "l"(xpol)
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(su32(S.b[s]) + static_cast<uint32_t>(q) * Sh::kBGroupK),
+                "l"(reinterpret_cast<uint64_t>(&a.xmap8)), "r"(0), "r"(grow[q]), "r"(0), "r"(su32(&S.full[s]))
                 : "memory");
         const uint32_t dst0 = su32(S.b[s]) + piece * kBGroupN;
 #pragma unroll
@@ -536,9 +524,8 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           const int r = __shfl_sync(0xffffffffu, rows[(i * Sh::kRowsPerCopy) >> 5], k & 31);
           if (k < kc && !((gmask >> (k >> 3)) & 1u)) {
             const uint16_t *src = a.xts + static_cast<int64_t>(r) * (2 * R) + piece * 8;
-            asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(
-                             dst0 + (k >> 3) * Sh::kBGroupK + (k & 7) * 16),
-                         "l"(src), "l"(xpol)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst0 + (k >> 3) * Sh::kBGroupK + (k & 7) * 16),
+                         "l"(src)
                          : "memory");
           }
         }
