@@ -423,7 +423,9 @@ def learned_measurement(dev):
         torch.cuda.synchronize()
         rec = {"build_seconds": build, "build": H.build_profile(), "aca_batches": inf["aca_batches"],
                "aca_workspace_gb": inf["aca_workspace_bytes"] / 1e9, "aca_reruns": inf["aca_reruns"],
-               "misprediction_rate": inf["aca_reruns"] / max(1, inf["admissible_leaves"]),
+               "aca_continued": inf["aca_continued"],
+               "misprediction_rate": (inf["aca_reruns"] + inf["aca_continued"]) / max(1, inf["admissible_leaves"]),
+               "restart_rate": inf["aca_reruns"] / max(1, inf["admissible_leaves"]),
                "lowrank_blocks": inf["admissible_leaves"], "dense_blocks": inf["full_leaves"],
                "stored_gb": inf["matrix_bytes"] / 1e9, "ms_per_product": s.elapsed_time(e) / 10}
         if y_first is None:

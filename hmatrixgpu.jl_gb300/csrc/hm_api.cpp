@@ -634,6 +634,7 @@ extern "C" int hmgpu_hmatrix_info(const hmgpu_hmatrix *h, hmgpu_info *info) {
   info->aca_batches = H.aca_batches;
   info->aca_reruns = H.aca_reruns;
   info->aca_workspace_bytes = H.aca_ws_bytes;
+  info->aca_continued = H.aca_continued;
   return HMGPU_OK;
 }
 

@@ -50,7 +50,7 @@ struct HMatrix {
   int64_t prof_launches = 0;
   double build_seconds = 0.0;
   double build_phase[HMGPU_BUILD_PHASES] = {};  // see hmgpu_hmatrix_build_profile
-  int64_t aca_batches = 0, aca_reruns = 0, aca_ws_bytes = 0;
+  int64_t aca_batches = 0, aca_reruns = 0, aca_ws_bytes = 0, aca_continued = 0;
   int64_t device_bytes = 0;
   std::vector<void *> dev_allocs;
   // batches: first row and first column of every member, then m and n (empty

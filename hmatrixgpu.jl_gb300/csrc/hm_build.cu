@@ -255,6 +255,10 @@ struct AcaJob {
   int64_t ws;            // workspace offset in doubles
   int32_t kcap;          // U columns / V rows available
   int32_t max_iter;      // min(m, n, max_iter)
+  // continuation: k0 > 0 resumes an ACA that stopped with k0 terms when its
+  // workspace (at `carry`, kcap0 terms) was full; its state is copied over
+  int32_t k0, kcap0;
+  int64_t carry;
 };
 
 struct AcaRes {
@@ -353,17 +357,34 @@ __device__ void aca_team(const KDev &K, const int32_t *tmap0, const int32_t *sma
   const int m = jb.m, n = jb.n, kcap = jb.kcap;
   WS w = ws_view(wsbase + jb.ws, m, n, kcap);
   const int32_t *trow = tmap0 + jb.rs, *scol = smap0 + jb.cs;
-  for (int j = t; j < n; j += NT) {
-    w.rrow[j] = 0.0;
-    w.used_c[j] = 0;
-  }
-  for (int i = t; i < m; i += NT) {
-    w.rcol[i] = 0.0;
-    w.used_r[i] = 0;
+  if (jb.k0 > 0) {
+    // a continuation: the first k0 terms, the last residual row and column
+    // and the used pivots, exactly as the stopped run left them, so the run
+    // goes on as if its workspace had been large enough
+    const WS o = ws_view(wsbase + jb.carry, m, n, jb.kcap0);
+    for (int64_t e = t; e < static_cast<int64_t>(m) * jb.k0; e += NT) w.U[e] = o.U[e];
+    for (int64_t e = t; e < static_cast<int64_t>(jb.k0) * n; e += NT) w.V[e] = o.V[e];
+    for (int j = t; j < n; j += NT) {
+      w.rrow[j] = o.rrow[j];
+      w.used_c[j] = o.used_c[j];
+    }
+    for (int i = t; i < m; i += NT) {
+      w.rcol[i] = o.rcol[i];
+      w.used_r[i] = o.used_r[i];
+    }
+  } else {
+    for (int j = t; j < n; j += NT) {
+      w.rrow[j] = 0.0;
+      w.used_c[j] = 0;
+    }
+    for (int i = t; i < m; i += NT) {
+      w.rcol[i] = 0.0;
+      w.used_r[i] = 0;
+    }
   }
   tsync<NT>();
-  int k = 0, flags = 0;
-  for (int it = 1; it <= jb.max_iter; it++) {
+  int k = jb.k0 > 0 ? jb.k0 : 0, flags = 0;
+  for (int it = k + 1; it <= jb.max_iter; it++) {
     int rp = 0, cp = 0;
     if (it > 1) {  // :72-73
       cp = team_argmax_unused<NT>(w.rrow, w.used_c, n, sc);
@@ -800,17 +821,79 @@ struct Compressor {
   int svd;
   int64_t budget;  // doubles of workspace per batch
   int grid_aca = 1, grid_qr = 1, grid_form = 1;
-  int64_t batches = 0, ws_bytes = 0;  // statistics of all run() calls
+  // continuation: batches fill 3/4 of the budget, and a block that fills its
+  // workspace goes on in the last quarter, from its state, in the same batch
+  bool resume = false;
+  int64_t batches = 0, ws_bytes = 0, continued = 0;  // statistics of all run() calls
 
   // Processes jobs[idx] for idx in `sel`, writing results into res (indexed like jobs).
   // keep(jj, k, r) -> bool decides whether low-rank factors are written; factors
   // of kept blocks go to (ustore + uoff[jj], vstore + voff[jj]) allocated by `place`.
+  // The blocks of a batch that filled their workspace before converging go
+  // on in the free part of the workspace with the next cap (the fixed cap,
+  // then min(m, n)), from the state they stopped in; the batch's jobs and
+  // results on the device are updated to the continued runs. Blocks that do
+  // not fit are left to the restart after all batches.
+  int continue_full(std::vector<AcaJob> &batch, int64_t used, DevBuf &ws, DevBuf &djobs, DevBuf &dres, DevBuf &dcj,
+                    DevBuf &dcr, int32_t *tk) {
+    const int nb = static_cast<int>(batch.size());
+    std::vector<AcaRes> hr(nb);
+    cudaError_t e = cudaMemcpy(hr.data(), dres.p, nb * sizeof(AcaRes), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "ACA kernel");
+    std::vector<AcaJob> cj;
+    std::vector<int> cidx;
+    int64_t extra = used;
+    const int64_t room = static_cast<int64_t>(ws.cap / sizeof(double));
+    for (int b = 0; b < nb; b++) {  // team jobs stay first: the batch lists them first
+      if (!(hr[b].flags & 2)) continue;
+      AcaJob j2 = batch[b];
+      const int32_t fixed = std::min(j2.max_iter, 48);
+      const int32_t cap2 = j2.kcap < fixed ? fixed : j2.max_iter;
+      const int64_t need = ws_doubles(j2.m, j2.n, cap2);
+      if (extra + need > room) continue;
+      j2.k0 = hr[b].k;
+      j2.kcap0 = j2.kcap;
+      j2.carry = j2.ws;
+      j2.kcap = cap2;
+      j2.ws = extra;
+      extra += need;
+      cj.push_back(j2);
+      cidx.push_back(b);
+    }
+    if (cj.empty()) return HMGPU_OK;
+    const int nc = static_cast<int>(cj.size());
+    int nbig = 0;
+    while (nbig < nc && team_job(cj[nbig])) nbig++;
+    int rc;
+    if ((rc = dcj.reserve(nc * sizeof(AcaJob))) || (rc = dcr.reserve(nc * sizeof(AcaRes)))) return rc;
+    cudaMemcpy(dcj.p, cj.data(), nc * sizeof(AcaJob), cudaMemcpyHostToDevice);
+    cudaMemset(dcr.p, 0, nc * sizeof(AcaRes));
+    cudaMemset(tk, 0, 2 * sizeof(int32_t));
+    aca_kernel<<<grid_aca, kBuildThreads>>>(K, tmap0, smap0, dcj.as<AcaJob>(), nbig, nc, eps_aca, ws.as<double>(),
+                                            dcr.as<AcaRes>(), tk);
+    std::vector<AcaRes> cr(nc);
+    e = cudaMemcpy(cr.data(), dcr.p, nc * sizeof(AcaRes), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "ACA continuation");
+    for (int q = 0; q < nc; q++) {
+      batch[cidx[q]] = cj[q];
+      hr[cidx[q]] = cr[q];
+    }
+    cudaMemcpy(djobs.p, batch.data(), nb * sizeof(AcaJob), cudaMemcpyHostToDevice);
+    cudaMemcpy(dres.p, hr.data(), nb * sizeof(AcaRes), cudaMemcpyHostToDevice);
+    continued += nc;
+    ws_bytes += (extra - used) * static_cast<int64_t>(sizeof(double));
+    return HMGPU_OK;
+  }
+
   template <typename Keep, typename Place, typename After>
   int run(std::vector<AcaJob> &jobs, std::vector<AcaRes> &res, const std::vector<int> &sel,
           Keep keep, Place place, After after) {
     size_t pos = 0;
-    DevBuf ws, djobs, dres, dtick, duo, dvo;
+    DevBuf ws, djobs, dres, dtick, duo, dvo, dcj, dcr;
     if (int rc = dtick.alloc(8 * sizeof(int32_t))) return rc;
+    const int64_t fill = resume ? budget / 4 * 3 : budget;
+    if (resume)
+      if (int rc = ws.reserve(budget * sizeof(double))) return rc;
     while (pos < sel.size()) {
       std::vector<AcaJob> batch;
       std::vector<int> ids;
@@ -818,7 +901,7 @@ struct Compressor {
       while (pos < sel.size()) {
         AcaJob jb = jobs[sel[pos]];
         int64_t need = ws_doubles(jb.m, jb.n, jb.kcap);
-        if (!batch.empty() && used + need > budget) break;
+        if (!batch.empty() && used + need > fill) break;
         jb.ws = used;
         used += need;
         batch.push_back(jb);
@@ -855,6 +938,7 @@ struct Compressor {
       int32_t *tk = dtick.as<int32_t>();
       aca_kernel<<<grid_aca, kBuildThreads>>>(K, tmap0, smap0, djobs.as<AcaJob>(), nbig, nb, eps_aca,
                                           ws.as<double>(), dres.as<AcaRes>(), tk);
+      if (resume && (rc = continue_full(batch, used, ws, djobs, dres, dcj, dcr, tk + 6))) return rc;
       qr_kernel<<<grid_qr, kBuildThreads>>>(djobs.as<AcaJob>(), nbig, nb, svd, ws.as<double>(), dres.as<AcaRes>(),
                                          tk + 2);
       jacobi_kernel<<<(nb + kBuildThreads - 1) / kBuildThreads, kBuildThreads>>>(
@@ -1059,6 +1143,8 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   C.grid_aca = persistent_grid(aca_kernel);
   C.grid_qr = persistent_grid(qr_kernel);
   C.grid_form = persistent_grid(form_kernel);
+  // with learned caps, a block that outgrows its cap continues in its batch
+  C.resume = o.rank_model != nullptr;
 
   H.build_phase[1] = clk.lap();
   std::vector<AcaRes> res(na);
@@ -1132,6 +1218,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   }
   H.aca_batches = C.batches;
   H.aca_reruns = reruns;
+  H.aca_continued = C.continued;
   H.aca_ws_bytes = C.ws_bytes;
   H.build_phase[2] = clk.lap();
 
@@ -1252,7 +1339,7 @@ extern "C" int hmgpu_aca_plus(const double *A, int64_t lda, int64_t m, int64_t n
   cudaMemcpy(dt.p, id.data(), m * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(ds.p, id.data(), n * 4, cudaMemcpyHostToDevice);
   AcaJob j{0, static_cast<int32_t>(m), 0, static_cast<int32_t>(n), 0, static_cast<int32_t>(mi),
-           static_cast<int32_t>(mi)};
+           static_cast<int32_t>(mi), 0, 0, 0};
   if ((rc = dws.alloc(ws_doubles(m, n, mi) * 8))) return rc;
   cudaMemcpy(dj.p, &j, sizeof j, cudaMemcpyHostToDevice);
   cudaMemset(dr.p, 0, sizeof(AcaRes));
@@ -1294,7 +1381,7 @@ extern "C" int hmgpu_svd_recompress(int64_t m, int64_t n, int64_t k, const doubl
     for (int64_t c = 0; c < n; c++) w[m * k + q * n + c] = V[q + c * k];
   cudaMemcpy(dws.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice);
   AcaJob j{0, static_cast<int32_t>(m), 0, static_cast<int32_t>(n), 0, static_cast<int32_t>(k),
-           static_cast<int32_t>(k)};
+           static_cast<int32_t>(k), 0, 0, 0};
   AcaRes r0{static_cast<int32_t>(k), 0, 0, 0};
   cudaMemcpy(dj.p, &j, sizeof j, cudaMemcpyHostToDevice);
   cudaMemcpy(dr.p, &r0, sizeof r0, cudaMemcpyHostToDevice);

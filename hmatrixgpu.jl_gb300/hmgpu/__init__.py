@@ -383,7 +383,8 @@ class HMatrix:
                 "matrix_bytes": i.matrix_bytes, "device_bytes": i.device_bytes,
                 "n_tiles": i.n_tiles, "hi_only_blocks": i.hi_only_blocks,
                 "build_seconds": i.build_seconds, "aca_batches": i.aca_batches,
-                "aca_reruns": i.aca_reruns, "aca_workspace_bytes": i.aca_workspace_bytes}
+                "aca_reruns": i.aca_reruns, "aca_workspace_bytes": i.aca_workspace_bytes,
+                "aca_continued": i.aca_continued}
 
     BUILD_PHASES = ("block_tree", "setup", "aca", "gather", "plan", "pack", "tensor_core")
 

@@ -47,7 +47,8 @@ class Info(C.Structure):
                 ("matrix_bytes", C.c_int64), ("device_bytes", C.c_int64),
                 ("n_tiles", C.c_int64), ("precision", C.c_int32), ("hi_only_blocks", C.c_int32),
                 ("build_seconds", C.c_double), ("aca_batches", C.c_int64),
-                ("aca_reruns", C.c_int64), ("aca_workspace_bytes", C.c_int64)]
+                ("aca_reruns", C.c_int64), ("aca_workspace_bytes", C.c_int64),
+                ("aca_continued", C.c_int64)]
 
 
 # name -> (restype, argtypes); every entry point returns an int status unless noted

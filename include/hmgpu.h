@@ -219,6 +219,8 @@ typedef struct {
   int64_t aca_batches;           /* device ACA batches of the build                 */
   int64_t aca_reruns;            /* blocks rerun after outgrowing their workspace   */
   int64_t aca_workspace_bytes;   /* workspace bytes summed over the batches         */
+  int64_t aca_continued;         /* blocks that outgrew a learned workspace cap and
+                                    went on from their state in the same batch      */
 } hmgpu_info;
 /* info(::HMatrixCPU) (src/hmatrix.jl:289-330) plus storage figures. */
 int hmgpu_hmatrix_info(const hmgpu_hmatrix *H, hmgpu_info *info);

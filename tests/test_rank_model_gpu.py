@@ -75,3 +75,31 @@ def test_training_and_learned_bucketing(gpu):
         nblocks = len(hmgpu.block_features(T, T, 2.0, eps))
         assert il["aca_workspace_bytes"] < gain * ip["aca_workspace_bytes"], (eps, ip, il)
         assert il["aca_reruns"] <= 0.05 * nblocks, (eps, il["aca_reruns"], nblocks)
+
+
+def test_outgrown_caps_continue_bitwise(gpu):
+    """A network that predicts far too low (untrained, caps near 4 terms) makes
+    most blocks outgrow their workspace. Each continues from its state in the
+    same batch (the first terms, the last residual row and column, the used
+    pivots), so the H-matrix is bitwise the one built without the network."""
+    import torch
+    P = geometry.film(90, 70, seed=5)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=32)
+    K = hmgpu.Kernel("laplace", P)
+    plain = hmgpu.HMatrix(K, T, T, eta=2.0, eps=1e-6, precision="f64", keep_factors=True)
+    low = hmgpu.RankModel(seed=3)
+    low.params(set_params=np.zeros(hmgpu.RankModel.NPARAMS, np.float32))  # predicts 0 everywhere
+    learned = hmgpu.HMatrix(K, T, T, eta=2.0, eps=1e-6, precision="f64", keep_factors=True, rank_model=low)
+    il = learned.info()
+    nblocks = len(hmgpu.block_features(T, T, 2.0, 1e-6))
+    assert il["aca_continued"] > 0.5 * nblocks, (il["aca_continued"], nblocks)
+    a_p, _ = plain.aca_ranks(nblocks)
+    a_l, _ = learned.aca_ranks(nblocks)
+    np.testing.assert_array_equal(a_p, a_l)
+    for b in range(0, plain.info()["admissible_leaves"], 7):
+        Up, Vp = plain.block_factors(b)
+        Ul, Vl = learned.block_factors(b)
+        np.testing.assert_array_equal(Up, Ul)
+        np.testing.assert_array_equal(Vp, Vl)
+    x = torch.randn(P.shape[1], dtype=torch.float64, device=gpu)
+    assert torch.equal(plain * x, learned * x)
