@@ -175,6 +175,10 @@ def batch_measurement(dev, steps):
     ph = ph / max(npd.value, 1)
     inf = B.info()
     byts = 4 * (inf["dense_entries"] + inf["far_entries"]) + 4 * (2 * n + 2 * inf["total_rank"])
+    _, a = B.blocks()
+    u_entries = int(((a[:, 1] - a[:, 0] + 1) * a[:, 4]).sum()) if len(a) else 0
+    du_b = 4 * (inf["dense_entries"] + u_entries) + 4 * (2 * n + inf["total_rank"])
+    v_b = 4 * (inf["far_entries"] - u_entries) + 4 * inf["total_rank"]
     return {"workload": "32 sphere H-matrices, N log-uniform in [8192, 131072] (total %d), Yukawa, "
                         "leaf 32, eta 1.5, tol 1e-5, FP32, 1 RHS each" % int(sizes.sum()),
             "ms_members_one_by_one": t_each, "ms_batch": t_batch, "ms_batch_cuda_graph": t_graph,
@@ -182,6 +186,8 @@ def batch_measurement(dev, steps):
             "speedup_batch_graph_vs_one_by_one": t_each / t_graph,
             "batch_equals_members_bitwise": same, "algorithmic_gbs_batch_graph": byts / (t_graph * 1e-3) / 1e9,
             "phases_ms": {"permute": ph[0], "v_pass": ph[1], "near_u_pass": ph[2]}, "autotuned": tune,
+            "v_pass_gbs": v_b / (ph[1] * 1e-3) / 1e9, "near_u_gbs": du_b / (ph[2] * 1e-3) / 1e9,
+            "dense_entries": inf["dense_entries"], "far_entries": inf["far_entries"],
             "build_seconds": build}
 
 
