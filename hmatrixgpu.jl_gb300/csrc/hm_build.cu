@@ -830,57 +830,63 @@ struct Compressor {
   // keep(jj, k, r) -> bool decides whether low-rank factors are written; factors
   // of kept blocks go to (ustore + uoff[jj], vstore + voff[jj]) allocated by `place`.
   // The blocks of a batch that filled their workspace before converging go
-  // on in the free part of the workspace with the next cap (the fixed cap,
-  // then min(m, n)), from the state they stopped in; the batch's jobs and
-  // results on the device are updated to the continued runs. Blocks that do
-  // not fit are left to the restart after all batches.
+  // on in the free part of the workspace, from the state they stopped in,
+  // with room for half as many terms again (at least 8 more, at most
+  // min(m, n)), round after round while blocks still fill up and room is
+  // left; the batch's jobs and results on the device are updated to the
+  // continued runs. Blocks that do not fit are left to the restart after all
+  // batches.
   int continue_full(std::vector<AcaJob> &batch, int64_t used, DevBuf &ws, DevBuf &djobs, DevBuf &dres, DevBuf &dcj,
                     DevBuf &dcr, int32_t *tk) {
     const int nb = static_cast<int>(batch.size());
     std::vector<AcaRes> hr(nb);
     cudaError_t e = cudaMemcpy(hr.data(), dres.p, nb * sizeof(AcaRes), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "ACA kernel");
-    std::vector<AcaJob> cj;
-    std::vector<int> cidx;
-    int64_t extra = used;
     const int64_t room = static_cast<int64_t>(ws.cap / sizeof(double));
-    for (int b = 0; b < nb; b++) {  // team jobs stay first: the batch lists them first
-      if (!(hr[b].flags & 2)) continue;
-      AcaJob j2 = batch[b];
-      const int32_t fixed = std::min(j2.max_iter, 48);
-      const int32_t cap2 = j2.kcap < fixed ? fixed : j2.max_iter;
-      const int64_t need = ws_doubles(j2.m, j2.n, cap2);
-      if (extra + need > room) continue;
-      j2.k0 = hr[b].k;
-      j2.kcap0 = j2.kcap;
-      j2.carry = j2.ws;
-      j2.kcap = cap2;
-      j2.ws = extra;
-      extra += need;
-      cj.push_back(j2);
-      cidx.push_back(b);
+    int64_t extra = used;
+    bool changed = false;
+    for (;;) {
+      std::vector<AcaJob> cj;
+      std::vector<int> cidx;
+      for (int b = 0; b < nb; b++) {  // team jobs stay first: the batch lists them first
+        if (!(hr[b].flags & 2)) continue;
+        AcaJob j2 = batch[b];
+        const int32_t cap2 = std::min(j2.max_iter, std::max(j2.kcap + 8, j2.kcap + j2.kcap / 2));
+        const int64_t need = ws_doubles(j2.m, j2.n, cap2);
+        if (extra + need > room) continue;
+        j2.k0 = hr[b].k;
+        j2.kcap0 = j2.kcap;
+        j2.carry = j2.ws;
+        j2.kcap = cap2;
+        j2.ws = extra;
+        extra += need;
+        cj.push_back(j2);
+        cidx.push_back(b);
+      }
+      if (cj.empty()) break;
+      const int nc = static_cast<int>(cj.size());
+      int nbig = 0;
+      while (nbig < nc && team_job(cj[nbig])) nbig++;
+      int rc;
+      if ((rc = dcj.reserve(nc * sizeof(AcaJob))) || (rc = dcr.reserve(nc * sizeof(AcaRes)))) return rc;
+      cudaMemcpy(dcj.p, cj.data(), nc * sizeof(AcaJob), cudaMemcpyHostToDevice);
+      cudaMemset(dcr.p, 0, nc * sizeof(AcaRes));
+      cudaMemset(tk, 0, 2 * sizeof(int32_t));
+      aca_kernel<<<grid_aca, kBuildThreads>>>(K, tmap0, smap0, dcj.as<AcaJob>(), nbig, nc, eps_aca,
+                                              ws.as<double>(), dcr.as<AcaRes>(), tk);
+      std::vector<AcaRes> cr(nc);
+      e = cudaMemcpy(cr.data(), dcr.p, nc * sizeof(AcaRes), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "ACA continuation");
+      for (int q = 0; q < nc; q++) {
+        batch[cidx[q]] = cj[q];
+        hr[cidx[q]] = cr[q];
+      }
+      continued += nc;
+      changed = true;
     }
-    if (cj.empty()) return HMGPU_OK;
-    const int nc = static_cast<int>(cj.size());
-    int nbig = 0;
-    while (nbig < nc && team_job(cj[nbig])) nbig++;
-    int rc;
-    if ((rc = dcj.reserve(nc * sizeof(AcaJob))) || (rc = dcr.reserve(nc * sizeof(AcaRes)))) return rc;
-    cudaMemcpy(dcj.p, cj.data(), nc * sizeof(AcaJob), cudaMemcpyHostToDevice);
-    cudaMemset(dcr.p, 0, nc * sizeof(AcaRes));
-    cudaMemset(tk, 0, 2 * sizeof(int32_t));
-    aca_kernel<<<grid_aca, kBuildThreads>>>(K, tmap0, smap0, dcj.as<AcaJob>(), nbig, nc, eps_aca, ws.as<double>(),
-                                            dcr.as<AcaRes>(), tk);
-    std::vector<AcaRes> cr(nc);
-    e = cudaMemcpy(cr.data(), dcr.p, nc * sizeof(AcaRes), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "ACA continuation");
-    for (int q = 0; q < nc; q++) {
-      batch[cidx[q]] = cj[q];
-      hr[cidx[q]] = cr[q];
-    }
+    if (!changed) return HMGPU_OK;
     cudaMemcpy(djobs.p, batch.data(), nb * sizeof(AcaJob), cudaMemcpyHostToDevice);
     cudaMemcpy(dres.p, hr.data(), nb * sizeof(AcaRes), cudaMemcpyHostToDevice);
-    continued += nc;
     ws_bytes += (extra - used) * static_cast<int64_t>(sizeof(double));
     return HMGPU_OK;
   }
@@ -1104,7 +1110,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   std::vector<int> order(na);
   for (size_t a = 0; a < na; a++) order[a] = static_cast<int>(a);
   if (o.rank_model && na > 0) {
-    // learned bucketing: workspace for 1.25 x the predicted rank + 4 terms,
+    // learned bucketing: workspace for 1.5 x the predicted rank + 6 terms,
     // blocks of equal predicted workspace batched together
     std::vector<float> feats(na * HMGPU_RANK_FEATURES), pred(na);
     for (size_t a = 0; a < na; a++)
@@ -1115,7 +1121,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
       return rc;
     for (size_t a = 0; a < na; a++) {
       const float p = std::isfinite(pred[a]) ? std::max(pred[a], 0.0f) : 1e9f;
-      const int64_t cap = static_cast<int64_t>(std::ceil(1.25 * p)) + 4;
+      const int64_t cap = static_cast<int64_t>(std::ceil(1.5 * p)) + 6;
       // never above the fixed cap: a prediction can only shrink the workspace
       // (a block that needs more is rerun with room for min(m, n) terms either way)
       jobs[a].kcap = static_cast<int32_t>(std::max<int64_t>(1, std::min<int64_t>(cap, jobs[a].kcap)));
