@@ -315,15 +315,22 @@ __global__ void __launch_bounds__(kThreads, 6) du_rows_kernel(DuArgs<T> a) {
     for (int c0 = 0; c0 < d.ld; c0 += CH) {
       const int cn = min(CH, d.ld - c0);
       __syncthreads();  // segments loaded / previous chunk's entries no longer read
-      // the chunk's vector entries, segment by segment: a warp copies one
-      // segment's run of XT (coalesced, no search per column); the segments
-      // cover the columns [0, ncols) in order, the stride padding reads zero
-      for (int sg = warp; sg < d.nseg; sg += kThreads / 32) {
-        const Seg g = S[sg];
-        const int b0 = max(g.col0, c0), b1 = min(g.col0 + g.ncols, c0 + cn);
-        for (int c = b0 + lane; c < b1; c += 32) vals[c - c0] = a.xt[g.vec_off + (c - g.col0)];
+      for (int j = tid; j < cn; j += kThreads) {
+        const int c = c0 + j;
+        T v = T(0);
+        if (c < d.ncols) {
+          int lo = 0, hi = d.nseg - 1;  // last segment with col0 <= c
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S[mid].col0 <= c)
+              lo = mid;
+            else
+              hi = mid - 1;
+          }
+          v = a.xt[S[lo].vec_off + (c - S[lo].col0)];
+        }
+        vals[j] = v;
       }
-      for (int c = max(d.ncols, c0) + tid; c < c0 + cn; c += kThreads) vals[c - c0] = T(0);
       __syncthreads();
       const int nv = cn / VEC;
       const VT *E = reinterpret_cast<const VT *>(vals);
