@@ -297,10 +297,48 @@ function status(H::HMatrix)
     return Int(st[])
 end
 
+# ---------------------------------------------------------------------------
+# Row shards for products over several GPUs (row ownership of src/mult.jl:144)
+# ---------------------------------------------------------------------------
+mutable struct Shard{T<:AbstractFloat}
+    handle::Ptr{Cvoid}
+    rows::UnitRange{Int}   # owned rows, 1-based, in the permuted target order
+    n::Int
+end
+
+"""
+    shard(H, rank, world) -> Shard
+
+Shard `rank` (0-based) of `world`: a contiguous range of H's permuted rows with
+the panels and V rows it needs, on the current device. `mul_shard!(y_rows, S,
+x_perm)` computes those rows of H x from x in the permuted source order (all n
+entries, gathered from the ranks first); every row is bitwise H's own.
+"""
+function shard(H::HMatrix{T}, rank::Integer, world::Integer) where {T}
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hmgpu_hmatrix_shard, libhmgpu), Cint, (Ptr{Cvoid}, Int32, Int32, Ref{Ptr{Cvoid}}),
+                H.handle, rank, world, h))
+    b, e = Ref{Int64}(0), Ref{Int64}(0)
+    check(ccall((:hmgpu_shard_rows, libhmgpu), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}), h[], b, e))
+    S = Shard{T}(h[], (b[] + 1):e[], H.n)
+    finalizer(S) do S
+        ccall((:hmgpu_hmatrix_free, libhmgpu), Cint, (Ptr{Cvoid},), S.handle)
+    end
+    return S
+end
+
+function mul_shard!(y_rows::AbstractVector{T}, S::Shard{T}, x_perm::AbstractVector{T}) where {T}
+    length(x_perm) == S.n && length(y_rows) == length(S.rows) ||
+        throw(DimensionMismatch("x_perm has $(length(x_perm)) entries (need $(S.n)), y_rows $(length(y_rows)) (need $(length(S.rows)))"))
+    check(ccall((:hmgpu_matvec_shard, libhmgpu), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                S.handle, _devptr(x_perm), _devptr(y_rows), _stream()))
+    return y_rows
+end
+
 # CUDA.jl hooks, resolved at run time so that this file loads without CUDA.jl.
 _devptr(a) = reinterpret(Ptr{Cvoid}, UInt(Base.unsafe_convert(Main.CUDA.CuPtr{eltype(a)}, a)))
 _stream() = reinterpret(Ptr{Cvoid}, Main.CUDA.stream().handle)
 
-export ClusterTree, HMatrix, info, sparsify_hmatrix, batch, save, load, autotune!, status
+export ClusterTree, HMatrix, info, sparsify_hmatrix, batch, save, load, autotune!, status, shard, mul_shard!
 
 end # module
