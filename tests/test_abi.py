@@ -35,3 +35,12 @@ def test_library_is_in_tree():
     path = _lib._build.LIB
     assert os.path.commonpath([path, REPO]) == REPO
     assert os.path.exists(path)
+
+
+def test_julia_binding_calls_only_declared_symbols():
+    """The Julia binding (julia/HMatrixGB.jl; Julia itself is not installed
+    here) binds only entry points the header declares, by their names."""
+    jl = open(os.path.join(REPO, "hmatrixgpu.jl_gb300", "julia", "HMatrixGB.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(hmgpu_[a-z0-9_]+)", jl))
+    assert len(called) >= 15
+    assert called <= set(declared()), called - set(declared())
