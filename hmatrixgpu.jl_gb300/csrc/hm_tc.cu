@@ -643,6 +643,18 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       const int nch = ((I.ncols > 0 ? (I.ncols + 15) & ~15 : 16) + kKc - 1) / kKc;
       const int span = I.kind != 0 ? kSegChunksV : kSegChunksDU;
       const int nbuf = (nch + span - 1) / span;  // accumulator buffers of the item
+      // the row's factor (1 / rho_i, or gamma_k / nu_k for V rows) and, for y
+      // rows, the output row and the member, loaded now: they do not depend on
+      // the MMA, so their latency hides behind its wait
+      const bool has_row = row < I.m;
+      const float *trailer = reinterpret_cast<const float *>(a.adata + I.a_off + trailer_off(I.m, I.ncols));
+      const float f = has_row ? __ldg(trailer + row) : 0.0f;
+      int64_t yrow = 0;
+      int mem = 0;
+      if (I.kind == 0 && has_row) {
+        yrow = a.tmap0[a.tiles[I.out].row0 + I.row0 + row];
+        mem = __float_as_int(__ldg(trailer + 64));
+      }
       // w[c]: A_part B_hi + A_part B_lo of right-hand side c, chunk by chunk
       float w[R];
 #pragma unroll
@@ -681,15 +693,12 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       for (int c = 0; c < H; c++) v[c] = (lo_part ? w[H + c] : w[c]) + xi[row][c];
       __syncwarp();
       if (lane == 0) arrive(i_free);
-      if (row >= I.m) continue;
-      // the row's factor: 1 / rho_i (kind 0), or gamma_k / nu_k (V rows)
-      const float *trailer = reinterpret_cast<const float *>(a.adata + I.a_off + trailer_off(I.m, I.ncols));
-      const float f = __ldg(trailer + row);
+      if (!has_row) continue;
 #pragma unroll
       for (int c = 0; c < H; c++) v[c] *= f;
       if (I.kind == 0) {
-        float *yr = a.y + a.tmap0[a.tiles[I.out].row0 + I.row0 + row];
-        const float *xs = a.xs_inv + __float_as_int(__ldg(trailer + 64)) * kTcMaxRhs + keep;  // its member's
+        float *yr = a.y + yrow;
+        const float *xs = a.xs_inv + mem * kTcMaxRhs + keep;  // its member's
 #pragma unroll
         for (int c = 0; c < H; c++)
           if (keep + c < a.nr) yr[(keep + c) * a.ldy] = v[c] * __ldg(xs + c);
