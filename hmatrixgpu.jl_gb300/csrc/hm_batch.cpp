@@ -292,7 +292,7 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
     return hm::fail(HMGPU_ERR_NOMEM, std::string("autotune scratch: ") + cudaGetErrorString(e));
   }
   // single-RHS layout parameters and the V schedule
-  const int32_t cand_rows[2] = {8, 16}, cand_kib[3] = {32, 64, 128};
+  const int32_t cand_rows[4] = {8, 16, 32, 64}, cand_kib[3] = {32, 64, 128};
   float t1 = 0.0f;
   best[0] = 16;
   best[1] = 64;
@@ -354,8 +354,8 @@ extern "C" int hmgpu_hmatrix_tuning(const hmgpu_hmatrix *h, int32_t *v, int32_t 
 extern "C" int hmgpu_hmatrix_set_tuning(hmgpu_hmatrix *h, const int32_t *v, int32_t n) {
   if (!h || !v || n < 4) return hm::fail(HMGPU_ERR_INVALID, "need H and 4 values");
   HMatrix &H = *reinterpret_cast<HMatrix *>(h);
-  if ((v[0] != 8 && v[0] != 16) || (v[1] != 32 && v[1] != 64 && v[1] != 128) || v[2] < 2 || (v[3] != 0 && v[3] != 1))
-    return hm::fail(HMGPU_ERR_INVALID, "tuning values out of range (unit rows 8|16, V unit KiB 32|64|128, "
+  if ((v[0] != 8 && v[0] != 16 && v[0] != 32 && v[0] != 64) || (v[1] != 32 && v[1] != 64 && v[1] != 128) || v[2] < 2 || (v[3] != 0 && v[3] != 1))
+    return hm::fail(HMGPU_ERR_INVALID, "tuning values out of range (unit rows 8|16|32|64, V unit KiB 32|64|128, "
                                        "multi-RHS threshold >= 2, V schedule 0|1)");
   return apply(H, v[0], v[1], v[2], v[3]);
 }

@@ -177,7 +177,7 @@ struct Plan {
   std::vector<Seg> segs;
   int64_t panel_len = 0;
   std::vector<RowUnit> units;  // near/U pass work, largest first
-  int32_t unit_rows = 16;      // rows per unit (8 or 16)
+  int32_t unit_rows = 16;      // rows per unit (8, 16, 32 or 64; above 16 only for one-chunk tiles)
   std::vector<int32_t> tile_order;  // tiles by decreasing columns
   std::vector<PackJob> pjobs;
   // V pass

@@ -258,10 +258,11 @@ __global__ void __launch_bounds__(kThreads, 6) v_pass_dyn_kernel(const T *__rest
 }
 
 // ---------------------------------------------------------------------------
-// Near/U pass. CTAs take row units (<= 16 rows of one tile) from a ticket
-// counter, tiles with the most columns first. The CTA gathers the tile's
-// vector entries (x for dense columns, t for rank columns) into shared memory
-// once per unit; then each warp streams one or two whole rows of the tile's
+// Near/U pass. CTAs take row units (rows of one tile) from a ticket counter,
+// tiles with the most columns first. The CTA gathers the tile's vector
+// entries (x for dense columns, t for rank columns) into shared memory once
+// per unit (once per 16 rows when the tile needs several chunks of entries);
+// then each warp streams one or two whole rows of the tile's
 // row-major panel with 16-byte loads (up to 8 in flight per lane) against
 // 16-byte shared-memory loads of the entries, and reduces across lanes with a
 // fixed butterfly. Every lane adds its vectors in increasing column order in
@@ -309,81 +310,89 @@ __global__ void __launch_bounds__(kThreads, 6) du_rows_kernel(DuArgs<T> a) {
     if (seg_smem)
       for (int s = tid; s < d.nseg; s += kThreads) ssegs[s] = a.segs[d.seg0 + s];
     const Seg *S = seg_smem ? ssegs : a.segs + d.seg0;
-    const int ia = U.i0 + warp, ib = ia + kThreads / 32;
-    const bool ha = ia < U.i1, hb = ib < U.i1;
-    RowAcc<T, COMP> ra, rb;
-    for (int c0 = 0; c0 < d.ld; c0 += CH) {
-      const int cn = min(CH, d.ld - c0);
-      __syncthreads();  // segments loaded / previous chunk's entries no longer read
-      for (int j = tid; j < cn; j += kThreads) {
-        const int c = c0 + j;
-        T v = T(0);
-        if (c < d.ncols) {
-          int lo = 0, hi = d.nseg - 1;  // last segment with col0 <= c
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (S[mid].col0 <= c)
-              lo = mid;
-            else
-              hi = mid - 1;
+    // Rows 16 at a time (a warp per row pair); a unit has more than 16 rows
+    // only when its tile fits one chunk of entries, which are then gathered
+    // once for all its rows.
+    const bool single = d.ld <= CH;
+    for (int r0 = U.i0; r0 < U.i1; r0 += kThreads / 16) {
+      const int ia = r0 + warp, ib = ia + kThreads / 32;
+      const bool ha = ia < U.i1, hb = ib < U.i1;
+      RowAcc<T, COMP> ra, rb;
+      for (int c0 = 0; c0 < d.ld; c0 += CH) {
+        const int cn = min(CH, d.ld - c0);
+        if (!single || r0 == U.i0) {
+          __syncthreads();  // segments loaded / previous chunk's entries no longer read
+          for (int j = tid; j < cn; j += kThreads) {
+            const int c = c0 + j;
+            T v = T(0);
+            if (c < d.ncols) {
+              int lo = 0, hi = d.nseg - 1;  // last segment with col0 <= c
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (S[mid].col0 <= c)
+                  lo = mid;
+                else
+                  hi = mid - 1;
+              }
+              v = a.xt[S[lo].vec_off + (c - S[lo].col0)];
+            }
+            vals[j] = v;
           }
-          v = a.xt[S[lo].vec_off + (c - S[lo].col0)];
+          __syncthreads();
         }
-        vals[j] = v;
+        const int nv = cn / VEC;
+        const VT *E = reinterpret_cast<const VT *>(vals);
+        const VT *RA = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ia) * d.ld + c0);
+        const VT *RB = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ib) * d.ld + c0);
+        if (ha && hb) {
+          int p = lane;
+          for (; p + 96 < nv; p += 128) {
+            const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
+            const VT x2 = ld_stream(RA + p + 64), x3 = ld_stream(RA + p + 96);
+            const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
+            const VT z2 = ld_stream(RB + p + 64), z3 = ld_stream(RB + p + 96);
+            const VT e0 = E[p], e1 = E[p + 32], e2 = E[p + 64], e3 = E[p + 96];
+            ra.add(x0, e0);
+            ra.add(x1, e1);
+            ra.add(x2, e2);
+            ra.add(x3, e3);
+            rb.add(z0, e0);
+            rb.add(z1, e1);
+            rb.add(z2, e2);
+            rb.add(z3, e3);
+          }
+          for (; p + 32 < nv; p += 64) {
+            const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
+            const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
+            const VT e0 = E[p], e1 = E[p + 32];
+            ra.add(x0, e0);
+            ra.add(x1, e1);
+            rb.add(z0, e0);
+            rb.add(z1, e1);
+          }
+          if (p < nv) {
+            const VT e0 = E[p];
+            ra.add(ld_stream(RA + p), e0);
+            rb.add(ld_stream(RB + p), e0);
+          }
+        } else if (ha) {
+          int p = lane;
+          for (; p + 96 < nv; p += 128) {
+            const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
+            const VT x2 = ld_stream(RA + p + 64), x3 = ld_stream(RA + p + 96);
+            ra.add(x0, E[p]);
+            ra.add(x1, E[p + 32]);
+            ra.add(x2, E[p + 64]);
+            ra.add(x3, E[p + 96]);
+          }
+          for (; p < nv; p += 32) ra.add(ld_stream(RA + p), E[p]);
+        }
       }
-      __syncthreads();
-      const int nv = cn / VEC;
-      const VT *E = reinterpret_cast<const VT *>(vals);
-      const VT *RA = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ia) * d.ld + c0);
-      const VT *RB = reinterpret_cast<const VT *>(a.panels + d.data_off + static_cast<int64_t>(ib) * d.ld + c0);
-      if (ha && hb) {
-        int p = lane;
-        for (; p + 96 < nv; p += 128) {
-          const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
-          const VT x2 = ld_stream(RA + p + 64), x3 = ld_stream(RA + p + 96);
-          const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
-          const VT z2 = ld_stream(RB + p + 64), z3 = ld_stream(RB + p + 96);
-          const VT e0 = E[p], e1 = E[p + 32], e2 = E[p + 64], e3 = E[p + 96];
-          ra.add(x0, e0);
-          ra.add(x1, e1);
-          ra.add(x2, e2);
-          ra.add(x3, e3);
-          rb.add(z0, e0);
-          rb.add(z1, e1);
-          rb.add(z2, e2);
-          rb.add(z3, e3);
-        }
-        for (; p + 32 < nv; p += 64) {
-          const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
-          const VT z0 = ld_stream(RB + p), z1 = ld_stream(RB + p + 32);
-          const VT e0 = E[p], e1 = E[p + 32];
-          ra.add(x0, e0);
-          ra.add(x1, e1);
-          rb.add(z0, e0);
-          rb.add(z1, e1);
-        }
-        if (p < nv) {
-          const VT e0 = E[p];
-          ra.add(ld_stream(RA + p), e0);
-          rb.add(ld_stream(RB + p), e0);
-        }
-      } else if (ha) {
-        int p = lane;
-        for (; p + 96 < nv; p += 128) {
-          const VT x0 = ld_stream(RA + p), x1 = ld_stream(RA + p + 32);
-          const VT x2 = ld_stream(RA + p + 64), x3 = ld_stream(RA + p + 96);
-          ra.add(x0, E[p]);
-          ra.add(x1, E[p + 32]);
-          ra.add(x2, E[p + 64]);
-          ra.add(x3, E[p + 96]);
-        }
-        for (; p < nv; p += 32) ra.add(ld_stream(RA + p), E[p]);
+      const T ya = ra.total(), yb = rb.total();
+      if (lane == 0) {
+        if (ha) a.y[a.tmap0[d.row0 + ia]] = ya;
+        if (hb) a.y[a.tmap0[d.row0 + ib]] = yb;
       }
-    }
-    const T ya = ra.total(), yb = rb.total();
-    if (lane == 0) {
-      if (ha) a.y[a.tmap0[d.row0 + ia]] = ya;
-      if (hb) a.y[a.tmap0[d.row0 + ib]] = yb;
     }
   }
 }

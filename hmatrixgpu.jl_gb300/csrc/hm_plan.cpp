@@ -37,9 +37,13 @@ static inline int64_t round_up(int64_t a, int64_t b) { return (a + b - 1) / b * 
 void make_units(Plan &p, int32_t unit_rows) {
   p.units.clear();
   p.unit_rows = unit_rows;
+  // units of more than 16 rows only for tiles whose entries fit one
+  // shared-memory chunk of the near/U pass (16 KB: 1024 16-byte vectors)
+  const int64_t chunk_cols = 1024 * static_cast<int64_t>(p.vec);
   for (int32_t ti : p.tile_order) {
     const TileDesc &d = p.tiles[ti];
-    const int32_t parts = (d.m + unit_rows - 1) / unit_rows;
+    const int32_t ur = unit_rows > 16 && d.ld > chunk_cols ? 16 : unit_rows;
+    const int32_t parts = (d.m + ur - 1) / ur;
     for (int32_t q = 0; q < parts; q++) {
       // near-equal row runs
       int32_t i0 = static_cast<int32_t>(static_cast<int64_t>(d.m) * q / parts);

@@ -344,7 +344,9 @@ int hmgpu_graph_launch(hmgpu_graph *G, void *stream);
 int hmgpu_graph_free(hmgpu_graph *G);
 
 /* Times the product's free parameters on H's own data (about a second of
- * products) and keeps the fastest: rows per near/U unit (8 or 16), bytes per
+ * products) and keeps the fastest: rows per near/U unit (8, 16, 32 or 64;
+ * units above 16 rows only for tiles whose vector entries fit one 16 KB
+ * shared-memory chunk, which a unit then gathers once), bytes per
  * V unit (32, 64 or 128 KiB), the V schedule (see hmgpu_hmatrix_tuning) and
  * the number of right-hand sides from which one multi-RHS pass replaces
  * repeated single-RHS products. None of them changes
