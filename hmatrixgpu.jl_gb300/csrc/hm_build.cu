@@ -821,8 +821,8 @@ struct Compressor {
   int svd;
   int64_t budget;  // doubles of workspace per batch
   int grid_aca = 1, grid_qr = 1, grid_form = 1;
-  // continuation: batches fill 3/4 of the budget, and a block that fills its
-  // workspace goes on in the last quarter, from its state, in the same batch
+  // continuation: the workspace holds a quarter more than a batch fills, and a
+  // block that fills its own goes on there, from its state, in the same batch
   bool resume = false;
   int64_t batches = 0, ws_bytes = 0, continued = 0;  // statistics of all run() calls
 
@@ -897,9 +897,9 @@ struct Compressor {
     size_t pos = 0;
     DevBuf ws, djobs, dres, dtick, duo, dvo, dcj, dcr;
     if (int rc = dtick.alloc(8 * sizeof(int32_t))) return rc;
-    const int64_t fill = resume ? budget / 4 * 3 : budget;
-    if (resume)
-      if (int rc = ws.reserve(budget * sizeof(double))) return rc;
+    const int64_t fill = budget;
+    if (resume)  // a quarter more than the batches fill, for the continued blocks
+      if (int rc = ws.reserve((budget + budget / 4) * sizeof(double))) return rc;
     while (pos < sel.size()) {
       std::vector<AcaJob> batch;
       std::vector<int> ids;
