@@ -72,15 +72,15 @@ def test_svd_recompress_random(gpu):
         np.testing.assert_array_equal(Vs, Vo)
 
 
-def _oracle_h(kind, P, leaf, eta, eps, dims=1):
+def _oracle_h(kind, P, leaf, eta, eps, dims=1, dims_x=1):
     K = O.Kernel(kind, P.T, P.T)
-    X = O.Tree(P.T, leaf)
+    X = O.Tree(P.T, leaf, dims_x)
     Y = O.Tree(P.T, leaf, dims)
     return K, O.HMatrix(K, X, Y, eta=eta, eps=eps, nthreads=8)
 
 
-def _dev_h(kind, P, leaf, eta, eps, dims=1, precision="f64", **kw):
-    X = hmgpu.ClusterTree(P, max_points_per_leaf=leaf)
+def _dev_h(kind, P, leaf, eta, eps, dims=1, precision="f64", dims_x=1, **kw):
+    X = hmgpu.ClusterTree(P, max_points_per_leaf=leaf, dims=dims_x)
     Y = hmgpu.ClusterTree(P, max_points_per_leaf=leaf, dims=dims)
     return hmgpu.HMatrix(hmgpu.Kernel(kind, P), X, Y, eta=eta, eps=eps, precision=precision, **kw)
 
@@ -113,6 +113,8 @@ PARITY_CASES = {
     "cube4096": ("laplace", lambda: geometry.cube(4096, seed=0), 32, 2.0, 1e-6, 1),
     "sphere": ("laplace", lambda: geometry.sphere(6000, seed=2), 32, 1.5, 1e-5, 1),
     "film128": ("laplace", lambda: geometry.film(128, 128), 64, 2.0, 1e-4, 1),
+    # the demagnetising tensor (3 x 3 per point pair, both trees with dims = 3)
+    "dipolar": ("dipolar", lambda: geometry.cube(1200, seed=3), 16, 1.0, 1e-6, 3),
 }
 
 
@@ -125,9 +127,10 @@ def test_partition_and_ranks_match_oracle(gpu, case):
     The film case has blocks with m + n >= 4096, which a whole CTA works on."""
     import torch
     kind, pts, leaf, eta, eps, dims = PARITY_CASES[case]
+    dims_x = 3 if kind == "dipolar" else 1
     P = pts()
-    K, Ho = _oracle_h(kind, P, leaf, eta, eps, dims)
-    H = _dev_h(kind, P, leaf, eta, eps, dims, keep_factors=True)
+    K, Ho = _oracle_h(kind, P, leaf, eta, eps, dims, dims_x)
+    H = _dev_h(kind, P, leaf, eta, eps, dims, dims_x=dims_x, keep_factors=True)
     d, a = H.blocks()
     # dense list: tree dense leaves, then admissible leaves that did not compress
     np.testing.assert_array_equal(d, Ho.dense_block_indices[:, :4])
