@@ -240,7 +240,7 @@ def bench_config(n):
             "parallelism": "1 GPU"}
 
 
-def cube_measurement(dev, steps, hbm):
+def cube_measurement(dev, steps, hbm, npts=1 << 18):
     """The plain drop-in case: N = 2^18 points uniform in [0,1]^3, Laplace
     1/(4 pi r), leaf 64, eta 2, tol 1e-6, FP32 storage, one RHS. Device build
     (trees included), autotuned layout, product time with its phases, the
@@ -250,7 +250,7 @@ def cube_measurement(dev, steps, hbm):
 
     import hmgpu
     from tests import geometry
-    P = geometry.cube(1 << 18, seed=2)
+    P = geometry.cube(npts, seed=2)
     n = P.shape[1]
     t0 = time.time()
     T = hmgpu.ClusterTree(P, max_points_per_leaf=64, gpu=True)
@@ -363,7 +363,7 @@ def cube_measurement(dev, steps, hbm):
            "rel_err_256_exact_rows": float(np.linalg.norm(y64h[rows] - exact) / np.linalg.norm(exact)),
            "rel_diff_vs_f32": float(np.linalg.norm(y64h - ys) / np.linalg.norm(y64h))}
     del H64
-    return {"workload": "cube-2^18 Laplace leaf64 eta2 tol1e-6, 1 RHS, FP32 storage",
+    return {"workload": f"cube-{npts} Laplace leaf64 eta2 tol1e-6, 1 RHS, FP32 storage",
             "build_seconds": build, "build": H.build_profile(), "autotuned": tune,
             "dense_entries": inf["dense_entries"], "far_entries": inf["far_entries"],
             "lowrank_blocks": inf["admissible_leaves"], "dense_blocks": inf["full_leaves"],
@@ -652,7 +652,7 @@ def run_gpu(args):
     du_ms = ph[2]
     achieved = du_bytes / (du_ms * 1e-3) / 1e9
     batch32 = None if args.skip_batch else batch_measurement(dev, args.steps)
-    cube18 = None if args.skip_cube else cube_measurement(dev, args.steps, hbm)
+    cube18 = None if args.skip_cube else cube_measurement(dev, args.steps, hbm, args.cube_points)
     learned = learned_measurement(dev) if args.learned else None
     cores = os.cpu_count() or 1
     cpu_runs, cpu_desc = cpu_product([(1, 1, 4)] + ([(cores, 3, 10)] if cores > 1 else []))
@@ -708,6 +708,8 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="leave out the 32-H-matrix batch lines")
     ap.add_argument("--build-only", action="store_true", help="assemble the workload, print its build line, exit")
     ap.add_argument("--skip-cube", action="store_true", help="leave out the 2^18-cube tol 1e-6 line")
+    ap.add_argument("--cube-points", type=int, default=1 << 18,
+                    help="points of the cube case (2^18 = the plain drop-in workload; smaller for profiling captures)")
     ap.add_argument("--learned", action="store_true",
                     help="also assemble the 2^20 cube (tol 1e-4) without and with the learned rank predictor")
     args = ap.parse_args()
