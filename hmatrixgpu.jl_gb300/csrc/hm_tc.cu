@@ -21,38 +21,46 @@
 // The right-hand sides live in XTS, one row per entry of XT = [x permuted |
 // t]: R FP16 hi values, then R lo values (4R bytes).
 //
-// Pipeline (one persistent CTA per SM; items from a ticket counter, in list
+// Pipelines (one persistent CTA per SM; items from a ticket counter, in list
 // order, so concurrent CTAs work on neighbouring panels and share XTS rows in
-// L2; warp 0 takes the tickets and queues them for the other roles):
+// L2; warp 0 takes the tickets and queues them for the other roles). A 32-wide
+// pass runs two pipelines, item n in pipeline n & 1; they share the tensor
+// cores but have their own stages, producers, MMA warp and epilogue set,
+// because one MMA warp's own instructions per chunk bound a pipeline. A
+// 64-wide pass runs one (every item in pipeline 0), whose epilogue sets still
+// take every other item:
 //   warp 0      item tickets (lane 0), queued in shared memory for the others;
-//   producers   warps 1, 3 and 8.. (one per stage; chunk g to producer g mod
-//               the stage count) of a ring of 64-column chunks: two bulk
-//               copies of the chunk that complete on the stage's mbarrier (hi
-//               rows to tile rows 0..63, lo rows to tile rows 64..127), and
-//               the XTS rows of its columns (whole rows) as an N-major
-//               (MN-major) FP16 tile: for a V piece, whose columns are
-//               consecutive rows, one TMA tile load of 64 rows on the same
+//   producers   warps 1, 3 and 8.. (one per stage; producer b serves pipeline
+//               b mod kPipes, and the pipeline's chunk g goes to its producer
+//               g mod kPipeStages) of each pipeline's ring of 64-column
+//               chunks: two bulk copies of the chunk that complete on the
+//               stage's mbarrier (hi rows to tile rows 0..63, lo rows to tile
+//               rows 64..127), and the XTS rows of its columns (whole rows) as
+//               an N-major (MN-major) FP16 tile: for a V piece, whose columns
+//               are consecutive rows, one TMA tile load of 64 rows on the same
 //               barrier; for a row tile, one 8-row TMA tile load per K group
 //               of 8 columns that are 8 consecutive rows (the runs of whole
 //               source clusters and rank ranges), 16-byte cp.async gathers
 //               for the other groups (padding columns read the zero row),
 //               then a wait, a proxy fence and an mbarrier arrive;
-//   warp 2      MMA issuer (one elected lane): per 16 columns one UMMA,
+//   MMA         warp 2 (pipeline 0) and, in a 32-wide pass, the last warp
+//               (pipeline 1); one elected lane each: per 16 columns one UMMA,
 //               [A_hi; A_lo] x [B_hi B_lo] with M = 128, N = 2R (hi and lo
 //               stacked along both M and N; items have at most 64 rows), into
 //               a fresh TMEM accumulator buffer (FP32) every kSegChunks
 //               chunks; commits free the stage and hand each buffer to the
-//               item's epilogue set. In a V piece's last chunk it first zeroes
-//               the B rows of padding columns (other blocks' XTS rows, which
-//               the 64-row tile load brought in: 0 * Inf must not reach a sum);
-//   epilogue    two sets of 4 warps (warps 4-7 and the last four), set e for
-//               every other item: per accumulator buffer, tcgen05.ld of the
-//               warp's 32 TMEM lanes added to FP32 registers; at the item's
-//               end the sum of the four hi/lo quadrants (the hi-row and
-//               lo-row warps of the same rows swap halves of their sums, so
-//               each finishes half of the right-hand sides), the scales
-//               undone, then y rows, t rows of XTS (split again) or partial
-//               rows P.
+//               item's epilogue set. In a V piece's last chunk it first
+//               zeroes the B rows of padding columns (other blocks' XTS rows,
+//               which the 64-row tile load brought in: 0 * Inf must not reach
+//               a sum);
+//   epilogue    two sets of 4 warps (warps 4-7 and the four after the last
+//               producer), set e for items n with n & 1 == e: per
+//               accumulator buffer, tcgen05.ld of the warp's 32 TMEM lanes
+//               added to FP32 registers; at the item's end the sum of the
+//               four hi/lo quadrants (the hi-row and lo-row warps of the same
+//               rows swap halves of their sums, so each finishes half of the
+//               right-hand sides), the scales undone, then y rows, t rows of
+//               XTS (split again) or partial rows P.
 // Every wait is bounded by the global timer; one that runs out records a code
 // in `status`, raises a CTA-wide abort flag and every role leaves its loop.
 #include <cuda.h>
@@ -97,16 +105,22 @@ struct TcShape {
   static constexpr int kBN = 2 * R;                   // B rows: R hi, then R lo
   static constexpr int kBBytes = kBN * kKc * 2;       // one FP16 B tile: 8 or 16 KB
   static constexpr int kStages = R == 32 ? 8 : 6;
-  static constexpr int kBProducers = kStages;         // warps 1, 3, 8 .. 5 + kStages
-  static constexpr int kEpi1 = 6 + kBProducers;       // first warp of the second epilogue set
-  static constexpr int kWarps = kEpi1 + 4;            // roles: see the header comment
+  // Two pipelines for 32 right-hand sides. A 64-wide pass keeps one: a 17th
+  // warp would cap every thread at 96 registers (warps per scheduler x
+  // threads x registers), and its epilogue needs more for 64 sums a row.
+  static constexpr int kPipes = R == 32 ? 2 : 1;
+  static constexpr int kPipeStages = kStages / kPipes;  // stages of each pipeline
+  static constexpr int kBProducers = kStages;           // warps 1, 3, 8 .. 5 + kStages
+  static constexpr int kEpi1 = 6 + kBProducers;         // first warp of the second epilogue set
+  static constexpr int kMma1 = kEpi1 + 4;               // MMA warp of the second pipeline, if any
+  static constexpr int kWarps = kMma1 + kPipes - 1;     // roles: see the header comment
   static constexpr int kThreads = kWarps * 32;
   // TMEM: every column of the SM's 512, cut into accumulator buffers of kBN
   // columns, half of them for each epilogue set
   static constexpr uint32_t kTmemCols = 512;
   static constexpr int kBufs = static_cast<int>(kTmemCols) / kBN;  // 8 or 4
   static constexpr int kSetBufs = kBufs / 2;
-  static constexpr int kConsumers = kBProducers + 1 + 8;  // warps that read each queued item
+  static constexpr int kConsumers = kBProducers + kPipes + 8;  // warps that read each queued item
   static constexpr uint32_t kBGroupK = (kBN / 8) * kBGroupN;
   static constexpr int kPieces = R / 4;               // 16-byte pieces of an XTS row
   static constexpr int kRowsPerCopy = 32 / kPieces;   // XTS rows per warp-wide copy
@@ -118,6 +132,8 @@ struct TcShape {
   // one release ahead, which a parity wait on the stage's barrier could not
   // tell apart from the release before.
   static_assert(kBProducers == kStages, "one producer warp per stage");
+  // the MMA warp waits for a whole segment's chunks before it releases any
+  static_assert(kSegChunksDU <= kPipeStages && kSegChunksV <= kPipeStages, "a segment fits a pipeline's stages");
 };
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr unsigned long long kWaitIters = 1ull << 26;   // backstop if the timer stood still
@@ -418,22 +434,25 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       }
     }
   } else if (warp == 1 || warp == 3 || (warp >= 8 && warp < Sh::kEpi1)) {
-    // ---- producers: chunk g (stage g % kStages) goes to producer g % kStages --
-    // Column rows are looked up before the stage is free; then each warp-wide
-    // copy moves kRowsPerCopy whole XTS rows (kPieces lanes x 16 bytes per
-    // row), the warp waits for its copies, fences them for the tensor cores'
-    // proxy and publishes the stage.
+    // ---- producers: pipeline p = bw & 1 (items n with n & 1 == p); its chunk
+    // g (stage p kPipeStages + g % kPipeStages) goes to its producer
+    // q = g % kPipeStages. Column rows are looked up before the stage is
+    // free; then each warp-wide copy moves kRowsPerCopy whole XTS rows
+    // (kPieces lanes x 16 bytes per row), the warp waits for its copies,
+    // fences them for the tensor cores' proxy and publishes the stage.
     const int bw = warp == 1 ? 0 : warp == 3 ? 1 : warp - 6;  // 0..kStages-1
+    const int pipe = bw % Sh::kPipes, q = bw / Sh::kPipes;
     int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
     bool stop = false;
     const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
     for (int n = 0; !stop; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
+      if ((n & 1) % Sh::kPipes != pipe) continue;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
-        if (g % kStages != bw) continue;
-        const int kc = min(kKc, npad - c0), s = static_cast<int>(g % kStages);
+        if (g % Sh::kPipeStages != q) continue;
+        const int kc = min(kKc, npad - c0), s = pipe * Sh::kPipeStages + static_cast<int>(g % Sh::kPipeStages);
         // B of a V piece by one tile load of 64 XTS rows (in a last chunk the
         // MMA warp zeroes the rows of padding columns before it multiplies)
         const bool tma_b = I.kind != 0;
@@ -464,7 +483,7 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           }
           gmask &= (1u << (kc / 8)) - 1u;
         }
-        if (!wait_bar_warp(S, &S.empty[s], static_cast<uint32_t>((g / kStages) & 1) ^ 1u, a.status, 22)) {
+        if (!wait_bar_warp(S, &S.empty[s], static_cast<uint32_t>((g / Sh::kPipeStages) & 1) ^ 1u, a.status, 22)) {
           stop = true;
           break;
         }
@@ -540,15 +559,20 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // aborted or not (one stage per producer: earlier chunks have landed).
     if (last_g >= 0 && lane == 0) {
       volatile int32_t none = 0;
-      wait_bar_bounded(&S.full[last_g % kStages], static_cast<uint32_t>((last_g / kStages) & 1), &none, a.status, 31,
-                       kWaitNs);
+      wait_bar_bounded(&S.full[pipe * Sh::kPipeStages + last_g % Sh::kPipeStages],
+                       static_cast<uint32_t>((last_g / Sh::kPipeStages) & 1), &none, a.status, 31, kWaitNs);
     }
     __syncwarp();
-  } else if (warp == 2) {
-    // ---- MMA issuer: the warp runs the loop, one elected lane issues --------
+  } else if (warp == 2 || (Sh::kPipes == 2 && warp == Sh::kMma1)) {
+    // ---- MMA issuers: one warp per pipeline, one elected lane issues. The
+    // issuing warp's own instructions per chunk (waits, fence, election,
+    // UMMAs, commits) bound a single pipeline, so with two pipelines, each
+    // with its own stages, they share the tensor cores.
     // Per 16 columns one UMMA: [A_hi; A_lo] (M = 128) x [B_hi B_lo] (N = 2R)
     // into the item's accumulator; the epilogue adds its four quadrants.
-    int64_t g = 0;
+    const int pipe = warp == 2 ? 0 : 1;
+    const int s0 = pipe * Sh::kPipeStages;  // the pipeline's first stage
+    int64_t g = 0;                          // the pipeline's chunks so far
     int n = 0;
     bool stop = false;
     // Every kSegChunks chunks of an item go to a fresh accumulator buffer of
@@ -560,33 +584,42 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     for (; !stop; n++) {
       TcItem I;
       if (!next_item(S, n, a.status, I)) break;
-      const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
+      if ((n & 1) % Sh::kPipes != pipe) continue;
       const int e = n & 1;
+      const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       // V pieces' B tiles come from the tile load (K groups 128 B apart, N
       // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
       const bool tma_b = I.kind != 0;
       const int kSegChunks = tma_b ? kSegChunksV : kSegChunksDU;
-      for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
-        const int kc = min(kKc, npad - c0), st = static_cast<int>(g % kStages);
-        const int ci = c0 / kKc;  // chunk of the item
-        const bool first = ci % kSegChunks == 0, last = ci % kSegChunks == kSegChunks - 1 || c0 + kKc >= npad;
+      // One pass of this loop per accumulator buffer: the segment's chunks
+      // c0 / kKc .. + nseg - 1 (stages g .. g + nseg - 1) are waited for
+      // first, then all their UMMAs go out under one fence and one election.
+      // The warp's own per-chunk instructions are what bound the pass, so
+      // they are paid once per segment. nseg <= kPipeStages: the producers of
+      // the segment's chunks never wait for the segment itself.
+      for (int c0 = 0; c0 < npad;) {
+        const int nseg = min(kSegChunks, (npad - c0 + kKc - 1) / kKc);
         const int buf = e * Sh::kSetBufs + static_cast<int>(kseg[e] % Sh::kSetBufs);
-        if ((first && !wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23)) ||
-            !wait_bar_warp(S, &S.full[st], static_cast<uint32_t>((g / kStages) & 1), a.status, 24)) {
+        bool ok = wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23);
+        for (int j = 0; ok && j < nseg; j++)
+          ok = wait_bar_warp(S, &S.full[s0 + static_cast<int>((g + j) % Sh::kPipeStages)],
+                             static_cast<uint32_t>(((g + j) / Sh::kPipeStages) & 1), a.status, 24);
+        if (!ok) {
           stop = true;
           break;
         }
-        if (tma_b && I.ncols - c0 < kc) {
+        const int cl = c0 + (nseg - 1) * kKc, kcl = min(kKc, npad - cl);  // the segment's last chunk
+        if (tma_b && I.ncols - cl < kcl) {
           // the last chunk of a V piece: the tile load brought 64 consecutive
           // XTS rows, and those of the padding columns [ncols, kc) belong to
           // other blocks (or are t rows being rewritten). The A tile is zero
           // there, but 0 * Inf and 0 * NaN are not, so the rows are zeroed
           // (16 bytes per row and N group) before the UMMAs read them.
-          const int valid = I.ncols - c0, nz = kc - valid;
+          const uint32_t bl = su32(S.b[s0 + static_cast<int>((g + nseg - 1) % Sh::kPipeStages)]);
+          const int valid = I.ncols - cl, nz = kcl - valid;
           for (int z = lane; z < nz * (Sh::kBN / 8); z += 32) {
             const int k = valid + z % nz, gq = z / nz;
-            asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(su32(S.b[st]) + gq * 1024u + k * 16u),
-                         "r"(0u)
+            asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(bl + gq * 1024u + k * 16u), "r"(0u)
                          : "memory");
           }
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -595,26 +628,36 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (elect_one()) {
           const uint32_t acc = S.tmem + static_cast<uint32_t>(buf * Sh::kBN);
-          // leading byte offset: K direction; stride byte offset: N direction
-          const uint64_t da = sdesc(su32(S.a[st]), 128, static_cast<uint32_t>(kc) * 16);
-          const uint64_t db = tma_b ? sdesc(su32(S.b[st]), 128, 1024) : sdesc(su32(S.b[st]), Sh::kBGroupK, kBGroupN);
-          for (int ks = 0; ks < kc / 16; ks++) {
-            // the start address field counts 16-byte units
-            const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
-                           ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
-            mma(acc, da + oa, db + ob, Sh::kIdesc, (first && ks == 0) ? 0u : 1u);
+          for (int j = 0; j < nseg; j++) {
+            const int st = s0 + static_cast<int>((g + j) % Sh::kPipeStages), kc = min(kKc, npad - c0 - j * kKc);
+            // leading byte offset: K direction; stride byte offset: N direction
+            const uint64_t da = sdesc(su32(S.a[st]), 128, static_cast<uint32_t>(kc) * 16);
+            const uint64_t db =
+                tma_b ? sdesc(su32(S.b[st]), 128, 1024) : sdesc(su32(S.b[st]), Sh::kBGroupK, kBGroupN);
+#pragma unroll
+            for (int ks = 0; ks < kKc / 16; ks++) {
+              if (ks < kc / 16) {
+                // the start address field counts 16-byte units
+                const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
+                               ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
+                mma(acc, da + oa, db + ob, Sh::kIdesc, (j == 0 && ks == 0) ? 0u : 1u);
+              }
+            }
+            commit(&S.empty[st]);
           }
-          commit(&S.empty[st]);
-          if (last) commit(&S.seg_full[buf]);
+          commit(&S.seg_full[buf]);
         }
         __syncwarp();
-        if (last) kseg[e]++;
+        kseg[e]++;
+        g += nseg;
+        c0 += nseg * kKc;
       }
     }
     // the last stage release must land before the CTA's shared memory goes away
     if (!stop && g > 0)
-      wait_bar_warp(S, &S.empty[(g - 1) % kStages], static_cast<uint32_t>(((g - 1) / kStages) & 1), a.status, 26);
-  } else if ((warp >= 4 && warp < 8) || warp >= Sh::kEpi1) {
+      wait_bar_warp(S, &S.empty[s0 + static_cast<int>((g - 1) % Sh::kPipeStages)],
+                    static_cast<uint32_t>(((g - 1) / Sh::kPipeStages) & 1), a.status, 26);
+  } else if ((warp >= 4 && warp < 8) || (warp >= Sh::kEpi1 && warp < Sh::kEpi1 + 4)) {
     // ---- epilogue -----------------------------------------------------------
     // Set e (warps 4-7 or the last four) takes accumulator e, that is items
     // n = e, e + 2, ... Warp w reads TMEM lanes 32(w mod 4)..: quarters 0, 1
