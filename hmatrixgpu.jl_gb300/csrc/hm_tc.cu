@@ -132,8 +132,10 @@ struct TcShape {
   // one release ahead, which a parity wait on the stage's barrier could not
   // tell apart from the release before.
   static_assert(kBProducers == kStages, "one producer warp per stage");
-  // the MMA warp waits for a whole segment's chunks before it releases any
-  static_assert(kSegChunksDU <= kPipeStages && kSegChunksV <= kPipeStages, "a segment fits a pipeline's stages");
+  // the MMA warp waits for all chunks of a pass (a segment, or two chunks)
+  // before it releases any
+  static_assert(kSegChunksDU <= kPipeStages && kSegChunksV <= kPipeStages && kPipeStages >= 2,
+                "a pass fits a pipeline's stages");
 };
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr unsigned long long kWaitIters = 1ull << 26;   // backstop if the timer stood still
@@ -548,9 +550,12 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
                          : "memory");
           }
         }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        // the gathers complete on the stage's barrier as well: each lane's
+        // cp.async.mbarrier.arrive adds a pending arrival that lands once the
+        // lane's copies have, so the warp goes on to its next chunk at once
+        // (the MMA warp fences them for the tensor cores' proxy after its
+        // wait). Every lane registers before lane 0's own arrival.
+        asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(su32(&S.full[s])) : "memory");
         __syncwarp();
         if (lane == 0) arrive(&S.full[s]);
       }
@@ -591,31 +596,36 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
       // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
       const bool tma_b = I.kind != 0;
       const int kSegChunks = tma_b ? kSegChunksV : kSegChunksDU;
-      // One pass of this loop per accumulator buffer: the segment's chunks
-      // c0 / kKc .. + nseg - 1 (stages g .. g + nseg - 1) are waited for
+      // One pass of this loop per `nit` chunks c0 / kKc .. + nit - 1 (stages
+      // g .. g + nit - 1, accumulator buffers kseg .. + nb - 1, a fresh one
+      // every kSegChunks chunks): their buffers and stages are waited for
       // first, then all their UMMAs go out under one fence and one election.
-      // The warp's own per-chunk instructions are what bound the pass, so
-      // they are paid once per segment. nseg <= kPipeStages: the producers of
-      // the segment's chunks never wait for the segment itself.
+      // The warp's own instructions per pass are what bound a pipeline, so a
+      // pass takes two chunks where a set has buffers to spare. nit <=
+      // kPipeStages: the producers of the pass's chunks never wait for it.
+      const int kIter = kSegChunks > 1 ? kSegChunks : (Sh::kSetBufs >= 4 ? 2 : 1);
       for (int c0 = 0; c0 < npad;) {
-        const int nseg = min(kSegChunks, (npad - c0 + kKc - 1) / kKc);
-        const int buf = e * Sh::kSetBufs + static_cast<int>(kseg[e] % Sh::kSetBufs);
-        bool ok = wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23);
-        for (int j = 0; ok && j < nseg; j++)
+        const int nit = min(kIter, (npad - c0 + kKc - 1) / kKc);
+        const int nb = (nit + kSegChunks - 1) / kSegChunks;
+        auto buf_of = [&](int b) { return e * Sh::kSetBufs + static_cast<int>((kseg[e] + b) % Sh::kSetBufs); };
+        bool ok = true;
+        for (int b = 0; ok && b < nb; b++)
+          ok = wait_bar_warp(S, &S.seg_empty[buf_of(b)], (((kseg[e] + b) / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23);
+        for (int j = 0; ok && j < nit; j++)
           ok = wait_bar_warp(S, &S.full[s0 + static_cast<int>((g + j) % Sh::kPipeStages)],
                              static_cast<uint32_t>(((g + j) / Sh::kPipeStages) & 1), a.status, 24);
         if (!ok) {
           stop = true;
           break;
         }
-        const int cl = c0 + (nseg - 1) * kKc, kcl = min(kKc, npad - cl);  // the segment's last chunk
+        const int cl = c0 + (nit - 1) * kKc, kcl = min(kKc, npad - cl);  // the pass's last chunk
         if (tma_b && I.ncols - cl < kcl) {
           // the last chunk of a V piece: the tile load brought 64 consecutive
           // XTS rows, and those of the padding columns [ncols, kc) belong to
           // other blocks (or are t rows being rewritten). The A tile is zero
           // there, but 0 * Inf and 0 * NaN are not, so the rows are zeroed
           // (16 bytes per row and N group) before the UMMAs read them.
-          const uint32_t bl = su32(S.b[s0 + static_cast<int>((g + nseg - 1) % Sh::kPipeStages)]);
+          const uint32_t bl = su32(S.b[s0 + static_cast<int>((g + nit - 1) % Sh::kPipeStages)]);
           const int valid = I.ncols - cl, nz = kcl - valid;
           for (int z = lane; z < nz * (Sh::kBN / 8); z += 32) {
             const int k = valid + z % nz, gq = z / nz;
@@ -625,32 +635,36 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
         }
+        // gathered B rows were written through the generic proxy
+        if (!tma_b) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (elect_one()) {
-          const uint32_t acc = S.tmem + static_cast<uint32_t>(buf * Sh::kBN);
-          for (int j = 0; j < nseg; j++) {
+          for (int j = 0; j < nit; j++) {
+            const int buf = buf_of(j / kSegChunks);
+            const uint32_t acc = S.tmem + static_cast<uint32_t>(buf * Sh::kBN);
             const int st = s0 + static_cast<int>((g + j) % Sh::kPipeStages), kc = min(kKc, npad - c0 - j * kKc);
             // leading byte offset: K direction; stride byte offset: N direction
             const uint64_t da = sdesc(su32(S.a[st]), 128, static_cast<uint32_t>(kc) * 16);
             const uint64_t db =
                 tma_b ? sdesc(su32(S.b[st]), 128, 1024) : sdesc(su32(S.b[st]), Sh::kBGroupK, kBGroupN);
+            const bool fresh = j % kSegChunks == 0;  // the buffer's first chunk overwrites it
 #pragma unroll
             for (int ks = 0; ks < kKc / 16; ks++) {
               if (ks < kc / 16) {
                 // the start address field counts 16-byte units
                 const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
                                ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
-                mma(acc, da + oa, db + ob, Sh::kIdesc, (j == 0 && ks == 0) ? 0u : 1u);
+                mma(acc, da + oa, db + ob, Sh::kIdesc, (fresh && ks == 0) ? 0u : 1u);
               }
             }
             commit(&S.empty[st]);
+            if (j % kSegChunks == kSegChunks - 1 || j == nit - 1) commit(&S.seg_full[buf]);
           }
-          commit(&S.seg_full[buf]);
         }
         __syncwarp();
-        kseg[e]++;
-        g += nseg;
-        c0 += nseg * kKc;
+        kseg[e] += static_cast<uint32_t>(nb);
+        g += nit;
+        c0 += nit * kKc;
       }
     }
     // the last stage release must land before the CTA's shared memory goes away
@@ -785,8 +799,8 @@ __device__ __forceinline__ int member_of(const int64_t *col0, int nmem, int64_t 
 // which starts at zero. Members own the contiguous source ranges [col0[k],
 // col0[k + 1]). Block x takes source indices [x kXmaxSpan, (x + 1)
 // kXmaxSpan), its warp w right-hand side 8 y + w: coalesced loads along the
-// indices, four in flight per lane, one atomic per member met.
-constexpr int kXmaxSpan = 8192;
+// indices, eight in flight per lane, one atomic per member met.
+constexpr int kXmaxSpan = 2048;
 __global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, int64_t n_src,
                             const int64_t *__restrict__ col0, int nmem, unsigned *__restrict__ xmax) {
   const int lane = threadIdx.x & 31;
@@ -798,10 +812,12 @@ __global__ void xmax_kernel(const float *__restrict__ X, int64_t ldx, int nr, in
     const int64_t a0 = max(j0, col0[k]), a1 = min(j1, col0[k + 1]);
     unsigned m = 0u;
     int64_t j = a0 + lane;
-    for (; j + 96 < a1; j += 128) {
-      const float v0 = xr[j], v1 = xr[j + 32], v2 = xr[j + 64], v3 = xr[j + 96];
-      m = max(m, max(__float_as_uint(fabsf(v0)), __float_as_uint(fabsf(v1))));
-      m = max(m, max(__float_as_uint(fabsf(v2)), __float_as_uint(fabsf(v3))));
+    for (; j + 224 < a1; j += 256) {
+      float v[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) v[i] = xr[j + 32 * i];
+#pragma unroll
+      for (int i = 0; i < 8; i++) m = max(m, __float_as_uint(fabsf(v[i])));
     }
     for (; j < a1; j += 32) m = max(m, __float_as_uint(fabsf(xr[j])));
 #pragma unroll
@@ -1044,7 +1060,7 @@ static int run_tc(const DevPlan &p, const DevTc &t, const float *X, int64_t ldx,
   uint16_t *xts = R == 64 ? t.xts64 : t.xts;
   int nl = 0;
   int gp = static_cast<int>((p.n_src + 63) / 64);
-  if (gp > 2048) gp = 2048;
+  if (gp > 8192) gp = 8192;
   if (ev) cudaEventRecord(ev[0], s);
   // per member and right-hand side: max |x| bits, sigma, 1 / sigma
   const int64_t nm64 = static_cast<int64_t>(t.nmem) * kTcMaxRhs;
