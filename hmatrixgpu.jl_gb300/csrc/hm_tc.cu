@@ -25,11 +25,12 @@
 // order, so concurrent CTAs work on neighbouring panels and share XTS rows in
 // L2; warp 0 takes the tickets and queues them for the other roles). A 32-wide
 // pass runs two pipelines, item n in pipeline n & 1; they share the tensor
-// cores but have their own stages, producers, MMA warp and epilogue set,
-// because one MMA warp's own instructions per chunk bound a pipeline. A
-// 64-wide pass runs one (every item in pipeline 0), whose epilogue sets still
-// take every other item:
-//   warp 0      item tickets (lane 0), queued in shared memory for the others;
+// cores but have their own item queue, stages, producers, MMA warp and
+// epilogue set, because one MMA warp's own instructions per chunk bound a
+// pipeline. A 64-wide pass runs one (every item in pipeline 0), whose
+// epilogue sets still take every other item:
+//   warp 0      item tickets (lane 0), queued in shared memory for the others
+//               (one queue per pipeline);
 //   producers   warps 1, 3 and 8.. (one per stage; producer b serves pipeline
 //               b mod kPipes, and the pipeline's chunk g goes to its producer
 //               g mod kPipeStages) of each pipeline's ring of 64-column
@@ -76,7 +77,7 @@ namespace {
 
 constexpr int kKc = 64;                // columns per chunk
 constexpr int kABytes = 128 * kKc * 2;  // A tile: 64 hi rows, then 64 lo rows: 16 KB
-constexpr int kQ = 16;                  // item queue slots
+constexpr int kQ = 16;                  // item queue slots (split between the pipelines)
 #ifndef HM_TC_SEG_CHUNKS
 #define HM_TC_SEG_CHUNKS 1
 #endif
@@ -120,7 +121,10 @@ struct TcShape {
   static constexpr uint32_t kTmemCols = 512;
   static constexpr int kBufs = static_cast<int>(kTmemCols) / kBN;  // 8 or 4
   static constexpr int kSetBufs = kBufs / 2;
-  static constexpr int kConsumers = kBProducers + kPipes + 8;  // warps that read each queued item
+  // Each pipeline has its own item queue of kQP slots; its readers are its
+  // producers, its MMA warp and the epilogue warps that may finish its items.
+  static constexpr int kQP = kQ / kPipes;
+  static constexpr int kConsumers = kPipes == 2 ? kStages / 2 + 1 + 4 : kStages + 1 + 8;
   static constexpr uint32_t kBGroupK = (kBN / 8) * kBGroupN;
   static constexpr int kPieces = R / 4;               // 16-byte pieces of an XTS row
   static constexpr int kRowsPerCopy = 32 / kPieces;   // XTS rows per warp-wide copy
@@ -270,13 +274,13 @@ __device__ __forceinline__ bool wait_bar_warp(SM &S, uint64_t *bar, uint32_t par
   return __all_sync(0xffffffffu, wait_bar(S, bar, parity, status, code));
 }
 
-// Item n of this CTA from the queue (false: no more items, or an abort); every
-// consumer warp calls it once per n and releases the slot. The item itself
-// travels in the queue, so no consumer waits on a global load per item.
-template <class SM>
-__device__ __forceinline__ bool next_item(SM &S, int n, int32_t *status, TcItem &I) {
-  const int q = n % kQ;
-  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((n / kQ) & 1), status, 30)) return false;
+// Item m of pipeline `pipe`'s queue (false: no more items, or an abort); every
+// reader of that queue calls it once per m and releases the slot. The item
+// itself travels in the queue, so no consumer waits on a global load per item.
+template <int QP, class SM>
+__device__ __forceinline__ bool next_item(SM &S, int pipe, int m, int32_t *status, TcItem &I) {
+  const int q = pipe * QP + m % QP;
+  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((m / QP) & 1), status, 30)) return false;
   I = S.qdata[q];
   __syncwarp();
   if ((threadIdx.x & 31) == 0) arrive(&S.qempty[q]);
@@ -400,8 +404,19 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // One atomic takes a.grab consecutive items while more than 16 per CTA
     // remain (one ticket round trip per a.grab short items), single items
     // after that so that the CTAs finish together. Lanes load the grabbed
-    // items in parallel; lane 0 writes each into its queue slot.
+    // items in parallel; lane 0 writes each into its queue slot: item n to
+    // pipeline n mod kPipes's queue, and the end marker to every queue.
     int n = 0, last = 0;
+    int pushed[2] = {0, 0};  // items put into each pipeline's queue
+    auto push = [&](int pipe, const TcItem &t) {
+      const int m = pushed[pipe]++, q = pipe * Sh::kQP + m % Sh::kQP;
+      if (!wait_bar_warp(S, &S.qempty[q], static_cast<uint32_t>((m / Sh::kQP) & 1) ^ 1u, a.status, 29)) return false;
+      if (lane == 0) {
+        S.qdata[q] = t;
+        arrive(&S.qfull[q]);
+      }
+      return true;
+    };
     for (bool more = true; more;) {
       const int want = last + 16 * static_cast<int>(gridDim.x) < a.nitems ? a.grab : 1;
       int b = 0;
@@ -420,16 +435,13 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
         t.out = __shfl_sync(0xffffffffu, mine.out, j);
         t.kind = __shfl_sync(0xffffffffu, mine.kind, j);
         t.row0 = __shfl_sync(0xffffffffu, mine.row0, j);
-        const int q = n % kQ;
-        if (!wait_bar_warp(S, &S.qempty[q], static_cast<uint32_t>((n / kQ) & 1) ^ 1u, a.status, 29)) {
+        if (t.kind < 0) {
+          for (int pipe = 0; pipe < Sh::kPipes; pipe++)
+            if (!push(pipe, t)) break;
           more = false;
           break;
         }
-        if (lane == 0) {
-          S.qdata[q] = t;
-          arrive(&S.qfull[q]);
-        }
-        if (t.kind < 0) {
+        if (!push(n % Sh::kPipes, t)) {
           more = false;
           break;
         }
@@ -447,10 +459,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
     bool stop = false;
     const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
-    for (int n = 0; !stop; n++) {
+    for (int m = 0; !stop; m++) {
       TcItem I;
-      if (!next_item(S, n, a.status, I)) break;
-      if ((n & 1) % Sh::kPipes != pipe) continue;
+      if (!next_item<Sh::kQP>(S, pipe, m, a.status, I)) break;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         if (g % Sh::kPipeStages != q) continue;
@@ -578,19 +589,19 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     const int pipe = warp == 2 ? 0 : 1;
     const int s0 = pipe * Sh::kPipeStages;  // the pipeline's first stage
     int64_t g = 0;                          // the pipeline's chunks so far
-    int n = 0;
+    int m = 0;  // the pipeline's items so far
     bool stop = false;
     // Every kSegChunks chunks of an item go to a fresh accumulator buffer of
-    // the item's epilogue set (set n & 1, buffers used in turn), whose warps
+    // the item's epilogue set (the pipeline's set, or set m & 1 when one
+    // pipeline serves both; buffers used in turn), whose warps
     // add the buffers' sums in FP32 registers: the tensor cores' own
     // accumulation then spans at most 4 kSegChunks UMMAs, whatever the item's
     // length.
     uint32_t kseg[2] = {0u, 0u};  // buffers handed to each epilogue set so far
-    for (; !stop; n++) {
+    for (; !stop; m++) {
       TcItem I;
-      if (!next_item(S, n, a.status, I)) break;
-      if ((n & 1) % Sh::kPipes != pipe) continue;
-      const int e = n & 1;
+      if (!next_item<Sh::kQP>(S, pipe, m, a.status, I)) break;
+      const int e = Sh::kPipes == 2 ? pipe : (m & 1);
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       // V pieces' B tiles come from the tile load (K groups 128 B apart, N
       // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
@@ -692,11 +703,13 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     uint64_t *i_ready = lo_part ? &S.xb_ready[e] : &S.xa_ready[e];
     uint64_t *i_free = lo_part ? &S.xb_free[e] : &S.xa_free[e];
     uint32_t kseg = 0;  // accumulator buffers of this set consumed so far
-    for (int n = 0;; n++) {
+    // set e reads pipeline e's queue, or, with one pipeline, every other item
+    const int qpipe = Sh::kPipes == 2 ? e : 0;
+    for (int m = 0;; m++) {
       TcItem I;
-      if (!next_item(S, n, a.status, I)) break;
-      if ((n & 1) != e) continue;
-      const uint32_t k = static_cast<uint32_t>(n >> 1);  // this set's item count
+      if (!next_item<Sh::kQP>(S, qpipe, m, a.status, I)) break;
+      if (Sh::kPipes == 1 && (m & 1) != e) continue;
+      const uint32_t k = static_cast<uint32_t>(Sh::kPipes == 2 ? m : m >> 1);  // this set's item count
       const int nch = ((I.ncols > 0 ? (I.ncols + 15) & ~15 : 16) + kKc - 1) / kKc;
       const int span = I.kind != 0 ? kSegChunksV : kSegChunksDU;
       const int nbuf = (nch + span - 1) / span;  // accumulator buffers of the item
