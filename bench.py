@@ -603,7 +603,7 @@ def run_gpu(args):
     rel_err = float(torch.linalg.norm(y.double() - y64) / torch.linalg.norm(y64))
 
     # 32 right-hand sides: plain FP32 (CUDA cores) against mixed precision
-    # (BF16 hi/lo pairs on the tensor cores), same matrix, errors against the
+    # (scaled FP16 hi/lo pairs on the tensor cores), same matrix, errors against the
     # FP64 product of the same 32 vectors
     rhs32 = None
     if not args.skip_rhs32:

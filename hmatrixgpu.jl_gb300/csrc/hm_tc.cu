@@ -25,12 +25,11 @@
 // order, so concurrent CTAs work on neighbouring panels and share XTS rows in
 // L2; warp 0 takes the tickets and queues them for the other roles). A 32-wide
 // pass runs two pipelines, item n in pipeline n & 1; they share the tensor
-// cores but have their own item queue, stages, producers, MMA warp and
-// epilogue set, because one MMA warp's own instructions per chunk bound a
-// pipeline. A 64-wide pass runs one (every item in pipeline 0), whose
-// epilogue sets still take every other item:
-//   warp 0      item tickets (lane 0), queued in shared memory for the others
-//               (one queue per pipeline);
+// cores but have their own stages, producers, MMA warp and epilogue set,
+// because one MMA warp's own instructions per chunk bound a pipeline. A
+// 64-wide pass runs one (every item in pipeline 0), whose epilogue sets still
+// take every other item:
+//   warp 0      item tickets (lane 0), queued in shared memory for the others;
 //   producers   warps 1, 3 and 8.. (one per stage; producer b serves pipeline
 //               b mod kPipes, and the pipeline's chunk g goes to its producer
 //               g mod kPipeStages) of each pipeline's ring of 64-column
@@ -77,7 +76,7 @@ namespace {
 
 constexpr int kKc = 64;                // columns per chunk
 constexpr int kABytes = 128 * kKc * 2;  // A tile: 64 hi rows, then 64 lo rows: 16 KB
-constexpr int kQ = 16;                  // item queue slots (split between the pipelines)
+constexpr int kQ = 16;                  // item queue slots
 #ifndef HM_TC_SEG_CHUNKS
 #define HM_TC_SEG_CHUNKS 1
 #endif
@@ -121,10 +120,7 @@ struct TcShape {
   static constexpr uint32_t kTmemCols = 512;
   static constexpr int kBufs = static_cast<int>(kTmemCols) / kBN;  // 8 or 4
   static constexpr int kSetBufs = kBufs / 2;
-  // Each pipeline has its own item queue of kQP slots; its readers are its
-  // producers, its MMA warp and the epilogue warps that may finish its items.
-  static constexpr int kQP = kQ / kPipes;
-  static constexpr int kConsumers = kPipes == 2 ? kStages / 2 + 1 + 4 : kStages + 1 + 8;
+  static constexpr int kConsumers = kBProducers + kPipes + 8;  // warps that read each queued item
   static constexpr uint32_t kBGroupK = (kBN / 8) * kBGroupN;
   static constexpr int kPieces = R / 4;               // 16-byte pieces of an XTS row
   static constexpr int kRowsPerCopy = 32 / kPieces;   // XTS rows per warp-wide copy
@@ -136,10 +132,8 @@ struct TcShape {
   // one release ahead, which a parity wait on the stage's barrier could not
   // tell apart from the release before.
   static_assert(kBProducers == kStages, "one producer warp per stage");
-  // the MMA warp waits for all chunks of a pass (a segment, or two chunks)
-  // before it releases any
-  static_assert(kSegChunksDU <= kPipeStages && kSegChunksV <= kPipeStages && kPipeStages >= 2,
-                "a pass fits a pipeline's stages");
+  // the MMA warp waits for a whole segment's chunks before it releases any
+  static_assert(kSegChunksDU <= kPipeStages && kSegChunksV <= kPipeStages, "a segment fits a pipeline's stages");
 };
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 constexpr unsigned long long kWaitIters = 1ull << 26;   // backstop if the timer stood still
@@ -274,13 +268,13 @@ __device__ __forceinline__ bool wait_bar_warp(SM &S, uint64_t *bar, uint32_t par
   return __all_sync(0xffffffffu, wait_bar(S, bar, parity, status, code));
 }
 
-// Item m of pipeline `pipe`'s queue (false: no more items, or an abort); every
-// reader of that queue calls it once per m and releases the slot. The item
-// itself travels in the queue, so no consumer waits on a global load per item.
-template <int QP, class SM>
-__device__ __forceinline__ bool next_item(SM &S, int pipe, int m, int32_t *status, TcItem &I) {
-  const int q = pipe * QP + m % QP;
-  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((m / QP) & 1), status, 30)) return false;
+// Item n of this CTA from the queue (false: no more items, or an abort); every
+// consumer warp calls it once per n and releases the slot. The item itself
+// travels in the queue, so no consumer waits on a global load per item.
+template <class SM>
+__device__ __forceinline__ bool next_item(SM &S, int n, int32_t *status, TcItem &I) {
+  const int q = n % kQ;
+  if (!wait_bar_warp(S, &S.qfull[q], static_cast<uint32_t>((n / kQ) & 1), status, 30)) return false;
   I = S.qdata[q];
   __syncwarp();
   if ((threadIdx.x & 31) == 0) arrive(&S.qempty[q]);
@@ -404,19 +398,8 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     // One atomic takes a.grab consecutive items while more than 16 per CTA
     // remain (one ticket round trip per a.grab short items), single items
     // after that so that the CTAs finish together. Lanes load the grabbed
-    // items in parallel; lane 0 writes each into its queue slot: item n to
-    // pipeline n mod kPipes's queue, and the end marker to every queue.
+    // items in parallel; lane 0 writes each into its queue slot.
     int n = 0, last = 0;
-    int pushed[2] = {0, 0};  // items put into each pipeline's queue
-    auto push = [&](int pipe, const TcItem &t) {
-      const int m = pushed[pipe]++, q = pipe * Sh::kQP + m % Sh::kQP;
-      if (!wait_bar_warp(S, &S.qempty[q], static_cast<uint32_t>((m / Sh::kQP) & 1) ^ 1u, a.status, 29)) return false;
-      if (lane == 0) {
-        S.qdata[q] = t;
-        arrive(&S.qfull[q]);
-      }
-      return true;
-    };
     for (bool more = true; more;) {
       const int want = last + 16 * static_cast<int>(gridDim.x) < a.nitems ? a.grab : 1;
       int b = 0;
@@ -435,13 +418,16 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
         t.out = __shfl_sync(0xffffffffu, mine.out, j);
         t.kind = __shfl_sync(0xffffffffu, mine.kind, j);
         t.row0 = __shfl_sync(0xffffffffu, mine.row0, j);
-        if (t.kind < 0) {
-          for (int pipe = 0; pipe < Sh::kPipes; pipe++)
-            if (!push(pipe, t)) break;
+        const int q = n % kQ;
+        if (!wait_bar_warp(S, &S.qempty[q], static_cast<uint32_t>((n / kQ) & 1) ^ 1u, a.status, 29)) {
           more = false;
           break;
         }
-        if (!push(n % Sh::kPipes, t)) {
+        if (lane == 0) {
+          S.qdata[q] = t;
+          arrive(&S.qfull[q]);
+        }
+        if (t.kind < 0) {
           more = false;
           break;
         }
@@ -459,9 +445,10 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     int64_t g = 0, last_g = -1;  // last_g: the chunk whose bulk copies this warp issued last
     bool stop = false;
     const int piece = lane % Sh::kPieces, sub = lane / Sh::kPieces;
-    for (int m = 0; !stop; m++) {
+    for (int n = 0; !stop; n++) {
       TcItem I;
-      if (!next_item<Sh::kQP>(S, pipe, m, a.status, I)) break;
+      if (!next_item(S, n, a.status, I)) break;
+      if ((n & 1) % Sh::kPipes != pipe) continue;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       for (int c0 = 0; c0 < npad; c0 += kKc, g++) {
         if (g % Sh::kPipeStages != q) continue;
@@ -561,12 +548,9 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
                          : "memory");
           }
         }
-        // the gathers complete on the stage's barrier as well: each lane's
-        // cp.async.mbarrier.arrive adds a pending arrival that lands once the
-        // lane's copies have, so the warp goes on to its next chunk at once
-        // (the MMA warp fences them for the tensor cores' proxy after its
-        // wait). Every lane registers before lane 0's own arrival.
-        asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(su32(&S.full[s])) : "memory");
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
         if (lane == 0) arrive(&S.full[s]);
       }
@@ -589,54 +573,49 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     const int pipe = warp == 2 ? 0 : 1;
     const int s0 = pipe * Sh::kPipeStages;  // the pipeline's first stage
     int64_t g = 0;                          // the pipeline's chunks so far
-    int m = 0;  // the pipeline's items so far
+    int n = 0;
     bool stop = false;
     // Every kSegChunks chunks of an item go to a fresh accumulator buffer of
-    // the item's epilogue set (the pipeline's set, or set m & 1 when one
-    // pipeline serves both; buffers used in turn), whose warps
+    // the item's epilogue set (set n & 1, buffers used in turn), whose warps
     // add the buffers' sums in FP32 registers: the tensor cores' own
     // accumulation then spans at most 4 kSegChunks UMMAs, whatever the item's
     // length.
     uint32_t kseg[2] = {0u, 0u};  // buffers handed to each epilogue set so far
-    for (; !stop; m++) {
+    for (; !stop; n++) {
       TcItem I;
-      if (!next_item<Sh::kQP>(S, pipe, m, a.status, I)) break;
-      const int e = Sh::kPipes == 2 ? pipe : (m & 1);
+      if (!next_item(S, n, a.status, I)) break;
+      if ((n & 1) % Sh::kPipes != pipe) continue;
+      const int e = n & 1;
       const int npad = I.ncols > 0 ? (I.ncols + 15) & ~15 : 16;
       // V pieces' B tiles come from the tile load (K groups 128 B apart, N
       // groups 1024 B), near/U tiles' from the gather (kBGroupK, 128 B)
       const bool tma_b = I.kind != 0;
       const int kSegChunks = tma_b ? kSegChunksV : kSegChunksDU;
-      // One pass of this loop per `nit` chunks c0 / kKc .. + nit - 1 (stages
-      // g .. g + nit - 1, accumulator buffers kseg .. + nb - 1, a fresh one
-      // every kSegChunks chunks): their buffers and stages are waited for
+      // One pass of this loop per accumulator buffer: the segment's chunks
+      // c0 / kKc .. + nseg - 1 (stages g .. g + nseg - 1) are waited for
       // first, then all their UMMAs go out under one fence and one election.
-      // The warp's own instructions per pass are what bound a pipeline, so a
-      // pass takes two chunks where a set has buffers to spare. nit <=
-      // kPipeStages: the producers of the pass's chunks never wait for it.
-      const int kIter = kSegChunks > 1 ? kSegChunks : (Sh::kSetBufs >= 4 ? 2 : 1);
+      // The warp's own per-chunk instructions are what bound the pass, so
+      // they are paid once per segment. nseg <= kPipeStages: the producers of
+      // the segment's chunks never wait for the segment itself.
       for (int c0 = 0; c0 < npad;) {
-        const int nit = min(kIter, (npad - c0 + kKc - 1) / kKc);
-        const int nb = (nit + kSegChunks - 1) / kSegChunks;
-        auto buf_of = [&](int b) { return e * Sh::kSetBufs + static_cast<int>((kseg[e] + b) % Sh::kSetBufs); };
-        bool ok = true;
-        for (int b = 0; ok && b < nb; b++)
-          ok = wait_bar_warp(S, &S.seg_empty[buf_of(b)], (((kseg[e] + b) / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23);
-        for (int j = 0; ok && j < nit; j++)
+        const int nseg = min(kSegChunks, (npad - c0 + kKc - 1) / kKc);
+        const int buf = e * Sh::kSetBufs + static_cast<int>(kseg[e] % Sh::kSetBufs);
+        bool ok = wait_bar_warp(S, &S.seg_empty[buf], ((kseg[e] / Sh::kSetBufs) & 1u) ^ 1u, a.status, 23);
+        for (int j = 0; ok && j < nseg; j++)
           ok = wait_bar_warp(S, &S.full[s0 + static_cast<int>((g + j) % Sh::kPipeStages)],
                              static_cast<uint32_t>(((g + j) / Sh::kPipeStages) & 1), a.status, 24);
         if (!ok) {
           stop = true;
           break;
         }
-        const int cl = c0 + (nit - 1) * kKc, kcl = min(kKc, npad - cl);  // the pass's last chunk
+        const int cl = c0 + (nseg - 1) * kKc, kcl = min(kKc, npad - cl);  // the segment's last chunk
         if (tma_b && I.ncols - cl < kcl) {
           // the last chunk of a V piece: the tile load brought 64 consecutive
           // XTS rows, and those of the padding columns [ncols, kc) belong to
           // other blocks (or are t rows being rewritten). The A tile is zero
           // there, but 0 * Inf and 0 * NaN are not, so the rows are zeroed
           // (16 bytes per row and N group) before the UMMAs read them.
-          const uint32_t bl = su32(S.b[s0 + static_cast<int>((g + nit - 1) % Sh::kPipeStages)]);
+          const uint32_t bl = su32(S.b[s0 + static_cast<int>((g + nseg - 1) % Sh::kPipeStages)]);
           const int valid = I.ncols - cl, nz = kcl - valid;
           for (int z = lane; z < nz * (Sh::kBN / 8); z += 32) {
             const int k = valid + z % nz, gq = z / nz;
@@ -646,36 +625,32 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
         }
-        // gathered B rows were written through the generic proxy
-        if (!tma_b) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (elect_one()) {
-          for (int j = 0; j < nit; j++) {
-            const int buf = buf_of(j / kSegChunks);
-            const uint32_t acc = S.tmem + static_cast<uint32_t>(buf * Sh::kBN);
+          const uint32_t acc = S.tmem + static_cast<uint32_t>(buf * Sh::kBN);
+          for (int j = 0; j < nseg; j++) {
             const int st = s0 + static_cast<int>((g + j) % Sh::kPipeStages), kc = min(kKc, npad - c0 - j * kKc);
             // leading byte offset: K direction; stride byte offset: N direction
             const uint64_t da = sdesc(su32(S.a[st]), 128, static_cast<uint32_t>(kc) * 16);
             const uint64_t db =
                 tma_b ? sdesc(su32(S.b[st]), 128, 1024) : sdesc(su32(S.b[st]), Sh::kBGroupK, kBGroupN);
-            const bool fresh = j % kSegChunks == 0;  // the buffer's first chunk overwrites it
 #pragma unroll
             for (int ks = 0; ks < kKc / 16; ks++) {
               if (ks < kc / 16) {
                 // the start address field counts 16-byte units
                 const uint64_t oa = static_cast<uint64_t>(ks * 256) >> 4,
                                ob = static_cast<uint64_t>(tma_b ? ks * 256 : ks * 2 * Sh::kBGroupK) >> 4;
-                mma(acc, da + oa, db + ob, Sh::kIdesc, (fresh && ks == 0) ? 0u : 1u);
+                mma(acc, da + oa, db + ob, Sh::kIdesc, (j == 0 && ks == 0) ? 0u : 1u);
               }
             }
             commit(&S.empty[st]);
-            if (j % kSegChunks == kSegChunks - 1 || j == nit - 1) commit(&S.seg_full[buf]);
           }
+          commit(&S.seg_full[buf]);
         }
         __syncwarp();
-        kseg[e] += static_cast<uint32_t>(nb);
-        g += nit;
-        c0 += nit * kKc;
+        kseg[e]++;
+        g += nseg;
+        c0 += nseg * kKc;
       }
     }
     // the last stage release must land before the CTA's shared memory goes away
@@ -703,13 +678,11 @@ __global__ void __launch_bounds__(TcShape<R>::kThreads, 1) tc_kernel(const __gri
     uint64_t *i_ready = lo_part ? &S.xb_ready[e] : &S.xa_ready[e];
     uint64_t *i_free = lo_part ? &S.xb_free[e] : &S.xa_free[e];
     uint32_t kseg = 0;  // accumulator buffers of this set consumed so far
-    // set e reads pipeline e's queue, or, with one pipeline, every other item
-    const int qpipe = Sh::kPipes == 2 ? e : 0;
-    for (int m = 0;; m++) {
+    for (int n = 0;; n++) {
       TcItem I;
-      if (!next_item<Sh::kQP>(S, qpipe, m, a.status, I)) break;
-      if (Sh::kPipes == 1 && (m & 1) != e) continue;
-      const uint32_t k = static_cast<uint32_t>(Sh::kPipes == 2 ? m : m >> 1);  // this set's item count
+      if (!next_item(S, n, a.status, I)) break;
+      if ((n & 1) != e) continue;
+      const uint32_t k = static_cast<uint32_t>(n >> 1);  // this set's item count
       const int nch = ((I.ncols > 0 ? (I.ncols + 15) & ~15 : 16) + kKc - 1) / kKc;
       const int span = I.kind != 0 ? kSegChunksV : kSegChunksDU;
       const int nbuf = (nch + span - 1) / span;  // accumulator buffers of the item
