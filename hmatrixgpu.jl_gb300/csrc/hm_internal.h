@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/hmgpu.h"
+#include "hm_packjob.h"
 
 namespace hm {
 
@@ -152,20 +153,6 @@ constexpr int kTcTrailer = 68 * 4;  // bytes after an item's chunks: 64 row fact
 struct VGroup {
   int64_t v_off;
   int32_t stride, rows, x_off, t_off;
-};
-
-// Copy job of the packing pass: a row-major source slice -> rows of a tile panel.
-struct PackJob {
-  int64_t src_off;   // element offset in the source array
-  int64_t dst_off;   // element offset of (first row, first column) in the panel array
-  int32_t src_ld;    // source row stride
-  int32_t dst_ld;    // panel row stride
-  int32_t ncols;
-  int32_t m;         // rows
-  int32_t kind;      // 0 dense source, 1 U source, 2 dense generated from the kernel
-  int32_t row0;      // generated: first permuted row
-  int32_t col0;      // generated: first permuted column
-  int32_t pad;
 };
 
 struct Plan {

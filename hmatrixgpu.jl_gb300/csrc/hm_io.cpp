@@ -20,6 +20,7 @@ using hm::HMatrix;
 namespace {
 
 constexpr char kMagic[8] = {'H', 'M', 'G', 'P', 'U', 'H', '0', '1'};
+constexpr int32_t kFileVersion = 1;  // layout of what follows the magic
 
 struct Writer {
   FILE *f;
@@ -120,7 +121,7 @@ extern "C" int hmgpu_hmatrix_save(const hmgpu_hmatrix *h, const char *path) {
   if (!f) return hm::fail(HMGPU_ERR_INVALID, std::string("cannot open ") + path + " for writing");
   Writer w{f.get()};
   w.raw(kMagic, sizeof kMagic);
-  w.val(static_cast<int32_t>(hmgpu_abi_version()));
+  w.val(kFileVersion);
   w.val(H.opt.precision);
   w.val(H.opt.compensated);
   w.val(static_cast<int32_t>(H.multi_from));
@@ -189,8 +190,8 @@ extern "C" int hmgpu_hmatrix_load(const char *path, hmgpu_hmatrix **out) {
   r.val(H->opt.precision);
   r.val(H->opt.compensated);
   r.val(multi_from);
-  if (!r.ok || abi != hmgpu_abi_version())
-    return hm::fail(HMGPU_ERR_INVALID, std::string(path) + ": written by another ABI version");
+  if (!r.ok || abi != kFileVersion)
+    return hm::fail(HMGPU_ERR_INVALID, std::string(path) + ": written in another file version");
   if (H->opt.precision != HMGPU_F64 && H->opt.precision != HMGPU_F32 && H->opt.precision != HMGPU_MIXED)
     return hm::fail(HMGPU_ERR_INVALID, std::string(path) + ": unknown precision");
   cudaGetDevice(&H->device);

@@ -209,15 +209,49 @@ def SVD_recompress(U, V, eps):
     return np.array(Uo[:, :r]), np.array(Vo[: r * n].reshape((r, n), order="F"))
 
 
+class UserKernel:
+    """A kernel K[i, j] = f(x_i, y_j) of the caller's own: CUDA C++ source that
+    defines ``__device__ double hmgpu_entry(const double *x, const double *y,
+    const double *p)`` (target point x, source point y, 3 coordinates each; p
+    the parameters given to Kernel('user', ...)), compiled at run time with
+    NVRTC into the library's ACA+, dense-block and sparsify kernels
+    (hmgpu_user_kernel_compile). A compile error raises HMGPUError with the
+    compiler's log in ``.log``."""
+
+    def __init__(self, source):
+        self._h = C.c_void_p()
+        buf = C.create_string_buffer(1 << 16)
+        rc = lib().hmgpu_user_kernel_compile(source.encode(), C.byref(self._h), buf, len(buf))
+        self.log = buf.value.decode(errors="replace")
+        if rc != 0:
+            err = HMGPUError(rc, lib().hmgpu_last_error().decode())
+            err.log = self.log
+            raise err
+        self.source = source
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().hmgpu_user_kernel_free(h)
+            self._h = None
+
+
 class Kernel:
     """A matrix K generated on the device: kind in {'laplace', 'yukawa', 'log2d',
-    'vector_r', 'dipolar'} over target points X and source points Y (3 x N), or
-    'explicit' with a dense matrix A."""
+    'vector_r', 'dipolar'} over target points X and source points Y (3 x N),
+    'explicit' with a dense matrix A, or 'user' with a UserKernel (or its
+    source) and up to 64 parameters."""
 
-    def __init__(self, kind, X=None, Y=None, A=None):
+    def __init__(self, kind, X=None, Y=None, A=None, user=None, params=()):
         if kind not in KERNEL_IDS:
             raise ValueError(f"unknown kernel {kind!r}")
         self.kind = kind
+        self.user = None
+        self.params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+        if kind == "user":
+            if user is None:
+                raise ValueError("a 'user' kernel needs user= (a UserKernel or its source)")
+            self.user = user if isinstance(user, UserKernel) else UserKernel(user)
         if kind == "explicit":
             self.A = np.asfortranarray(A, dtype=np.float64)
             self.X = self.Y = None
@@ -240,6 +274,10 @@ class Kernel:
             d.nX = self.X.shape[1]
             d.Y = ptr(self.Y)
             d.nY = self.Y.shape[1]
+        if self.user is not None:
+            d.user = self.user._h
+            d.params = ptr(self.params) if self.params.size else None
+            d.nparams = self.params.size
         return d
 
     def size(self):

@@ -42,11 +42,31 @@ def _compile(src, extra):
     return obj, r.stderr
 
 
+# Headers the library compiles again at run time, with a user's entry function
+# (NVRTC, hm_user.cpp): embedded in the library as strings.
+EMBEDDED = (("hm_src_entry_cuh", "hm_entry.cuh"), ("hm_src_packjob_h", "hm_packjob.h"))
+
+
+def _embedded_sources():
+    """Writes _build/hm_sources.cpp, which defines each embedded header's text."""
+    out = []
+    for sym, name in EMBEDDED:
+        with open(os.path.join(CSRC, name)) as f:
+            text = f.read()
+        if ')HMSRC"' in text:
+            raise RuntimeError(f"{name} contains the raw-string delimiter")
+        out.append(f'extern const char {sym}[];\nconst char {sym}[] = R"HMSRC({text})HMSRC";\n')
+    path = os.path.join(BUILD, "hm_sources.cpp")
+    with open(path, "w") as f:
+        f.write("".join(out))
+    return path
+
+
 def build(verbose=False, extra=(), jobs=None):
     """Compile every source in csrc/ in parallel and link libhmgpu.so. Returns the path."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    srcs = sources()
+    srcs = sources() + [_embedded_sources()]
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         results = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
     objs = [o for o, _ in results]

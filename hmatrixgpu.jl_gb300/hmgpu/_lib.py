@@ -14,7 +14,7 @@ VP = C.c_void_p
 F64, F32, MIXED = 0, 1, 2
 PRECISIONS = {"f64": F64, "float64": F64, "f32": F32, "float32": F32, "mixed": MIXED}
 
-KERNEL_IDS = {"explicit": 0, "laplace": 1, "yukawa": 2, "log2d": 3, "vector_r": 4, "dipolar": 5}
+KERNEL_IDS = {"explicit": 0, "laplace": 1, "yukawa": 2, "log2d": 3, "vector_r": 4, "dipolar": 5, "user": 6}
 
 _lock = threading.Lock()
 _LIB = None
@@ -35,7 +35,8 @@ class Options(C.Structure):
 
 class KernelDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("X", F64P), ("nX", C.c_int64),
-                ("Y", F64P), ("nY", C.c_int64), ("A", F64P), ("lda", C.c_int64)]
+                ("Y", F64P), ("nY", C.c_int64), ("A", F64P), ("lda", C.c_int64),
+                ("user", C.c_void_p), ("params", F64P), ("nparams", C.c_int64)]
 
 
 class Info(C.Structure):
@@ -101,6 +102,8 @@ SIGNATURES = {
     "hmgpu_rank_model_free": (C.c_int, [VP]),
     "hmgpu_block_features": (C.c_int, [VP, VP, C.c_double, C.c_double, F32P, I64P]),
     "hmgpu_sparsify": (C.c_int, [C.POINTER(KernelDesc), VP, VP, C.c_double, I64P, I64P, F64P, I64P]),
+    "hmgpu_user_kernel_compile": (C.c_int, [C.c_char_p, C.POINTER(VP), C.c_char_p, C.c_int64]),
+    "hmgpu_user_kernel_free": (C.c_int, [VP]),
     "hmgpu_hmatrix_batch": (C.c_int, [C.POINTER(VP), C.c_int32, C.POINTER(VP)]),
     "hmgpu_graph_create": (C.c_int, [VP, VP, VP, C.c_int64, C.c_int64, C.c_int64, C.POINTER(VP)]),
     "hmgpu_graph_launch": (C.c_int, [VP, VP]),

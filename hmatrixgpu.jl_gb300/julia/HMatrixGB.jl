@@ -52,6 +52,35 @@ struct KernelDesc
     nY::Int64
     A::Ptr{Float64}
     lda::Int64
+    user::Ptr{Cvoid}        # const hmgpu_user_kernel* (HMGPU_KERNEL_USER)
+    params::Ptr{Float64}
+    nparams::Int64
+end
+KernelDesc(kind, reserved, X, nX, Y, nY, A, lda) =
+    KernelDesc(kind, reserved, X, nX, Y, nY, A, lda, C_NULL, C_NULL, 0)
+
+"""
+    UserKernel(source)
+
+A kernel K[i, j] = f(x_i, y_j) of the caller's own, for `HMatrix(uk, ...)`: the
+reference builds an HMatrix from any K it can index (src/hmatrix.jl:183). The
+CUDA C++ `source` defines
+`__device__ double hmgpu_entry(const double *x, const double *y, const double *p)`
+and is compiled at run time (NVRTC) into the library's assembly kernels.
+"""
+mutable struct UserKernel
+    handle::Ptr{Cvoid}
+    function UserKernel(source::AbstractString)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        log = zeros(UInt8, 1 << 16)
+        rc = ccall((:hmgpu_user_kernel_compile, libhmgpu), Cint,
+                   (Cstring, Ref{Ptr{Cvoid}}, Ptr{UInt8}, Int64), source, h, log, length(log))
+        rc == 0 || throw(HMGPUError(rc, unsafe_string(ccall((:hmgpu_last_error, libhmgpu), Cstring, ())) *
+                                        "\n" * unsafe_string(pointer(log))))
+        uk = new(h[])
+        finalizer(u -> ccall((:hmgpu_user_kernel_free, libhmgpu), Cint, (Ptr{Cvoid},), u.handle), uk)
+        return uk
+    end
 end
 
 struct HMGPUError <: Exception
@@ -164,6 +193,27 @@ function HMatrix(kind::Symbol, Xpts::AbstractMatrix, Ypts::AbstractMatrix, X::Cl
                                    (Ref{Options}, Ref{KernelDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Float64,
                                     Float64, Cint, Ref{Ptr{Cvoid}}),
                                    o, k, X.handle, Y.handle, eta, eps, svd_recompress, h))
+    return _wrap(_T(precision), h[])
+end
+
+"""
+    HMatrix(uk::UserKernel, Xpts, Ypts, X::ClusterTree, Y::ClusterTree;
+            params=Float64[], eta=1.5, eps=1e-5, svd_recompress=true, precision=:f64)
+
+HMatrix(K, X, Y; eta, eps) with K[i, j] = f(Xpts[:, i], Ypts[:, j]) from the
+caller's compiled entry function and its parameters `params` (at most 64).
+"""
+function HMatrix(uk::UserKernel, Xpts::AbstractMatrix, Ypts::AbstractMatrix, X::ClusterTree,
+                 Y::ClusterTree; params=Float64[], eta=1.5, eps=1e-5, svd_recompress=true, precision=:f64)
+    xp, yp, pp = Matrix{Float64}(Xpts), Matrix{Float64}(Ypts), Vector{Float64}(params)
+    o = Ref(Options(_mode(precision), 0, 0, 0))
+    k = Ref(KernelDesc(Int32(6), 0, pointer(xp), size(xp, 2), pointer(yp), size(yp, 2), C_NULL, 0,
+                       uk.handle, isempty(pp) ? C_NULL : pointer(pp), length(pp)))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve xp yp pp uk check(ccall((:hmgpu_hmatrix_build, libhmgpu), Cint,
+                                         (Ref{Options}, Ref{KernelDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Float64,
+                                          Float64, Cint, Ref{Ptr{Cvoid}}),
+                                         o, k, X.handle, Y.handle, eta, eps, svd_recompress, h))
     return _wrap(_T(precision), h[])
 end
 
@@ -339,6 +389,6 @@ end
 _devptr(a) = reinterpret(Ptr{Cvoid}, UInt(Base.unsafe_convert(Main.CUDA.CuPtr{eltype(a)}, a)))
 _stream() = reinterpret(Ptr{Cvoid}, Main.CUDA.stream().handle)
 
-export ClusterTree, HMatrix, info, sparsify_hmatrix, batch, save, load, autotune!, status, shard, mul_shard!
+export ClusterTree, HMatrix, UserKernel, info, sparsify_hmatrix, batch, save, load, autotune!, status, shard, mul_shard!
 
 end # module

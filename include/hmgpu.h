@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define HMGPU_ABI_VERSION 1
+#define HMGPU_ABI_VERSION 2
 
 /* status codes */
 #define HMGPU_OK 0
@@ -59,6 +59,8 @@ extern "C" {
 #define HMGPU_KERNEL_LOG2D 3     /* -log(r)/(2 pi), 1 at r < 1e-12                 */
 #define HMGPU_KERNEL_VECTOR_R 4  /* R_c/r^2 over 3 columns per source point        */
 #define HMGPU_KERNEL_DIPOLAR 5   /* 3x3 demagnetising tensor per point pair        */
+#define HMGPU_KERNEL_USER 6      /* f(x_i, y_j) of the caller's own, compiled at run
+                                    time (hmgpu_user_kernel_compile)               */
 
 /* Returns the message of the last failed call on this thread ("" if none). */
 const char *hmgpu_last_error(void);
@@ -124,6 +126,7 @@ int hmgpu_blocks_free(hmgpu_blocks *b);
 typedef struct hmgpu_hmatrix hmgpu_hmatrix;
 
 typedef struct hmgpu_rank_model hmgpu_rank_model;
+typedef struct hmgpu_user_kernel hmgpu_user_kernel;
 
 typedef struct {
   int32_t precision;   /* HMGPU_F64, HMGPU_F32 or HMGPU_MIXED                     */
@@ -146,7 +149,25 @@ typedef struct {
   int64_t nY;
   const double *A; /* HMGPU_KERNEL_EXPLICIT: column-major matrix, host or device  */
   int64_t lda;
+  const hmgpu_user_kernel *user; /* HMGPU_KERNEL_USER: the compiled entry function */
+  const double *params;          /* HMGPU_KERNEL_USER: its parameters, host or device */
+  int64_t nparams;               /* HMGPU_KERNEL_USER: 0 to 64 parameters          */
 } hmgpu_kernel;
+
+/* A matrix K[i, j] = f(x_i, y_j) of the caller's own, for hmgpu_hmatrix_build
+ * and hmgpu_sparsify: the reference builds an HMatrix from any K it can index
+ * (HMatrix(K, X, Y), src/hmatrix.jl:183,195-196 read K[i, j]). `source` is CUDA
+ * C++ that defines
+ *   __device__ double hmgpu_entry(const double *x, const double *y, const double *p)
+ * (x the target point and y the source point, 3 coordinates each; p the
+ * kernel's parameters, hmgpu_kernel.params). It is compiled with NVRTC for
+ * sm_103a into the library's own ACA+, dense-block and sparsify kernels,
+ * without FMA contraction, like the built-in kernels; the module is loaded on
+ * each device at its first use. On failure the compiler's log is copied to
+ * `log` (log_len bytes, NUL-terminated; NULL for none) and HMGPU_ERR_INVALID
+ * returned; HMGPU_ERR_UNSUPPORTED when the NVRTC library cannot be loaded. */
+int hmgpu_user_kernel_compile(const char *source, hmgpu_user_kernel **out, char *log, int64_t log_len);
+int hmgpu_user_kernel_free(hmgpu_user_kernel *uk);
 
 /* Imports a reference-layout flattened HMatrix{Float64} (src/hmatrix.jl:46-57,
  * built at :95-147): m x n operator, target/source index maps (1-based), dense

@@ -26,7 +26,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_abi_version_and_errors():
     L = _lib.lib()
-    assert L.hmgpu_abi_version() == 1
+    assert L.hmgpu_abi_version() == 2
     rc = L.hmgpu_tree_build(None, 10, 4, 1, ctypes.byref(ctypes.c_void_p()))
     assert rc == -1 and b"NULL" in L.hmgpu_last_error()
 
