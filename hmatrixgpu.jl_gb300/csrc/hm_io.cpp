@@ -245,7 +245,8 @@ extern "C" int hmgpu_hmatrix_load(const char *path, hmgpu_hmatrix **out) {
               static_cast<int64_t>(smap0.size()) <= p.x_len &&
               static_cast<int64_t>(smap0.size()) >= b.n && p.xt_len >= p.x_len + p.R &&
               zero_row >= 0 && zero_row < p.x_len && p.panel_len > 0 && p.v_len > 0 &&
-              p.tile_order.size() == p.tiles.size() && (p.unit_rows == 8 || p.unit_rows == 16) &&
+              p.tile_order.size() == p.tiles.size() &&
+              (p.unit_rows == 8 || p.unit_rows == 16 || p.unit_rows == 32 || p.unit_rows == 64) &&
               p.vunit_bytes > 0;
   for (size_t i = 0; sane && i < p.tiles.size(); i++) {
     const hm::TileDesc &d = p.tiles[i];

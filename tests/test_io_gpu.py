@@ -59,3 +59,18 @@ def test_damaged_files_are_refused(gpu, tmp_path):
     bad.write_bytes(bytes(flip))
     with pytest.raises(hmgpu.HMGPUError, match="checksum"):
         hmgpu.HMatrix.load(bad)
+
+
+@pytest.mark.parametrize("unit_rows", [32, 64])
+def test_tuned_round_trip(gpu, tmp_path, unit_rows):
+    """A matrix saved after tuning keeps its tuning: every unit size the tuner
+    may choose loads back (near/U units of 8, 16, 32 or 64 rows)."""
+    import torch
+    H = _h("f32", 3000, 5)
+    H.set_tuning(unit_rows, 64, 8, 1)
+    path = tmp_path / "t.hmgpu"
+    H.save(path)
+    G = hmgpu.HMatrix.load(path)
+    assert G.tuning() == H.tuning()
+    x = torch.randn(H.shape[1], device=gpu)
+    assert torch.equal(H * x, G * x)
