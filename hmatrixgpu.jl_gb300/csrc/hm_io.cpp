@@ -3,7 +3,8 @@
 // The file holds the product layout as it lives on the device (plan tables,
 // index maps, tile panels and V rows in the storage precision) plus the block
 // set for the queries, so a load is a few large copies and no ACA. Layout:
-//   "HMGPUH01" | int32 abi, precision, compensated, multi_from | sections |
+//   "HMGPUH01" | int32 file version, precision, compensated, multi_from,
+//   V schedule (1 = tickets) | sections |
 //   uint64 FNV-1a of everything before it
 // where every section is int64 count + count fixed-size records. The tensor-
 // core copy of a mixed-precision matrix is rebuilt on load from the FP32 data.
@@ -20,7 +21,7 @@ using hm::HMatrix;
 namespace {
 
 constexpr char kMagic[8] = {'H', 'M', 'G', 'P', 'U', 'H', '0', '1'};
-constexpr int32_t kFileVersion = 1;  // layout of what follows the magic
+constexpr int32_t kFileVersion = 2;  // layout of what follows the magic
 
 struct Writer {
   FILE *f;
@@ -125,6 +126,7 @@ extern "C" int hmgpu_hmatrix_save(const hmgpu_hmatrix *h, const char *path) {
   w.val(H.opt.precision);
   w.val(H.opt.compensated);
   w.val(static_cast<int32_t>(H.multi_from));
+  w.val(static_cast<int32_t>(H.dp.v_dynamic ? 1 : 0));
   // block set
   w.val(b.m);
   w.val(b.n);
@@ -184,12 +186,13 @@ extern "C" int hmgpu_hmatrix_load(const char *path, hmgpu_hmatrix **out) {
   r.raw(magic, sizeof magic);
   if (!r.ok || std::memcmp(magic, kMagic, sizeof kMagic) != 0)
     return hm::fail(HMGPU_ERR_INVALID, std::string(path) + " is not an hmgpu H-matrix file");
-  int32_t abi = 0, multi_from = 0;
+  int32_t abi = 0, multi_from = 0, v_dynamic = 0;
   auto H = std::make_unique<HMatrix>();
   r.val(abi);
   r.val(H->opt.precision);
   r.val(H->opt.compensated);
   r.val(multi_from);
+  r.val(v_dynamic);
   if (!r.ok || abi != kFileVersion)
     return hm::fail(HMGPU_ERR_INVALID, std::string(path) + ": written in another file version");
   if (H->opt.precision != HMGPU_F64 && H->opt.precision != HMGPU_F32 && H->opt.precision != HMGPU_MIXED)
@@ -304,6 +307,7 @@ extern "C" int hmgpu_hmatrix_load(const char *path, hmgpu_hmatrix **out) {
   r.val(sum);
   if (!r.ok || sum != want) return hm::fail(HMGPU_ERR_INVALID, std::string(path) + ": checksum mismatch");
   if ((rc = hm::upload_plan(*H, tmap0, smap0, zero_row))) return rc;
+  H->dp.v_dynamic = v_dynamic != 0;
   if (H->opt.precision == HMGPU_MIXED && (rc = hm::build_tc(*H))) return rc;
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return hm::cuda_fail(e, "loading an H-matrix");
