@@ -570,9 +570,14 @@ static int check_kernel(const hmgpu_kernel *kd, int64_t m, int64_t n) {
     case HMGPU_KERNEL_LAPLACE3D:
     case HMGPU_KERNEL_YUKAWA:
     case HMGPU_KERNEL_LOG2D:
-    case HMGPU_KERNEL_USER:
       km = kd->nX;
       kn = kd->nY;
+      break;
+    case HMGPU_KERNEL_USER:  // dims entries per point, as the trees have them
+      if (kd->nX <= 0 || kd->nY <= 0 || m % kd->nX != 0 || n % kd->nY != 0)
+        return fail(HMGPU_ERR_INVALID, "a user kernel's rows and columns must be whole multiples of its points");
+      km = m;
+      kn = n;
       break;
     case HMGPU_KERNEL_VECTOR_R:
       km = kd->nX;
@@ -602,9 +607,9 @@ static int check_kernel(const hmgpu_kernel *kd, int64_t m, int64_t n) {
 
 // The kernel's points (or explicit matrix, and a user kernel's parameters) on
 // the device; `uf` the user kernel's entry kernels, or NULL.
-static int upload_kernel(const hmgpu_kernel *kd, int64_t n, DevBuf &dX, DevBuf &dY, DevBuf &dA, DevBuf &dP,
-                         KDev &K, const UserFns *&uf) {
-  K = KDev{kd->kind, nullptr, nullptr, nullptr, kd->lda, nullptr};
+static int upload_kernel(const hmgpu_kernel *kd, int64_t m, int64_t n, DevBuf &dX, DevBuf &dY, DevBuf &dA,
+                         DevBuf &dP, KDev &K, const UserFns *&uf) {
+  K = KDev{kd->kind, nullptr, nullptr, nullptr, kd->lda, nullptr, 1, 1};
   uf = nullptr;
   int rc;
   if (kd->kind == HMGPU_KERNEL_USER) {
@@ -615,6 +620,8 @@ static int upload_kernel(const hmgpu_kernel *kd, int64_t n, DevBuf &dX, DevBuf &
       if (e != cudaSuccess) return cuda_fail(e, "copying the user kernel's parameters");
     }
     K.P = dP.as<double>();
+    K.dx = static_cast<int32_t>(m / kd->nX);
+    K.dy = static_cast<int32_t>(n / kd->nY);
   }
   if (kd->kind == HMGPU_KERNEL_EXPLICIT) {
     if ((rc = dA.alloc(static_cast<size_t>(kd->lda) * n * sizeof(double)))) return rc;
@@ -677,7 +684,7 @@ extern "C" int hmgpu_hmatrix_build(const hmgpu_options *opt, const hmgpu_kernel 
   KDev K;
   const UserFns *uf;
   int rc;
-  if ((rc = upload_kernel(kd, n, dX, dY, dA, dP, K, uf))) return rc;
+  if ((rc = upload_kernel(kd, m, n, dX, dY, dA, dP, K, uf))) return rc;
   {
     std::vector<int32_t> t0v(m), s0v(n);
     for (int64_t i = 0; i < m; i++) t0v[i] = static_cast<int32_t>(X.index_map[i] - 1);
@@ -1054,7 +1061,7 @@ extern "C" int hmgpu_sparsify(const hmgpu_kernel *kd, const hmgpu_tree *Xh, cons
   KDev K;
   const UserFns *uf;
   int rc;
-  if ((rc = upload_kernel(kd, n, dX, dY, dA, dP, K, uf))) return rc;
+  if ((rc = upload_kernel(kd, m, n, dX, dY, dA, dP, K, uf))) return rc;
   {
     std::vector<int32_t> t0v(m), s0v(n);
     for (int64_t i = 0; i < m; i++) t0v[i] = static_cast<int32_t>(X.index_map[i] - 1);

@@ -6,9 +6,10 @@
 // The header is compiled twice: into the library, with the built-in kernels,
 // and at run time by NVRTC for a user's kernel (hmgpu_user_kernel_compile),
 // with HM_USER_ENTRY defined and the user's
-//   __device__ double hmgpu_entry(const double *x, const double *y, const double *p)
+//   __device__ double hmgpu_entry(const double *x, const double *y, const double *p, int a, int b)
 // (target point x, source point y, both 3 coordinates; p the kernel's
-// parameters) placed before it. It therefore includes nothing that NVRTC
+// parameters; a and b the components of a vector or tensor kernel, 0 for a
+// scalar one) placed before it. It therefore includes nothing that NVRTC
 // lacks; under NVRTC the integer types and the HMGPU_KERNEL_* kinds come from
 // a prelude the library writes from its own definitions.
 #pragma once
@@ -33,6 +34,7 @@ struct KDev {
   const double *A;      // explicit matrix, column-major
   int64_t lda;
   const double *P;      // user kernel: its parameters (device)
+  int32_t dx, dy;       // user kernel: entries per target / source point (tree dims)
 };
 
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
@@ -70,7 +72,10 @@ __device__ double dip_xy(double x, double y, double z) {
 __device__ double kentry(const KDev &K, int64_t i, int64_t j) {
 #ifdef HM_USER_ENTRY
   // a user's kernel (kind HMGPU_KERNEL_USER): its function of the two points
-  return hmgpu_entry(K.X + 3 * i, K.Y + 3 * j, K.P);
+  // and the two components (row i is component i mod dx of point i / dx)
+  const int64_t pi = i / K.dx, pj = j / K.dy;
+  return hmgpu_entry(K.X + 3 * pi, K.Y + 3 * pj, K.P, static_cast<int>(i - pi * K.dx),
+                     static_cast<int>(j - pj * K.dy));
 #else
   switch (K.kind) {
     case HMGPU_KERNEL_EXPLICIT:

@@ -183,7 +183,7 @@ extern "C" int hmgpu_user_kernel_compile(const char *source, hmgpu_user_kernel *
   if (log && log_len > 0) log[0] = '\0';
   if (!std::strstr(source, "hmgpu_entry"))
     return fail(HMGPU_ERR_INVALID, "the source must define __device__ double hmgpu_entry(const double *x, "
-                                   "const double *y, const double *p)");
+                                   "const double *y, const double *p, int a, int b)");
   const Nvrtc &nv = nvrtc();
   if (!nv.ok) return fail(HMGPU_ERR_UNSUPPORTED, "the NVRTC library (libnvrtc.so.13) cannot be loaded");
   // the user's lines keep their own numbers in the compiler's messages

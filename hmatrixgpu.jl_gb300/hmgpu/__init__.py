@@ -212,8 +212,10 @@ def SVD_recompress(U, V, eps):
 class UserKernel:
     """A kernel K[i, j] = f(x_i, y_j) of the caller's own: CUDA C++ source that
     defines ``__device__ double hmgpu_entry(const double *x, const double *y,
-    const double *p)`` (target point x, source point y, 3 coordinates each; p
-    the parameters given to Kernel('user', ...)), compiled at run time with
+    const double *p, int a, int b)`` (target point x, source point y, 3
+    coordinates each; p the parameters given to Kernel('user', ...); a, b the
+    components of a vector or tensor kernel over trees with dims 3, 0 for a
+    scalar kernel), compiled at run time with
     NVRTC into the library's ACA+, dense-block and sparsify kernels
     (hmgpu_user_kernel_compile). A compile error raises HMGPUError with the
     compiler's log in ``.log``."""
@@ -260,6 +262,7 @@ class Kernel:
             self.X = _coords(X)
             self.Y = _coords(X if Y is None else Y)
             nx, ny = self.X.shape[1], self.Y.shape[1]
+            # (a user kernel's rows and columns per point come from the trees' dims)
             self.shape = {"vector_r": (nx, 3 * ny), "dipolar": (3 * nx, 3 * ny)}.get(kind, (nx, ny))
             self.A = None
 
@@ -602,7 +605,8 @@ def sparsify_hmatrix(K, X, Y, eta=1.5, triplets=False):
     if triplets:
         return I, J, V
     import scipy.sparse as sp
-    return sp.csc_matrix((V, (I - 1, J - 1)), shape=K.size())
+    shape = (len(X.index_map), len(Y.index_map)) if K.kind == "user" else K.size()
+    return sp.csc_matrix((V, (I - 1, J - 1)), shape=shape)
 
 
 def batch(members):

@@ -65,7 +65,7 @@ KernelDesc(kind, reserved, X, nX, Y, nY, A, lda) =
 A kernel K[i, j] = f(x_i, y_j) of the caller's own, for `HMatrix(uk, ...)`: the
 reference builds an HMatrix from any K it can index (src/hmatrix.jl:183). The
 CUDA C++ `source` defines
-`__device__ double hmgpu_entry(const double *x, const double *y, const double *p)`
+`__device__ double hmgpu_entry(const double *x, const double *y, const double *p, int a, int b)`
 and is compiled at run time (NVRTC) into the library's assembly kernels.
 """
 mutable struct UserKernel

@@ -158,9 +158,12 @@ typedef struct {
  * and hmgpu_sparsify: the reference builds an HMatrix from any K it can index
  * (HMatrix(K, X, Y), src/hmatrix.jl:183,195-196 read K[i, j]). `source` is CUDA
  * C++ that defines
- *   __device__ double hmgpu_entry(const double *x, const double *y, const double *p)
+ *   __device__ double hmgpu_entry(const double *x, const double *y, const double *p, int a, int b)
  * (x the target point and y the source point, 3 coordinates each; p the
- * kernel's parameters, hmgpu_kernel.params). It is compiled with NVRTC for
+ * kernel's parameters, hmgpu_kernel.params; a and b the components of a vector
+ * or tensor kernel: with trees of dims d_x and d_y, row i is component i mod
+ * d_x of target point i / d_x and column j component j mod d_y of source
+ * point j / d_y; 0 for a scalar kernel). It is compiled with NVRTC for
  * sm_103a into the library's own ACA+, dense-block and sparsify kernels,
  * without FMA contraction, like the built-in kernels; the module is loaded on
  * each device at its first use. On failure the compiler's log is copied to

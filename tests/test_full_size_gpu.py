@@ -9,7 +9,8 @@ Size-independent checks:
   * repeatability: two products are bitwise equal;
   * linearity: H(a x + b z) = a H x + b H z to FP64 rounding;
   * precision modes: FP32 within 1e-5 and mixed precision (32 right-hand sides
-    on the tensor cores) within 2e-4 of the FP64 product of the same matrix."""
+    on the tensor cores) within 1e-6 of the FP64 product of the same matrix
+    (the plain FP32 form's error there is about 5.6e-7)."""
 import numpy as np
 import pytest
 
@@ -73,5 +74,5 @@ def test_precision_modes(film, gpu):
     Hm = hmgpu.HMatrix(K, T, T, eta=2.0, eps=1e-4, precision="mixed")
     Ym = Hm * X
     err = ((Ym.double() - Y64).norm(dim=0) / Y64.norm(dim=0)).max()
-    assert float(err) < 2e-4
+    assert float(err) < 1e-6, float(err)
     assert Hm.status() == 0

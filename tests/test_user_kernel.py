@@ -6,7 +6,7 @@ import pytest
 
 import hmgpu
 
-LAPLACE = """__device__ double hmgpu_entry(const double *x, const double *y, const double *p) {
+LAPLACE = """__device__ double hmgpu_entry(const double *x, const double *y, const double *p, int a, int b) {
   double dx = x[0] - y[0], dy = x[1] - y[1], dz = x[2] - y[2];
   double r = sqrt(dx * dx + dy * dy + dz * dz);
   return r == 0.0 ? 0.0 : 0.07957747154594767 / r;
@@ -25,7 +25,7 @@ def test_compiles_and_frees():
 
 
 def test_compile_error_reports_the_users_line():
-    bad = "__device__ double hmgpu_entry(const double *x, const double *y, const double *p) {\n" \
+    bad = "__device__ double hmgpu_entry(const double *x, const double *y, const double *p, int a, int b) {\n" \
           "  return x[0] +* y[0];\n}\n"
     with pytest.raises(hmgpu.HMGPUError) as e:
         hmgpu.UserKernel(bad)

@@ -18,7 +18,7 @@ from tests.test_user_kernel import LAPLACE
 
 pytestmark = pytest.mark.gpu
 
-GAUSS = """__device__ double hmgpu_entry(const double *x, const double *y, const double *p) {
+GAUSS = """__device__ double hmgpu_entry(const double *x, const double *y, const double *p, int a, int b) {
   double dx = x[0] - y[0], dy = x[1] - y[1], dz = x[2] - y[2];
   return exp(-(dx * dx + dy * dy + dz * dz) / (2.0 * p[0] * p[0]));
 }
@@ -86,3 +86,56 @@ def test_bad_user_kernel_arguments(gpu):
     K = hmgpu.Kernel("user", P, user=GAUSS, params=np.ones(65))
     with pytest.raises(hmgpu.HMGPUError, match="parameters"):
         hmgpu.HMatrix(K, T, T, eta=1.5, eps=1e-6)
+
+
+# the demagnetising tensor of the reference's example (examples/hmatrix_vector.jl:12-80),
+# written as a user kernel with the built-in kernel's operation order
+DIPOLAR = """
+__device__ double dxx(double x, double y, double z) {
+  double R = x * x + y * y + z * z;
+  if (R == 0.0) return 0.0;
+  double num = 2.0 * x * x - y * y - z * z;
+  return -num / (R * R * sqrt(R)) / (4.0 * 3.141592653589793);
+}
+__device__ double dxy(double x, double y, double z) {
+  double R = x * x + y * y + z * z;
+  if (R == 0.0) return 0.0;
+  return -3.0 * x * y / (R * R * sqrt(R)) / (4.0 * 3.141592653589793);
+}
+__device__ double hmgpu_entry(const double *p, const double *q, const double *prm, int a, int b) {
+  double x = p[0] - q[0], y = p[1] - q[1], z = p[2] - q[2];
+  switch (a < b ? a * 3 + b : b * 3 + a) {
+    case 0: return dxx(x, y, z);
+    case 1: return dxy(x, y, z);
+    case 2: return dxy(x, z, y);
+    case 4: return dxx(y, x, z);
+    case 5: return dxy(y, z, x);
+    default: return dxx(z, y, x);
+  }
+}
+"""
+
+
+def test_user_tensor_kernel_equals_builtin_dipolar(gpu):
+    """A 3 x 3 block per point pair over trees of dims 3: component a of target
+    point i / 3 is row i, component b of source point j / 3 is column j."""
+    import torch
+    P = geometry.cube(1200, seed=3)
+    T = hmgpu.ClusterTree(P, max_points_per_leaf=16, dims=3)
+    Hu = hmgpu.HMatrix(hmgpu.Kernel("user", P, user=DIPOLAR), T, T, eta=1.0, eps=1e-6, precision="f64",
+                       keep_factors=True)
+    Hb = hmgpu.HMatrix(hmgpu.Kernel("dipolar", P), T, T, eta=1.0, eps=1e-6, precision="f64", keep_factors=True)
+    assert Hu.shape == Hb.shape == (3600, 3600)
+    du, au = Hu.blocks()
+    db, ab = Hb.blocks()
+    np.testing.assert_array_equal(du, db)
+    np.testing.assert_array_equal(au, ab)
+    for b in range(0, len(au), 3):
+        Uu, Vu = Hu.block_factors(b)
+        Ub, Vb = Hb.block_factors(b)
+        np.testing.assert_array_equal(Uu, Ub)
+        np.testing.assert_array_equal(Vu, Vb)
+    x = torch.randn(3600, dtype=torch.float64, device=gpu)
+    assert torch.equal(Hu * x, Hb * x)
+    S = hmgpu.sparsify_hmatrix(hmgpu.Kernel("user", P, user=DIPOLAR), T, T, eta=1.0)
+    assert S.shape == (3600, 3600)
