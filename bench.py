@@ -240,6 +240,74 @@ def bench_config(n):
             "parallelism": "1 GPU"}
 
 
+def film_tight_measurement(dev, steps, hbm, P, T, tol=1e-6):
+    """The headline film at the tighter tolerance the precision case also names
+    (tol 1e-6, same points, tree, leaf 64 and eta 2): the 1-RHS FP32 product
+    (time, algorithmic GB/s, error against the FP64 H-matrix) and 32 RHS plain
+    FP32 against mixed precision, errors against the FP64 product of the same
+    32 vectors."""
+    import torch
+
+    import hmgpu
+    n = P.shape[1]
+    K = hmgpu.Kernel("laplace", P)
+    t0 = time.time()
+    H = hmgpu.HMatrix(K, T, T, eta=ETA, eps=tol, precision="f32")
+    torch.cuda.synchronize()
+    build = time.time() - t0
+    tune = H.autotune()
+    inf = H.info()
+    g = torch.Generator(dev).manual_seed(21)
+    x = torch.randn(n, device=dev, generator=g)
+    X = torch.randn(32, n, device=dev, generator=g).t()
+    H64 = hmgpu.HMatrix(K, T, T, eta=ETA, eps=tol, precision="f64")
+    y64 = H64 * x.double()
+    Y64 = torch.empty(32, n, dtype=torch.float64, device=dev).t()
+    hmgpu.mul_(Y64, H64, X.double())
+    del H64
+    y = torch.empty(n, device=dev)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        hmgpu.mul_(y, H, x)
+    reps = max(10, min(steps, 200))
+    torch.cuda.synchronize()
+    s.record()
+    for _ in range(reps):
+        hmgpu.mul_(y, H, x)
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / reps
+    err1 = float(torch.linalg.norm(y.double() - y64) / torch.linalg.norm(y64))
+    alg = 4 * (inf["dense_entries"] + inf["far_entries"] + 2 * n + 2 * inf["total_rank"])
+    out = {"workload": f"film-{GRID}x{GRID} Laplace leaf{LEAF} eta{ETA:g} tol{tol:g}",
+           "build_seconds": build, "autotuned": tune, "dense_entries": inf["dense_entries"],
+           "far_entries": inf["far_entries"], "max_rank": inf["max_rank"],
+           "f32_1rhs": {"ms_per_product": ms, "matvec_per_s": 1e3 / ms, "hbm_gbs": alg / (ms * 1e-3) / 1e9,
+                        "frac_of_measured": alg / (ms * 1e-3) / 1e9 / hbm, "rel_err_vs_fp64_hmatrix": err1}}
+    Hm = hmgpu.HMatrix(K, T, T, eta=ETA, eps=tol, precision="mixed")
+    Y = torch.empty(32, n, device=dev).t()
+    rhs = {"errors": "max over the 32 columns of ||y - y64|| / ||y64||"}
+    for name, HH in (("plain_f32", H), ("mixed_tensor_cores", Hm)):
+        for _ in range(3):
+            hmgpu.mul_(Y, HH, X)
+        r32 = max(5, min(steps // 10, 30))
+        torch.cuda.synchronize()
+        s.record()
+        for _ in range(r32):
+            hmgpu.mul_(Y, HH, X)
+        e.record()
+        torch.cuda.synchronize()
+        t32 = s.elapsed_time(e) / r32
+        err = float(((Y.double() - Y64).norm(dim=0) / Y64.norm(dim=0)).max())
+        rhs[name] = {"ms_per_32rhs_product": t32, "matvec_per_s": 32e3 / t32, "rel_err": err}
+    rhs["mixed_speedup_vs_plain_f32"] = rhs["plain_f32"]["ms_per_32rhs_product"] / \
+        rhs["mixed_tensor_cores"]["ms_per_32rhs_product"]
+    out["rhs32"] = rhs
+    del Hm, H
+    torch.cuda.empty_cache()
+    return out
+
+
 def cube_measurement(dev, steps, hbm, npts=1 << 18):
     """The plain drop-in case: N = 2^18 points uniform in [0,1]^3, Laplace
     1/(4 pi r), leaf 64, eta 2, tol 1e-6, FP32 storage, one RHS. Device build
@@ -653,6 +721,7 @@ def run_gpu(args):
     achieved = du_bytes / (du_ms * 1e-3) / 1e9
     batch32 = None if args.skip_batch else batch_measurement(dev, args.steps)
     cube18 = None if args.skip_cube else cube_measurement(dev, args.steps, hbm, args.cube_points)
+    film_tight = None if args.skip_film_tight else film_tight_measurement(dev, args.steps, hbm, P, T)
     learned = learned_measurement(dev) if args.learned else None
     cores = os.cpu_count() or 1
     cpu_runs, cpu_desc = cpu_product([(1, 1, 4)] + ([(cores, 3, 10)] if cores > 1 else []))
@@ -689,6 +758,7 @@ def run_gpu(args):
         "rhs32": rhs32,
         "batch32": batch32,
         "cube18": cube18,
+        "film_tol1e-6": film_tight,
         "learned_cube20": learned,
         "clocks": clk.summary(),
     }
@@ -708,6 +778,7 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="leave out the 32-H-matrix batch lines")
     ap.add_argument("--build-only", action="store_true", help="assemble the workload, print its build line, exit")
     ap.add_argument("--skip-cube", action="store_true", help="leave out the 2^18-cube tol 1e-6 line")
+    ap.add_argument("--skip-film-tight", action="store_true", help="leave out the film tol 1e-6 line")
     ap.add_argument("--cube-points", type=int, default=1 << 18,
                     help="points of the cube case (2^18 = the plain drop-in workload; smaller for profiling captures)")
     ap.add_argument("--learned", action="store_true",
