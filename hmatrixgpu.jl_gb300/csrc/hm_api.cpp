@@ -197,6 +197,17 @@ int finalize_layout(HMatrix &H, const double *d64, const std::vector<int64_t> &d
   H.build_phase[5] = clk.lap();
   if (H.opt.precision == HMGPU_MIXED) {
     rc = build_tc(H);
+    if (rc == HMGPU_OK && H.opt.lean) {
+      // only the FP16 pairs stay: the FP32 panels, V rows and single-RHS XT go
+      const size_t es = 4;
+      H.dfree(H.panels);
+      H.dfree(H.vdata);
+      H.dfree(H.xt);
+      H.device_bytes -= static_cast<int64_t>((H.plan.panel_len + H.plan.v_len + H.plan.xt_len) * es);
+      H.panels = H.vdata = H.xt = nullptr;
+      H.lean = true;
+      H.multi_from = 1;  // every product on the tensor cores
+    }
     H.build_phase[6] = clk.lap();
     return rc;
   }
@@ -626,7 +637,7 @@ extern "C" int hmgpu_hmatrix_info(const hmgpu_hmatrix *h, hmgpu_info *info) {
   double comp = static_cast<double>(H.plan.dense_entries + H.plan.far_entries);
   info->compression_ratio = comp > 0 ? static_cast<double>(b.m) * b.n / comp : 0.0;
   const int64_t es = H.opt.precision == HMGPU_F64 ? 8 : 4;
-  info->matrix_bytes = (H.plan.panel_len + H.plan.v_len) * es;
+  info->matrix_bytes = H.lean ? H.tc_bytes : (H.plan.panel_len + H.plan.v_len) * es;
   info->device_bytes = H.device_bytes;
   info->n_tiles = static_cast<int64_t>(H.plan.tiles.size());
   info->precision = H.opt.precision;

@@ -52,6 +52,7 @@ struct HMatrix {
   double build_phase[HMGPU_BUILD_PHASES] = {};  // see hmgpu_hmatrix_build_profile
   int64_t aca_batches = 0, aca_reruns = 0, aca_ws_bytes = 0, aca_continued = 0;
   int64_t device_bytes = 0;
+  bool lean = false;  // HMGPU_MIXED with only the tensor-core copy (options.lean)
   std::vector<void *> dev_allocs;
   // batches: first row and first column of every member, then m and n (empty
   // outside batches)

@@ -32,6 +32,7 @@ extern "C" int hmgpu_hmatrix_batch(hmgpu_hmatrix *const *members, int32_t count,
     if (!members[k]) return hm::fail(HMGPU_ERR_INVALID, "member " + std::to_string(k) + " is NULL");
     M[k] = reinterpret_cast<const HMatrix *>(members[k]);
     if (M[k]->is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard cannot be a batch member");
+    if (M[k]->lean) return hm::fail(HMGPU_ERR_INVALID, "a lean mixed H-matrix keeps only its tensor-core copy; a batch is built from the FP32 layouts");
   }
   int dev = 0;
   cudaGetDevice(&dev);
@@ -254,6 +255,13 @@ extern "C" int hmgpu_hmatrix_autotune(hmgpu_hmatrix *h, const char *cache_path, 
   if (!h) return hm::fail(HMGPU_ERR_INVALID, "H is NULL");
   HMatrix &H = *reinterpret_cast<HMatrix *>(h);
   if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard multiplies through hmgpu_matvec_shard only");
+  if (H.lean) {  // only the tensor-core pass, which has nothing to tune
+    if (result) {
+      const int32_t cur[4] = {H.plan.unit_rows, static_cast<int32_t>(H.plan.vunit_bytes / 1024), H.multi_from, 0};
+      std::copy(cur, cur + 4, result);
+    }
+    return HMGPU_OK;
+  }
   const uint64_t key = structure_hash(H);
   int32_t best[4];
   if (cache_lookup(cache_path, key, best)) {
@@ -357,5 +365,6 @@ extern "C" int hmgpu_hmatrix_set_tuning(hmgpu_hmatrix *h, const int32_t *v, int3
   if ((v[0] != 8 && v[0] != 16 && v[0] != 32 && v[0] != 64) || (v[1] != 32 && v[1] != 64 && v[1] != 128) || v[2] < 2 || (v[3] != 0 && v[3] != 1))
     return hm::fail(HMGPU_ERR_INVALID, "tuning values out of range (unit rows 8|16|32|64, V unit KiB 32|64|128, "
                                        "multi-RHS threshold >= 2, V schedule 0|1)");
+  if (H.lean) return hm::fail(HMGPU_ERR_INVALID, "a lean mixed H-matrix keeps only its tensor-core copy: every product runs on the tensor cores");
   return apply(H, v[0], v[1], v[2], v[3]);
 }

@@ -111,6 +111,8 @@ extern "C" int hmgpu_hmatrix_save(const hmgpu_hmatrix *h, const char *path) {
   if (!h || !path) return hm::fail(HMGPU_ERR_INVALID, "NULL argument");
   const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);
   if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard has no file form; save the whole H-matrix");
+  if (H.lean)
+    return hm::fail(HMGPU_ERR_INVALID, "a lean mixed H-matrix keeps only its tensor-core copy, and a file holds the FP32 layout it is packed from");
   const hm::Plan &p = H.plan;
   const hm::BlockSet &b = H.bs;
   const int64_t es = H.opt.precision == HMGPU_F64 ? 8 : 4;

@@ -48,6 +48,7 @@ extern "C" int hmgpu_matvec_noalloc(hmgpu_hmatrix *h, const void *x, void *y, vo
   if (!x || !y) return hm::fail(HMGPU_ERR_INVALID, "x or y is NULL");
   hm::HMatrix &H = *reinterpret_cast<hm::HMatrix *>(h);
   if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "a shard multiplies through hmgpu_matvec_shard only");
+  if (H.lean) return hm::fail(HMGPU_ERR_INVALID, "a lean mixed H-matrix keeps only its tensor-core copy; this entry runs the FP32 single-RHS kernels");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return hm::cuda_fail(e, "cudaGetDevice");

@@ -146,6 +146,7 @@ extern "C" int hmgpu_hmatrix_shard(const hmgpu_hmatrix *h, int32_t rank, int32_t
   *out = nullptr;
   const HMatrix &H = *reinterpret_cast<const HMatrix *>(h);
   if (H.is_shard) return hm::fail(HMGPU_ERR_INVALID, "H is itself a shard");
+  if (H.lean) return hm::fail(HMGPU_ERR_INVALID, "a lean mixed H-matrix keeps only its tensor-core copy; shards take the FP32 layout");
   if (world < 1 || rank < 0 || rank >= world) return hm::fail(HMGPU_ERR_INVALID, "need 0 <= rank < world");
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);

@@ -287,11 +287,12 @@ class Kernel:
         return self.shape
 
 
-def _opts(precision, compensated, keep_factors, rank_model=None):
+def _opts(precision, compensated, keep_factors, rank_model=None, lean=False):
     o = Options()
     o.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.compensated = int(bool(compensated))
     o.keep_factors = int(bool(keep_factors))
+    o.lean = int(bool(lean))
     o.rank_model = rank_model._h if rank_model is not None else None
     return o
 
@@ -359,10 +360,12 @@ class RankModel:
 
 class HMatrix:
     """HMatrix(K, X, Y; eta=1.5, eps=1e-5, svd_recompress=True) (src/hmatrix.jl:72-148),
-    assembled on the device, stored in `precision` ('f64', 'f32' or 'mixed')."""
+    assembled on the device, stored in `precision` ('f64', 'f32' or 'mixed');
+    with 'mixed', lean=True keeps only the tensor-core copy (half the memory;
+    every product on the tensor cores)."""
 
     def __init__(self, K, X, Y, eta=1.5, eps=1e-5, svd_recompress=True, precision="f64",
-                 compensated=False, keep_factors=False, rank_model=None, _handle=None):
+                 compensated=False, keep_factors=False, rank_model=None, lean=False, _handle=None):
         self._h = None
         if _handle is not None:
             self._h = _handle
@@ -370,7 +373,7 @@ class HMatrix:
             if not isinstance(K, Kernel):
                 K = Kernel("explicit", A=K)
             self.K = K
-            o = _opts(precision, compensated, keep_factors, rank_model)
+            o = _opts(precision, compensated, keep_factors, rank_model, lean)
             h = C.c_void_p()
             d = K.desc()
             check(lib().hmgpu_hmatrix_build(C.byref(o), C.byref(d), X._h, Y._h, float(eta),
@@ -381,7 +384,7 @@ class HMatrix:
     @classmethod
     def from_flat(cls, m, n, target_index_map, source_index_map, dense_block_indices, dense_blocks,
                   U_block_indices, U_matrices, V_block_indices, V_matrices, precision="f64",
-                  compensated=False, keep_factors=False):
+                  compensated=False, keep_factors=False, lean=False):
         """Imports the reference's flattened HMatrix{Float64} fields
         (src/hmatrix.jl:46-57): index tables as (nblocks, 5) / (R, 3) arrays of
         the 1-based Julia columns."""
@@ -390,7 +393,7 @@ class HMatrix:
         tm, sm = a64(target_index_map), a64(source_index_map)
         di, ui, vi = a64(dense_block_indices), a64(U_block_indices), a64(V_block_indices)
         dd, ud, vd = f64(dense_blocks), f64(U_matrices), f64(V_matrices)
-        o = _opts(precision, compensated, keep_factors)
+        o = _opts(precision, compensated, keep_factors, lean=lean)
         h = C.c_void_p()
         check(lib().hmgpu_hmatrix_import_flat(
             C.byref(o), m, n, ptr(tm, I64P), ptr(sm, I64P), ptr(di, I64P), di.shape[0] if di.size else 0,

@@ -30,7 +30,7 @@ class HMGPUError(RuntimeError):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("compensated", C.c_int32),
-                ("keep_factors", C.c_int32), ("reserved", C.c_int32), ("rank_model", C.c_void_p)]
+                ("keep_factors", C.c_int32), ("lean", C.c_int32), ("rank_model", C.c_void_p)]
 
 
 class KernelDesc(C.Structure):

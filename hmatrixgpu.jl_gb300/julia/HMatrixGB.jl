@@ -37,11 +37,11 @@ struct Options            # hmgpu_options
     precision::Int32
     compensated::Int32
     keep_factors::Int32
-    reserved::Int32
+    lean::Int32            # mixed precision: 1 = keep only the tensor-core copy
     rank_model::Ptr{Cvoid} # const hmgpu_rank_model* (C_NULL: fixed ACA workspace)
 end
-Options(precision, compensated, keep_factors, reserved) =
-    Options(precision, compensated, keep_factors, reserved, C_NULL)
+Options(precision, compensated, keep_factors, lean) =
+    Options(precision, compensated, keep_factors, lean, C_NULL)
 
 struct KernelDesc
     kind::Int32

@@ -132,7 +132,13 @@ typedef struct {
   int32_t precision;   /* HMGPU_F64, HMGPU_F32 or HMGPU_MIXED                     */
   int32_t compensated; /* FP32 modes: 1 = compensated (Dot2) accumulation        */
   int32_t keep_factors;/* 1 = keep the FP64 block factors for export             */
-  int32_t reserved;
+  int32_t lean;        /* HMGPU_MIXED: 1 = keep only the tensor-core copy (FP16
+                          pairs): the FP32 layout is freed once the copy is
+                          packed, halving the matrix's memory; every product,
+                          1 and 2 right-hand sides too, runs on the tensor
+                          cores. A lean H-matrix cannot be saved, sharded,
+                          batched or used by hmgpu_matvec_noalloc; autotuning
+                          leaves it as it is.                                */
   /* Optional learned rank predictor (see below): when set, hmgpu_hmatrix_build
    * sizes each admissible block's ACA workspace from the predicted rank and
    * batches blocks of similar predicted rank together; blocks that need more
