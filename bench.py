@@ -697,7 +697,28 @@ def run_gpu(args):
             rhs32[name] = {"ms_per_32rhs_product": t32, "matvec_per_s": 32e3 / t32, "rel_err": err}
         rhs32["mixed_speedup_vs_plain_f32"] = rhs32["plain_f32"]["ms_per_32rhs_product"] / \
             rhs32["mixed_tensor_cores"]["ms_per_32rhs_product"]
+        rhs32["mixed_device_gb"] = Hm.info()["device_bytes"] / 1e9
         del Hm
+        # lean mixed: only the tensor-core copy on the device; 1 RHS runs on
+        # the tensor cores as well (error of the first column against FP64)
+        Hl = hmgpu.HMatrix(hmgpu.Kernel("laplace", P), T, T, eta=ETA, eps=TOL, precision="mixed", lean=True)
+        lean = {"device_gb": Hl.info()["device_bytes"] / 1e9}
+        x1, y1 = X[:, 0].contiguous(), torch.empty(n, device=dev)
+        for name, xx, yy in (("1rhs", x1, y1), ("32rhs", X, Y)):
+            for _ in range(3):
+                hmgpu.mul_(yy, Hl, xx)
+            reps = max(5, min(args.steps // 10, 50))
+            torch.cuda.synchronize()
+            s.record(stream)
+            for _ in range(reps):
+                hmgpu.mul_(yy, Hl, xx)
+            e.record(stream)
+            torch.cuda.synchronize()
+            yv = yy.reshape(n, -1).double()
+            lean["ms_" + name] = s.elapsed_time(e) / reps
+            lean["rel_err_" + name] = float(((yv - Y64[:, :yv.shape[1]]).norm(dim=0) / Y64[:, :yv.shape[1]].norm(dim=0)).max())
+        rhs32["mixed_lean"] = lean
+        del Hl
     else:
         del H64
 
