@@ -238,6 +238,9 @@ class UserKernel:
             self._h = None
 
 
+_USER_KERNELS = {}  # source -> UserKernel compiled from it
+
+
 class Kernel:
     """A matrix K generated on the device: kind in {'laplace', 'yukawa', 'log2d',
     'vector_r', 'dipolar'} over target points X and source points Y (3 x N),
@@ -253,7 +256,11 @@ class Kernel:
         if kind == "user":
             if user is None:
                 raise ValueError("a 'user' kernel needs user= (a UserKernel or its source)")
-            self.user = user if isinstance(user, UserKernel) else UserKernel(user)
+            if not isinstance(user, UserKernel):  # one compilation per source
+                if user not in _USER_KERNELS:
+                    _USER_KERNELS[user] = UserKernel(user)
+                user = _USER_KERNELS[user]
+            self.user = user
         if kind == "explicit":
             self.A = np.asfortranarray(A, dtype=np.float64)
             self.X = self.Y = None
